@@ -1,0 +1,336 @@
+"""Benchmark: frames oriented per second on one GB300.
+
+Workload (the plain-FP32-at-scale configuration): a 81^3 float32 model,
+4 x 128 x 128 = 65,536-pixel frames, 100,000 reference orientations sliced by
+the type-2 NUFFT at eps 1e-6 and kept resident on the device, 10,000 Poisson
+frames (mean 0.5 photons/pixel, uint16 counts).  One step = orient every
+frame: distance to every reference + best index (the BF16 tensor-core path
+with top-8 FP32 re-rank when available, else the plain FP32 path).
+
+value : frames/s with frames and references resident in HBM;
+e2e   : frames/s through the host API: uint16 frames copied from pinned host
+        memory, matched, indices copied back, every step;
+roofline: the dominant kernel's achieved TFLOP/s (2 * n_pix * n_ref per frame)
+        against the measured peak;
+cpu_baseline: the oracle's numpy FP64 GEMM-form distance + argmin (what the
+        reference's CPU branch computes) on a bounded sample, on the host cores.
+
+`--impl reference` times that CPU implementation alone as the reference arm.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="om-plain-fp32-at-scale", M=81, panels=4, nx=128, ny=128, n_ref=100_000,
+                n_img=10_000, photons=0.5, eps=1e-6, seed=20261203)
+METRIC = "frames oriented/s: BF16-TC+rerank vs plain FP32 @ same argmin; p50/p99 latency"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d, "measured"
+    return dict(PEAKS_FALLBACK), "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if s[4 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(n_pix: int, n_ref_full: int, n_img_s=64, n_ref_s=10_000, seed=5, reps=1):
+    """Oracle numpy FP64 GEMM-form distance + argmin on a bounded sample."""
+    from oracle import matching as om
+
+    rng = np.random.default_rng(seed)
+    refs = rng.random((n_ref_s, n_pix))
+    imgs = rng.poisson(0.5, (n_img_s, n_pix)).astype(np.float64)
+    om.sklearn_argmin(refs[:16], imgs[:4])  # warm BLAS
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        om.sklearn_argmin(refs, imgs)
+    dt = (time.perf_counter() - t0) / reps
+    # frames/s against the full reference set: time scales with n_ref
+    fps = n_img_s / (dt * n_ref_full / n_ref_s)
+    return {"value": fps, "unit": "frames/s", "cores": cpu_threads(), "kind": "port",
+            "sample": f"{n_img_s} frames x {n_ref_s} refs x {n_pix} px in FP64 numpy BLAS "
+                      f"({dt:.2f} s), scaled to {n_ref_full} refs"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    W = WORKLOAD
+    n_pix = W["panels"] * W["nx"] * W["ny"]
+    vals = []
+    for _ in range(max(args.warmup, 0)):
+        cpu_baseline(n_pix, W["n_ref"], n_img_s=16, n_ref_s=2000)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(n_pix, W["n_ref"], n_img_s=32, n_ref_s=5000))
+    v = float(np.median([x["value"] for x in vals]))
+    cb = dict(vals[0])
+    cb["value"] = v
+    out = {"metric": METRIC, "impl": "reference", "value": v, "unit": "frames/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1000.0 * W["n_img"] / v,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "config": config_dict(W),
+           "cpu_baseline": cb,
+           "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def config_dict(W):
+    return {"workload": W["name"], "model_grid": W["M"], "n_pix": W["panels"] * W["nx"] * W["ny"],
+            "n_ref": W["n_ref"], "n_img": W["n_img"], "eps": W["eps"],
+            "l2": "inputs larger than L2 (26 GB resident references)",
+            "parallelism": "replicas (frames sharded, references replicated)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n-ref", type=int, default=None, help="override (testing only)")
+    ap.add_argument("--n-img", type=int, default=None, help="override (testing only)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    from spinifel_gb300 import _lib, geom, matching, synth
+    from spinifel_gb300.nufft import NufftPlan
+
+    W = dict(WORKLOAD)
+    if args.n_ref:
+        W["n_ref"] = args.n_ref
+    if args.n_img:
+        W["n_img"] = args.n_img
+    n_pix = W["panels"] * W["nx"] * W["ny"]
+    rng = np.random.default_rng(W["seed"])
+    model = synth.intensity_model(W["M"], seed=W["seed"], dtype=np.float32)
+    ppr, pdr = geom.flat_detector(W["panels"], W["nx"], W["ny"])
+    mult = float(np.pi / pdr.max())
+    ppr_t = torch.as_tensor(ppr.reshape(3, -1), dtype=torch.float32, device=dev)
+    ref_q = torch.as_tensor(geom.uniform_quaternions(W["n_ref"], rng), dtype=torch.float32,
+                            device=dev)
+    img_rng = np.random.default_rng(W["seed"] + 1 + rank)
+    img_q = torch.as_tensor(geom.uniform_quaternions(W["n_img"], img_rng), dtype=torch.float32,
+                            device=dev)
+
+    plan = NufftPlan(W["M"], W["eps"])
+    plan.set_modes(torch.as_tensor(model, device=dev))
+
+    # --- slicing: all references resident (timed separately) ---------------
+    refs = torch.empty(W["n_ref"], n_pix, dtype=torch.float32, device=dev)
+    B = 5000
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for st in range(0, W["n_ref"], B):
+        plan.slice(ref_q[st:st + B], ppr_t, mult, out=refs[st:st + B])
+    e1.record()
+    barrier()
+    slice_ms = e0.elapsed_time(e1)
+    refs_sq = matching.row_sqnorm(refs)
+
+    # --- frames: Poisson counts of slices at other orientations -------------
+    imgs_f = torch.empty(W["n_img"], n_pix, dtype=torch.float32, device=dev)
+    for st in range(0, W["n_img"], B):
+        plan.slice(img_q[st:st + B], ppr_t, mult, out=imgs_f[st:st + B])
+    lam = imgs_f.clamp_min_(0)
+    lam *= W["photons"] / lam.mean()
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(W["seed"] + 17 + rank)
+    counts = torch.poisson(lam, generator=gen).clamp_(max=65535)
+    # uint16 counts on the host (stored in an int16 tensor: same bytes)
+    c32 = counts.to(torch.int32)
+    imgs_u16_host = torch.where(c32 > 32767, c32 - 65536, c32).to(torch.int16).cpu().pin_memory()
+    imgs = counts.float().contiguous()
+    del c32
+    del lam, counts, imgs_f
+    # SNM scales the references by the std ratio (orientation_matching.py:165)
+    refs *= (imgs.double().std() / refs.double().std()).float()
+    refs_sq = matching.row_sqnorm(refs)
+
+    def step_plain(x):
+        return matching.argmin_fp32(x, refs, refs_sq=refs_sq)
+
+    step = step_plain
+    path = "plain-fp32"
+
+    # --- device-resident timing ---------------------------------------------
+    for _ in range(args.warmup):
+        step(imgs)
+    barrier()
+    l0 = _lib.launch_count()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        t0.record()
+        for _ in range(args.steps):
+            idx, _ = step(imgs)
+        t1.record()
+        barrier()
+    launches = (_lib.launch_count() - l0)
+    ms = t0.elapsed_time(t1) / args.steps
+    ms_t = torch.tensor([ms], device=dev)
+    if world > 1:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    value = W["n_img"] * world / (ms / 1e3)
+
+    # --- dominant kernel alone (CUDA events on its stream) ------------------
+    isq = matching.row_sqnorm(imgs)
+    tr = matching.BestTracker(W["n_img"], dev)
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0.record()
+    tr.update_fp32(imgs, isq, refs, refs_sq, 0)
+    k1.record()
+    torch.cuda.synchronize()
+    k_ms = k0.elapsed_time(k1)
+    flops = 2.0 * W["n_img"] * W["n_ref"] * n_pix
+    peaks, peak_src = load_peaks()
+    sm_clock = 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_clock * 1e6 / 1e12  # nominal SIMT FP32 at max clock
+    roofline = {"bound": "fp32-simt", "achieved": flops / (k_ms / 1e3) / 1e12,
+                "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": flops / (k_ms / 1e3) / 1e12 / fp32_peak, "traffic": None,
+                "kernel": "k_dist_argmin_f32", "peak_source": "nominal (152 SM x 128 FMA x 2 "
+                "x 2070 MHz); measured peaks cover HBM and bf16 only"}
+
+    # --- end to end through the host API ------------------------------------
+    out_host = torch.empty(W["n_img"], dtype=torch.int32).pin_memory()
+
+    u16_dev = torch.empty_like(imgs_u16_host, device=dev)
+    x_dev = torch.empty(W["n_img"], n_pix, dtype=torch.float32, device=dev)
+
+    def e2e_step():
+        u16_dev.copy_(imgs_u16_host, non_blocking=True)
+        matching.ingest_u16(u16_dev, x_dev)
+        i, _ = step(x_dev)
+        out_host.copy_(i, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    t0.record()
+    for _ in range(args.steps):
+        e2e_step()
+    t1.record()
+    barrier()
+    e2e_ms = t0.elapsed_time(t1) / args.steps
+    e2e = {"value": W["n_img"] * world / (e2e_ms / 1e3), "unit": "frames/s",
+           "h2d_bytes_per_step": int(imgs_u16_host.numel() * 2),
+           "d2h_bytes_per_step": int(out_host.numel() * 4)}
+
+    cb = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cb = cpu_baseline(n_pix, W["n_ref"])
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f32" if path == "plain-fp32" else "bf16", "data": "synthetic",
+               "config": config_dict(W), "path": path,
+               "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
+               "gpu_launches": int(launches), "clocks": clk.summary(),
+               "slicing": {"ms_all_refs": slice_ms,
+                           "points_per_s": W["n_ref"] * n_pix / (slice_ms / 1e3)},
+               "peaks_source": peak_src}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

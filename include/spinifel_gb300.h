@@ -1,0 +1,151 @@
+/*
+ * spinifel_gb300 -- C ABI of the GB300 (sm_103a) orientation-matching and
+ * 3D NUFFT library (libspinifel_gb300.so).
+ *
+ * Every entry point takes plain pointers and 64-bit sizes, runs on the CUDA
+ * stream it is given (cudaStream_t passed as void*; NULL = legacy default
+ * stream), never synchronises unless it says so, and returns an int status:
+ *   SPF_OK (0) or a negative SPF_ERR_* code.  spf_last_error() returns a
+ * thread-local message for the last failure on the calling thread.
+ * Device pointers ("d_") must point to device memory of the current device;
+ * host pointers ("h_") to host memory (pinned for asynchronous copies).
+ *
+ * Functions that replace a reference interface cite it as path:line within
+ * the spinifel project.
+ */
+#ifndef SPINIFEL_GB300_H
+#define SPINIFEL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPF_OK 0
+#define SPF_ERR_ARG (-1)        /* bad argument (size, pointer, alignment)   */
+#define SPF_ERR_OOM (-2)        /* device allocation failed                  */
+#define SPF_ERR_TIMEOUT (-3)    /* a bounded device wait gave up             */
+#define SPF_ERR_LAUNCH (-4)     /* kernel launch failed                      */
+#define SPF_ERR_CUDA (-5)       /* other CUDA runtime / cuFFT error          */
+#define SPF_ERR_UNSUPPORTED (-6) /* device or shape not supported            */
+
+typedef struct spf_nufft_plan_s *spf_nufft_plan;
+
+/* ---- library ---------------------------------------------------------- */
+const char *spf_version(void);
+const char *spf_status_string(int status);
+const char *spf_last_error(void);
+/* Number of kernels this library has launched in this process (all entry
+ * points, all devices).  Used to count launches inside a timed region. */
+uint64_t spf_launch_count(void);
+/* Device-side error word written by bounded waits (0 = none); reset to 0. */
+int spf_device_error(void *stream, int *h_code);
+
+/* ---- NUFFT plan ---------------------------------------------------------
+ * Replaces the cufinufft / finufft plans built in
+ * spinifel/extern/nufft_ext.py:271-280 (type 2) and :308-319 (type 1).
+ * Modes k = -floor(m/2) .. ceil(m/2)-1 on each axis of a C-ordered
+ * (m1, m2, m3) array; the first coordinate runs along axis 0 (the reference
+ * passes (L, K, H) to the Fortran-ordered library, cufinufft_ext.py:120-122).
+ * eps selects the exponential-of-semicircle width (w = ceil(-log10(eps/10))
+ * at upsampfac 2); upsampfac <= 0 selects 2.0. */
+int spf_nufft_plan_create(int m1, int m2, int m3, double eps, double upsampfac,
+                          spf_nufft_plan *out);
+int spf_nufft_plan_destroy(spf_nufft_plan plan);
+/* n_fine[3], kernel width, beta, padded fine-grid dims[3] */
+int spf_nufft_plan_info(spf_nufft_plan plan, int *n_fine, int *width, double *beta,
+                        int *n_padded);
+
+/* Type 2 set-up: real modes d_modes (m1*m2*m3 float, C order), optionally
+ * multiplied by d_support (same shape, NULL = none), deconvolved, FFT'd to
+ * the fine grid; keeps Re (and Im when want_imag) of the fine grid in the
+ * plan.  isign = -1 as in spinifel/extern/nufft_ext.py:63. */
+int spf_nufft_t2_set_modes(spf_nufft_plan plan, const float *d_modes,
+                           const float *d_support, int isign, int want_imag,
+                           void *stream);
+
+/* Type 2 at explicit points (radians, |x| < 3 pi): c_j real (and imaginary)
+ * parts.  Replaces nufft_3d_t2 (spinifel/autocorrelation.py:59,
+ * spinifel/extern/cufinufft_ext.py:384-) for real modes. */
+int spf_nufft_t2_interp(spf_nufft_plan plan, const float *d_x, const float *d_y,
+                        const float *d_z, int64_t npts, float *d_out_re,
+                        float *d_out_im, void *stream);
+
+/* Fused slicing (type 2 with coordinates made in the kernel): for each
+ * orientation o (quaternion [w,x,y,z], d_quats[4*o]) and pixel p
+ * (d_ppr = pixel_position_reciprocal, 3 x n_pix, float), the point
+ * scale * R(q_o)^-1 . ppr[:,p] is evaluated; d_out[o*n_pix + p] = Re c.
+ * scale = pi / (oversampling * max |q|).  Replaces NUFFT.forward
+ * (spinifel/extern/nufft_ext.py:248-284) together with the host-side
+ * HKL precompute it reads (nufft_ext.py:136-144).  When d_out_bf16 is not
+ * NULL the same values are also written there rounded to bf16. */
+int spf_slice_t2(spf_nufft_plan plan, const float *d_quats, int64_t n_orient,
+                 const float *d_ppr, int64_t n_pix, double scale, float *d_out,
+                 void *d_out_bf16, void *stream);
+
+/* Type 1: zero the plan's fine grid, spread real strengths, then FFT and
+ * deconvolve onto the (m1, m2, m3) modes.  isign as in the caller
+ * (+1 in spinifel/autocorrelation.py:118, -1 in nufft_ext.py:316).
+ * d_out_re/d_out_im receive m1*m2*m3 floats (d_out_im may be NULL). */
+int spf_nufft_t1_zero(spf_nufft_plan plan, void *stream);
+int spf_nufft_t1_spread(spf_nufft_plan plan, const float *d_x, const float *d_y,
+                        const float *d_z, const float *d_c, int64_t npts,
+                        void *stream);
+int spf_nufft_t1_spread_orient(spf_nufft_plan plan, const float *d_quats,
+                               int64_t n_orient, const float *d_ppr, int64_t n_pix,
+                               double scale, const float *d_c, void *stream);
+int spf_nufft_t1_finish(spf_nufft_plan plan, int isign, float *d_out_re,
+                        float *d_out_im, void *stream);
+
+/* ---- orientation matching --------------------------------------------- */
+
+/* pyCudaKNearestNeighbors.cudaEuclideanDistance
+ * (spinifel/sequential/orientation_matching_sp.cu:612-680): d_out[d*n_ref+r]
+ * = sum over the first 16*floor(n_pix/16) pixels of (data - ref)^2.
+ * f32 and f64 variants (the _SP and _DP modules). */
+int spf_knn_eudist_f32(const float *d_ref, const float *d_data, int64_t n_ref,
+                       int64_t n_data, int64_t n_pix, float *d_out, void *stream);
+int spf_knn_eudist_f64(const double *d_ref, const double *d_data, int64_t n_ref,
+                       int64_t n_data, int64_t n_pix, double *d_out, void *stream);
+
+/* pyCudaKNearestNeighbors.cudaHeapSort (orientation_matching_sp.cu:682-730):
+ * the k smallest entries of each row of d_dist [n_data][n_ref], ascending,
+ * indices written to d_idx [n_data][k]; ties go to the lower index.
+ * k <= 32. */
+int spf_knn_topk_f32(const float *d_dist, int64_t n_data, int64_t n_ref, int k,
+                     int32_t *d_idx, void *stream);
+int spf_knn_topk_f64(const double *d_dist, int64_t n_data, int64_t n_ref, int k,
+                     int32_t *d_idx, void *stream);
+
+/* Frame ingest: uint16 photon counts [n_img][n_pix] -> FP32 copy, and
+ * optionally a bf16 copy and the FP32 squared norm of each frame (NULL to
+ * skip).  Replaces the host-side cast of the data images in SNM.__init__
+ * (spinifel/sequential/orientation_matching.py:70-75). */
+int spf_frames_ingest_u16(const uint16_t *d_counts, int64_t n_img, int64_t n_pix,
+                          float *d_f32, void *d_bf16, float *d_sq, void *stream);
+
+/* Squared norms of rows: d_out[r] = sum_p x[r,p]^2 (FP32 data, FP32 result
+ * accumulated in FP64 then rounded). */
+int spf_row_sqnorm_f32(const float *d_x, int64_t n_rows, int64_t n_pix,
+                       float *d_out, void *stream);
+
+/* Plain FP32 matching, the drop-in for SNM.euclidean_dist + argmin
+ * (spinifel/sequential/orientation_matching.py:98-109,179):
+ * dist(i, r) = x2[i] + s2[r] - 2 x_i . s_r over all n_ref references
+ * (ref_offset is added to the reported index), running minimum kept in
+ * d_best (one uint64 per image: order-preserving float bits << 32 | index;
+ * initialise with spf_best_init).  Ties go to the lower index. */
+int spf_best_init(uint64_t *d_best, int64_t n_img, void *stream);
+int spf_dist_argmin_f32(const float *d_img, const float *d_img_sq, int64_t n_img,
+                        const float *d_ref, const float *d_ref_sq, int64_t n_ref,
+                        int64_t n_pix, int64_t ref_offset, uint64_t *d_best,
+                        void *stream);
+int spf_best_unpack(const uint64_t *d_best, int64_t n_img, int32_t *d_idx,
+                    float *d_dist, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPINIFEL_GB300_H */

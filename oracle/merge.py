@@ -1,0 +1,93 @@
+"""ORACLE -- test infrastructure only.
+
+FP64 numpy/scipy restatement of the autocorrelation merge
+(spinifel/sequential/autocorrelation.py:35-225, class Merge):
+
+  ugrid_conv = adjoint(ones, H, K, L, support=1, M_ups) (real, / M_ups^3)  :158-166
+  F_conv     = fftn(ifftshift(ugrid_conv)) / M^3                          :168-169
+  W x        = conv(x) + rlambda x + flambda fourier_reg(x)               :171-177
+    conv(x)  = crop_M( fftshift(ifftn(fftn(ifftshift(pad_{M_ups}(x S))) F_conv)) ) S, real
+    reg(x)   = fftshift(ifftn(fftn(ifftshift(x S)) ifftshift(F_antisupport))) S, real
+  d          = adjoint(data, H, K, L, support=S, M) + rlambda x0          :184-193
+  x          = cg(W, d, x0, maxiter)                                       :217
+
+with rlambda = 1 / N / 1000, flambda = 1e3 (:61-62), N = number of data
+values, F_antisupport = |q| > pi / oversampling on linspace(-pi, pi, M)^3
+(:78-81).  The adjoint is the FP64 ES NUFFT of oracle/nufft.py.
+"""
+from __future__ import annotations
+
+import numpy as np
+from scipy.ndimage import gaussian_filter
+from scipy.sparse.linalg import LinearOperator, cg
+
+from . import nufft as onufft
+
+
+def antisupport(M: int, oversampling: int) -> np.ndarray:
+    lu = np.linspace(-np.pi, np.pi, M)
+    Hu, Ku, Lu = np.meshgrid(lu, lu, lu, indexing="ij")
+    return np.sqrt(Hu ** 2 + Ku ** 2 + Lu ** 2) > np.pi / oversampling
+
+
+def support_from_estimate(ac_estimate: np.ndarray) -> np.ndarray:
+    """spinifel/sequential/autocorrelation.py:209-210."""
+    return (gaussian_filter(ac_estimate, 0.5) > 1e-12).astype(np.float64)
+
+
+class MergeOracle:
+    def __init__(self, M, M_ups, N, oversampling=1, maxiter=100, eps=1e-12):
+        self.M, self.M_ups, self.N = M, M_ups, N
+        self.rlambda = 1.0 / N / 1000.0
+        self.flambda = 1e3
+        self.maxiter = maxiter
+        self.eps = eps
+        self.F_antisupport = antisupport(M, oversampling)
+        self.iterations = 0
+        self.residuals = []
+
+    def conv(self, x, F_conv, S):
+        M, Mu = self.M, self.M_ups
+        ups = np.zeros((Mu,) * 3)
+        ups[:M, :M, :M] = x.reshape((M,) * 3) * S
+        out = np.fft.fftshift(np.fft.ifftn(np.fft.fftn(np.fft.ifftshift(ups)) * F_conv))
+        return (out[:M, :M, :M] * S).real.reshape(-1)
+
+    def reg(self, x, S):
+        M = self.M
+        g = x.reshape((M,) * 3) * S
+        F = np.fft.fftn(np.fft.ifftshift(g))
+        r = np.fft.fftshift(np.fft.ifftn(F * np.fft.ifftshift(self.F_antisupport)))
+        return (r * S).real.reshape(-1)
+
+    def kernel(self, H_, K_, L_):
+        """F_conv from the type 1 of ones onto the M_ups grid."""
+        ones = np.ones(np.size(H_))
+        ugrid_conv = onufft.adjoint(ones, H_, K_, L_, self.M_ups, True, None, eps=self.eps)
+        return np.fft.fftn(np.fft.ifftshift(ugrid_conv)) / self.M ** 3
+
+    def rhs(self, data, H_, K_, L_, S, x0):
+        adb = onufft.adjoint(np.asarray(data, dtype=np.float64).reshape(-1), H_, K_, L_, self.M,
+                             True, S, eps=self.eps)
+        return adb.reshape(-1) + self.rlambda * x0
+
+    def solve(self, data, H_, K_, L_, ac_support, x0, maxiter=None, rtol=1e-5):
+        F_conv = self.kernel(H_, K_, L_)
+        S = ac_support
+
+        def W(u):
+            u = np.real(u)
+            return self.conv(u, F_conv, S) + self.rlambda * u + self.flambda * self.reg(u, S)
+
+        d = self.rhs(data, H_, K_, L_, S, x0)
+        n = self.M ** 3
+        A = LinearOperator(dtype=np.float64, shape=(n, n), matvec=W)
+        self.iterations = 0
+        self.residuals = []
+
+        def cb(xk):
+            self.iterations += 1
+            self.residuals.append(float(np.linalg.norm(d - W(xk))))
+
+        x, info = cg(A, d, x0=x0.copy(), maxiter=maxiter or self.maxiter, rtol=rtol, callback=cb)
+        return x.reshape((self.M,) * 3), info, F_conv, d

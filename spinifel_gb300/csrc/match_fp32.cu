@@ -1,0 +1,453 @@
+// Plain (SIMT) distance kernels: the drop-in for the reference's CUDA KNN
+// module and the FP32 distance + argmin that SNM computes with cuBLAS + CUB.
+//
+// Both operands are row-major with the pixel axis contiguous ("K-major"):
+// images [n_img][n_pix] and references [n_ref][n_pix].  A CTA computes a
+// 128 x 128 tile of (image, reference) pairs with 256 threads, each thread an
+// 8 x 8 register tile, K staged through shared memory in steps of 16 pixels
+// with register double-buffering.  The tile order is grouped (8 image tiles
+// per group) so that CTAs resident at the same time share image and
+// reference rows in L2.
+#include "common.cuh"
+
+namespace spf {
+
+constexpr int TB_M = 128;  // image rows per CTA
+constexpr int TB_N = 128;  // reference rows per CTA
+constexpr int TB_K = 16;
+constexpr int TB_THREADS = 256;
+constexpr int GROUP_M = 8;
+
+enum class Mode { DIFF, DOT };
+
+template <typename T>
+struct TileLoader {
+  // 128 rows x 16 k per tile = 2048 elements, 8 per thread as 2 x 4.
+  T v[2][4];
+  __device__ __forceinline__ void load(const T *__restrict__ base, int64_t n_rows, int64_t ld,
+                                       int64_t K, int64_t row0, int64_t k0, bool vec) {
+    int tid = threadIdx.x;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      int idx = tid + i * TB_THREADS;
+      int r = idx >> 2;
+      int kq = (idx & 3) * 4;
+      int64_t row = row0 + r;
+      int64_t k = k0 + kq;
+      if (row < n_rows) {
+        const T *p = base + row * ld + k;
+        if constexpr (sizeof(T) == 4) {
+          if (vec && k + 3 < K) {
+            float4 f = __ldg(reinterpret_cast<const float4 *>(p));
+            v[i][0] = f.x; v[i][1] = f.y; v[i][2] = f.z; v[i][3] = f.w;
+            continue;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[i][j] = (k + j < K) ? __ldg(p + j) : T(0);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[i][j] = T(0);
+      }
+    }
+  }
+  __device__ __forceinline__ void store(T (*s)[TB_M + 4]) {
+    int tid = threadIdx.x;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      int idx = tid + i * TB_THREADS;
+      int r = idx >> 2;
+      int kq = (idx & 3) * 4;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) s[kq + j][r] = v[i][j];
+    }
+  }
+};
+
+__device__ __forceinline__ void tile_coords(int64_t n_img_tiles, int64_t n_ref_tiles,
+                                            int64_t &mt, int64_t &nt) {
+  int64_t bid = blockIdx.x;
+  int64_t per_group = (int64_t)GROUP_M * n_ref_tiles;
+  int64_t group = bid / per_group;
+  int64_t first_m = group * GROUP_M;
+  int64_t gm = n_img_tiles - first_m;
+  if (gm > GROUP_M) gm = GROUP_M;
+  int64_t in = bid % per_group;
+  mt = first_m + in % gm;
+  nt = in / gm;
+}
+
+// acc[i][j] accumulates for image row (ty*4 + i%4 + 64*(i/4)) and reference
+// row (tx*4 + j%4 + 64*(j/4)) of the tile.
+template <typename T, Mode MODE>
+__device__ __forceinline__ void tile_mainloop(const T *__restrict__ A, int64_t n_a,
+                                              const T *__restrict__ B, int64_t n_b, int64_t ld,
+                                              int64_t K, int64_t a0, int64_t b0, T acc[8][8],
+                                              T (*As)[TB_K][TB_M + 4],
+                                              T (*Bs)[TB_K][TB_N + 4]) {
+  const int tx = threadIdx.x & 15;
+  const int ty = threadIdx.x >> 4;
+  const bool vec = (sizeof(T) == 4) && (ld % 4 == 0) && aligned(A, 16) && aligned(B, 16);
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = T(0);
+  TileLoader<T> la, lb;
+  int64_t ktiles = (K + TB_K - 1) / TB_K;
+  if (ktiles == 0) return;
+  la.load(A, n_a, ld, K, a0, 0, vec);
+  lb.load(B, n_b, ld, K, b0, 0, vec);
+  la.store(As[0]);
+  lb.store(Bs[0]);
+  __syncthreads();
+  for (int64_t kt = 0; kt < ktiles; ++kt) {
+    int cur = kt & 1;
+    bool more = kt + 1 < ktiles;
+    if (more) {
+      la.load(A, n_a, ld, K, a0, (kt + 1) * TB_K, vec);
+      lb.load(B, n_b, ld, K, b0, (kt + 1) * TB_K, vec);
+    }
+#pragma unroll
+    for (int k = 0; k < TB_K; ++k) {
+      T a[8], b[8];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        a[i] = As[cur][k][ty * 4 + i];
+        a[i + 4] = As[cur][k][64 + ty * 4 + i];
+        b[i] = Bs[cur][k][tx * 4 + i];
+        b[i + 4] = Bs[cur][k][64 + tx * 4 + i];
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if constexpr (MODE == Mode::DIFF) {
+            T d = a[i] - b[j];
+            acc[i][j] = fma(d, d, acc[i][j]);
+          } else {
+            acc[i][j] = fma(a[i], b[j], acc[i][j]);
+          }
+        }
+    }
+    if (more) {
+      la.store(As[cur ^ 1]);
+      lb.store(Bs[cur ^ 1]);
+    }
+    __syncthreads();
+  }
+}
+
+// out[d][r] = sum_{p < K} (data[d][p] - ref[r][p])^2
+template <typename T>
+__global__ void __launch_bounds__(TB_THREADS) k_knn_eudist(const T *__restrict__ ref,
+                                                           const T *__restrict__ data,
+                                                           int64_t n_ref, int64_t n_data,
+                                                           int64_t ld, int64_t K,
+                                                           T *__restrict__ out) {
+  __shared__ __align__(16) T As[2][TB_K][TB_M + 4];
+  __shared__ __align__(16) T Bs[2][TB_K][TB_N + 4];
+  int64_t n_img_tiles = (n_data + TB_M - 1) / TB_M;
+  int64_t n_ref_tiles = (n_ref + TB_N - 1) / TB_N;
+  int64_t mt, nt;
+  tile_coords(n_img_tiles, n_ref_tiles, mt, nt);
+  T acc[8][8];
+  tile_mainloop<T, Mode::DIFF>(data, n_data, ref, n_ref, ld, K, mt * TB_M, nt * TB_N, acc, As,
+                               Bs);
+  const int tx = threadIdx.x & 15;
+  const int ty = threadIdx.x >> 4;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    int64_t d = mt * TB_M + ty * 4 + (i & 3) + 64 * (i >> 2);
+    if (d >= n_data) continue;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      int64_t r = nt * TB_N + tx * 4 + (j & 3) + 64 * (j >> 2);
+      if (r < n_ref) out[d * n_ref + r] = acc[i][j];
+    }
+  }
+}
+
+// Running argmin of x2 + s2 - 2 x.s, packed (order key << 32 | index).
+__global__ void __launch_bounds__(TB_THREADS) k_dist_argmin_f32(
+    const float *__restrict__ img, const float *__restrict__ img_sq, int64_t n_img,
+    const float *__restrict__ ref, const float *__restrict__ ref_sq, int64_t n_ref, int64_t K,
+    int64_t ref_offset, unsigned long long *__restrict__ best) {
+  __shared__ __align__(16) float As[2][TB_K][TB_M + 4];
+  __shared__ __align__(16) float Bs[2][TB_K][TB_N + 4];
+  int64_t n_img_tiles = (n_img + TB_M - 1) / TB_M;
+  int64_t n_ref_tiles = (n_ref + TB_N - 1) / TB_N;
+  int64_t mt, nt;
+  tile_coords(n_img_tiles, n_ref_tiles, mt, nt);
+  float acc[8][8];
+  tile_mainloop<float, Mode::DOT>(img, n_img, ref, n_ref, K, K, mt * TB_M, nt * TB_N, acc, As,
+                                  Bs);
+  const int tx = threadIdx.x & 15;
+  const int ty = threadIdx.x >> 4;
+  float s2[8];
+  int64_t rr[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    rr[j] = nt * TB_N + tx * 4 + (j & 3) + 64 * (j >> 2);
+    s2[j] = rr[j] < n_ref ? ref_sq[rr[j]] : 0.0f;
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    int64_t d = mt * TB_M + ty * 4 + (i & 3) + 64 * (i >> 2);
+    float x2 = d < n_img ? img_sq[d] : 0.0f;
+    unsigned long long key = ~0ULL;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      if (rr[j] < n_ref) {
+        float dist = (x2 + s2[j]) - 2.0f * acc[i][j];
+        unsigned long long k2 =
+            ((unsigned long long)float_key(dist) << 32) | (unsigned long long)(rr[j] + ref_offset);
+        key = k2 < key ? k2 : key;
+      }
+    }
+    // the 16 threads with this ty hold the other columns of the row
+#pragma unroll
+    for (int o = 8; o >= 1; o >>= 1) {
+      unsigned long long other = __shfl_xor_sync(0xffffffffu, key, o, 16);
+      key = other < key ? other : key;
+    }
+    if (tx == 0 && d < n_img && key != ~0ULL) atomicMin(best + d, key);
+  }
+}
+
+__global__ void k_best_init(unsigned long long *best, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    best[i] = ~0ULL;
+}
+
+__global__ void k_best_unpack(const unsigned long long *__restrict__ best, int64_t n,
+                              int32_t *__restrict__ idx, float *__restrict__ dist) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    unsigned long long b = best[i];
+    if (idx) idx[i] = (b == ~0ULL) ? -1 : (int32_t)(b & 0xffffffffu);
+    if (dist) dist[i] = key_float((uint32_t)(b >> 32));
+  }
+}
+
+// sum of squares per row (FP64 accumulation, one warp per row)
+__global__ void k_row_sqnorm(const float *__restrict__ x, int64_t n_rows, int64_t n_pix,
+                             float *__restrict__ out) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n_rows; r += nwarps) {
+    const float *p = x + r * n_pix;
+    double s = 0.0;
+    for (int64_t k = lane; k < n_pix; k += 32) {
+      double v = p[k];
+      s = fma(v, v, s);
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[r] = (float)s;
+  }
+}
+
+// uint16 counts -> f32 (+ bf16) (+ squared norm); one warp per frame
+__global__ void k_ingest_u16(const uint16_t *__restrict__ in, int64_t n_img, int64_t n_pix,
+                             float *__restrict__ f32, __nv_bfloat16 *__restrict__ bf,
+                             float *__restrict__ sq) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n_img; r += nwarps) {
+    const uint16_t *p = in + r * n_pix;
+    double s = 0.0;
+    for (int64_t k = lane; k < n_pix; k += 32) {
+      float v = (float)p[k];
+      f32[r * n_pix + k] = v;
+      if (bf) bf[r * n_pix + k] = __float2bfloat16_rn(v);
+      s = fma((double)v, (double)v, s);
+    }
+    if (sq) {
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) sq[r] = (float)s;
+    }
+  }
+}
+
+// k smallest of each row, ascending, ties to the lower index; warp per row.
+template <typename T>
+__global__ void k_topk(const T *__restrict__ dist, int64_t n_rows, int64_t n_cols, int k,
+                       int32_t *__restrict__ out) {
+  constexpr int KMAX = 32;
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n_rows; r += nwarps) {
+    T d[KMAX];
+    int32_t ix[KMAX];
+    int cnt = 0;
+    const T *row = dist + r * n_cols;
+    for (int64_t c = lane; c < n_cols; c += 32) {
+      T v = row[c];
+      int32_t ci = (int32_t)c;
+      // columns arrive in increasing order per lane, so an equal value never
+      // displaces an existing entry (lower index wins)
+      if (cnt < k) {
+        int pos = cnt++;
+        while (pos > 0 && d[pos - 1] > v) {
+          d[pos] = d[pos - 1];
+          ix[pos] = ix[pos - 1];
+          --pos;
+        }
+        d[pos] = v;
+        ix[pos] = ci;
+      } else if (v < d[k - 1]) {
+        int pos = k - 1;
+        while (pos > 0 && d[pos - 1] > v) {
+          d[pos] = d[pos - 1];
+          ix[pos] = ix[pos - 1];
+          --pos;
+        }
+        d[pos] = v;
+        ix[pos] = ci;
+      }
+    }
+    int head = 0;
+    for (int t = 0; t < k; ++t) {
+      T hv = head < cnt ? d[head] : T(0);
+      int32_t hi = head < cnt ? ix[head] : INT32_MAX;
+      bool valid = head < cnt;
+      // warp min by (valid, value, index)
+      T bv = hv;
+      int32_t bi = hi;
+      bool bvalid = valid;
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        T ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        int32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        bool ovalid = __shfl_xor_sync(0xffffffffu, (int)bvalid, o);
+        bool take = ovalid && (!bvalid || ov < bv || (ov == bv && oi < bi));
+        if (take) {
+          bv = ov;
+          bi = oi;
+          bvalid = true;
+        }
+      }
+      if (valid && hi == bi) ++head;
+      if (lane == 0) out[r * k + t] = bvalid ? bi : -1;
+    }
+  }
+}
+
+}  // namespace spf
+
+using namespace spf;
+
+template <typename T>
+static int knn_eudist(const T *ref, const T *data, int64_t n_ref, int64_t n_data, int64_t n_pix,
+                      T *out, void *stream, const char *name) {
+  SPF_REQUIRE(n_ref >= 0 && n_data >= 0 && n_pix >= 0, "%s: negative size", name);
+  if (n_ref == 0 || n_data == 0) return SPF_OK;
+  SPF_REQUIRE(ref && data && out, "%s: NULL pointer", name);
+  int64_t K = (n_pix / 16) * 16;  // the reference kernel drops the ragged tail
+  int64_t tiles = ((n_data + TB_M - 1) / TB_M) * ((n_ref + TB_N - 1) / TB_N);
+  SPF_REQUIRE(tiles < (1LL << 31), "%s: too many tiles", name);
+  k_knn_eudist<T><<<(unsigned)tiles, TB_THREADS, 0, as_stream(stream)>>>(ref, data, n_ref, n_data,
+                                                                          n_pix, K, out);
+  return check_launch(name);
+}
+
+template <typename T>
+static int knn_topk(const T *dist, int64_t n_data, int64_t n_ref, int k, int32_t *idx,
+                    void *stream, const char *name) {
+  SPF_REQUIRE(n_data >= 0 && n_ref >= 0, "%s: negative size", name);
+  SPF_REQUIRE(k >= 1 && k <= 32, "%s: k must be in [1, 32]", name);
+  SPF_REQUIRE(k <= n_ref || n_data == 0, "%s: k > n_ref", name);
+  if (n_data == 0) return SPF_OK;
+  SPF_REQUIRE(dist && idx, "%s: NULL pointer", name);
+  int blocks = grid_for(n_data * 32, 256, (int64_t)sm_count() * 32);
+  k_topk<T><<<blocks, 256, 0, as_stream(stream)>>>(dist, n_data, n_ref, k, idx);
+  return check_launch(name);
+}
+
+extern "C" {
+
+int spf_knn_eudist_f32(const float *d_ref, const float *d_data, int64_t n_ref, int64_t n_data,
+                       int64_t n_pix, float *d_out, void *stream) {
+  return knn_eudist<float>(d_ref, d_data, n_ref, n_data, n_pix, d_out, stream,
+                           "spf_knn_eudist_f32");
+}
+
+int spf_knn_eudist_f64(const double *d_ref, const double *d_data, int64_t n_ref, int64_t n_data,
+                       int64_t n_pix, double *d_out, void *stream) {
+  return knn_eudist<double>(d_ref, d_data, n_ref, n_data, n_pix, d_out, stream,
+                            "spf_knn_eudist_f64");
+}
+
+int spf_knn_topk_f32(const float *d_dist, int64_t n_data, int64_t n_ref, int k, int32_t *d_idx,
+                     void *stream) {
+  return knn_topk<float>(d_dist, n_data, n_ref, k, d_idx, stream, "spf_knn_topk_f32");
+}
+
+int spf_knn_topk_f64(const double *d_dist, int64_t n_data, int64_t n_ref, int k, int32_t *d_idx,
+                     void *stream) {
+  return knn_topk<double>(d_dist, n_data, n_ref, k, d_idx, stream, "spf_knn_topk_f64");
+}
+
+int spf_row_sqnorm_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_out,
+                       void *stream) {
+  SPF_REQUIRE(n_rows >= 0 && n_pix >= 0, "spf_row_sqnorm_f32: negative size");
+  if (n_rows == 0) return SPF_OK;
+  SPF_REQUIRE(d_x && d_out, "spf_row_sqnorm_f32: NULL pointer");
+  int blocks = grid_for(n_rows * 32, 256, (int64_t)sm_count() * 32);
+  k_row_sqnorm<<<blocks, 256, 0, as_stream(stream)>>>(d_x, n_rows, n_pix, d_out);
+  return check_launch("spf_row_sqnorm_f32");
+}
+
+int spf_frames_ingest_u16(const uint16_t *d_counts, int64_t n_img, int64_t n_pix, float *d_f32,
+                          void *d_bf16, float *d_sq, void *stream) {
+  SPF_REQUIRE(n_img >= 0 && n_pix >= 0, "spf_frames_ingest_u16: negative size");
+  if (n_img == 0 || n_pix == 0) return SPF_OK;
+  SPF_REQUIRE(d_counts && d_f32, "spf_frames_ingest_u16: NULL pointer");
+  int blocks = grid_for(n_img * 32, 256, (int64_t)sm_count() * 32);
+  k_ingest_u16<<<blocks, 256, 0, as_stream(stream)>>>(
+      d_counts, n_img, n_pix, d_f32, reinterpret_cast<__nv_bfloat16 *>(d_bf16), d_sq);
+  return check_launch("spf_frames_ingest_u16");
+}
+
+int spf_best_init(uint64_t *d_best, int64_t n_img, void *stream) {
+  SPF_REQUIRE(n_img >= 0, "spf_best_init: negative size");
+  if (n_img == 0) return SPF_OK;
+  SPF_REQUIRE(d_best != nullptr, "spf_best_init: NULL pointer");
+  k_best_init<<<grid_for(n_img, 256, 4096), 256, 0, as_stream(stream)>>>(
+      reinterpret_cast<unsigned long long *>(d_best), n_img);
+  return check_launch("spf_best_init");
+}
+
+int spf_dist_argmin_f32(const float *d_img, const float *d_img_sq, int64_t n_img,
+                        const float *d_ref, const float *d_ref_sq, int64_t n_ref, int64_t n_pix,
+                        int64_t ref_offset, uint64_t *d_best, void *stream) {
+  SPF_REQUIRE(n_img >= 0 && n_ref >= 0 && n_pix >= 0 && ref_offset >= 0,
+              "spf_dist_argmin_f32: negative size");
+  if (n_img == 0 || n_ref == 0) return SPF_OK;
+  SPF_REQUIRE(d_img && d_img_sq && d_ref && d_ref_sq && d_best,
+              "spf_dist_argmin_f32: NULL pointer");
+  SPF_REQUIRE(ref_offset + n_ref < (1LL << 32), "spf_dist_argmin_f32: index exceeds 32 bits");
+  int64_t tiles = ((n_img + TB_M - 1) / TB_M) * ((n_ref + TB_N - 1) / TB_N);
+  SPF_REQUIRE(tiles < (1LL << 31), "spf_dist_argmin_f32: too many tiles");
+  k_dist_argmin_f32<<<(unsigned)tiles, TB_THREADS, 0, as_stream(stream)>>>(
+      d_img, d_img_sq, n_img, d_ref, d_ref_sq, n_ref, n_pix, ref_offset,
+      reinterpret_cast<unsigned long long *>(d_best));
+  return check_launch("spf_dist_argmin_f32");
+}
+
+int spf_best_unpack(const uint64_t *d_best, int64_t n_img, int32_t *d_idx, float *d_dist,
+                    void *stream) {
+  SPF_REQUIRE(n_img >= 0, "spf_best_unpack: negative size");
+  if (n_img == 0) return SPF_OK;
+  SPF_REQUIRE(d_best != nullptr, "spf_best_unpack: NULL pointer");
+  k_best_unpack<<<grid_for(n_img, 256, 4096), 256, 0, as_stream(stream)>>>(
+      reinterpret_cast<const unsigned long long *>(d_best), n_img, d_idx, d_dist);
+  return check_launch("spf_best_unpack");
+}
+
+}  // extern "C"

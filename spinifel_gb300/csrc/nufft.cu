@@ -1,0 +1,627 @@
+// 3D type-1 / type-2 NUFFT with the exponential-of-semicircle (ES) kernel,
+// FP32 on the device, for the Spinifel slicing and merge operators.
+//
+// Layout in HBM (per plan):
+//   fine   : n1*n2*n3 complex64, the upsampled grid the FFT works on;
+//   re_pad : (n1+2p)(n2+2p)(n3+2p) float, Re of the type-2 fine grid with a
+//            periodic halo of p = ceil(w/2)+1 cells on every side, so that a
+//            kernel footprint never wraps (no modulo in the inner loop);
+//   im_pad : same for Im (only when requested);
+//   acc_pad: padded real grid that type-1 spreading accumulates into; the
+//            halo is folded back onto the periodic grid before the FFT.
+// A point x (radians) sits at fine-grid coordinate t = x n / (2 pi), wrapped
+// into [-n/2, n/2); its footprint is the w cells l0 .. l0+w-1 with
+// l0 = ceil(t - w/2), stored at padded index l + n/2 + p.
+#include <cufft.h>
+#include <math.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+struct spf_nufft_plan_s {
+  int dev = 0;
+  int m[3] = {0, 0, 0};
+  int n[3] = {0, 0, 0};
+  int np[3] = {0, 0, 0};
+  int pad = 0;
+  int w = 0;
+  double beta = 0, sigma = 2.0, eps = 1e-6;
+  float *inv_p[3] = {nullptr, nullptr, nullptr};  // 1 / kernel FT per mode
+  float2 *fine = nullptr;
+  float *re_pad = nullptr;
+  float *im_pad = nullptr;
+  float *acc_pad = nullptr;
+  cufftHandle fft = 0;
+  bool fft_ok = false;
+};
+
+namespace spf {
+
+static int next_smooth_even(int n) {
+  if (n < 2) n = 2;
+  if (n & 1) ++n;
+  for (;; n += 2) {
+    int m = n;
+    for (int p : {2, 3, 5})
+      while (m % p == 0) m /= p;
+    if (m == 1) return n;
+  }
+}
+
+// Gauss-Legendre nodes/weights on [-1, 1] by Newton iteration on P_q.
+static void gauss_legendre(int q, std::vector<double> &x, std::vector<double> &wt) {
+  x.assign(q, 0.0);
+  wt.assign(q, 0.0);
+  for (int i = 0; i < q; ++i) {
+    double z = cos(M_PI * (i + 0.75) / (q + 0.5));
+    double dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= q; ++k) {
+        double pk = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = pk;
+      }
+      dp = q * (z * p1 - p0) / (z * z - 1.0);
+      double dz = p1 / dp;
+      z -= dz;
+      if (fabs(dz) < 1e-15) break;
+    }
+    x[i] = z;
+    wt[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+static int es_width(double eps, double sigma) {
+  int w;
+  if (sigma == 2.0) {
+    w = (int)ceil(-log10(eps / 10.0));
+  } else {
+    w = (int)ceil(log(1.0 / eps) / (M_PI * sqrt(1.0 - 1.0 / sigma)));
+  }
+  if (w < 3) w = 3;
+  if (w > 8) w = 8;  // FP32 cannot resolve finer tolerances
+  return w;
+}
+
+static double es_beta(int w, double sigma) {
+  if (sigma == 2.0) {
+    double bon = (w == 2) ? 2.20 : (w == 3) ? 2.26 : (w == 4) ? 2.38 : 2.30;
+    return bon * w;
+  }
+  return 0.97 * M_PI * w * (1.0 - 1.0 / (2.0 * sigma));
+}
+
+// 1 / p(k), p(k) = int_{-w/2}^{w/2} phi(2t/w) cos(k h t) dt, h = 2 pi / n.
+static std::vector<float> inverse_kernel_ft(int m, int n, int w, double beta) {
+  std::vector<double> xq, wq;
+  gauss_legendre(4 * w + 40, xq, wq);
+  std::vector<float> out(m);
+  double h = 2.0 * M_PI / n;
+  for (int i = 0; i < m; ++i) {
+    double k = (double)(i - m / 2);
+    double s = 0.0;
+    for (size_t q = 0; q < xq.size(); ++q) {
+      double t = 0.25 * w * (xq[q] + 1.0);
+      double z = 2.0 * t / w;
+      double phi = exp(beta * (sqrt(fmax(1.0 - z * z, 0.0)) - 1.0));
+      s += 0.25 * w * wq[q] * phi * cos(k * h * t);
+    }
+    out[i] = (float)(1.0 / (2.0 * s));
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+
+struct GridGeom {
+  int n1, n2, n3;     // fine grid
+  int p1, p2, p3;     // padded dims
+  int off1, off2, off3;  // n/2 + pad
+  float beta;
+  float half_w;
+  float inv_half_w;   // 2 / w
+};
+
+static GridGeom geom_of(const spf_nufft_plan_s *P) {
+  GridGeom g;
+  g.n1 = P->n[0]; g.n2 = P->n[1]; g.n3 = P->n[2];
+  g.p1 = P->np[0]; g.p2 = P->np[1]; g.p3 = P->np[2];
+  g.off1 = P->n[0] / 2 + P->pad;
+  g.off2 = P->n[1] / 2 + P->pad;
+  g.off3 = P->n[2] / 2 + P->pad;
+  g.beta = (float)P->beta;
+  g.half_w = 0.5f * P->w;
+  g.inv_half_w = 2.0f / P->w;
+  return g;
+}
+
+__device__ __forceinline__ float es_eval(float z, float beta) {
+  float s = fmaxf(1.0f - z * z, 0.0f);
+  return expf(beta * (sqrtf(s) - 1.0f));
+}
+
+// Padded first index and the W weights along one axis for fine-grid
+// coordinate t (already scaled to grid units).
+template <int W>
+__device__ __forceinline__ int axis_setup(float t, int n, int off, float beta, float inv_half_w,
+                                          float *wt) {
+  float fn = (float)n;
+  t = t - fn * floorf(t / fn + 0.5f);  // [-n/2, n/2)
+  float l0 = ceilf(t - 0.5f * W);
+#pragma unroll
+  for (int a = 0; a < W; ++a) {
+    float z = (l0 + (float)a - t) * inv_half_w;
+    wt[a] = es_eval(z, beta);
+  }
+  return (int)l0 + off;
+}
+
+template <int W>
+__device__ __forceinline__ float interp_point(const float *__restrict__ grid, const GridGeom &g,
+                                              float t1, float t2, float t3) {
+  float w1[W], w2[W], w3[W];
+  int i0 = axis_setup<W>(t1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
+  int j0 = axis_setup<W>(t2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
+  int k0 = axis_setup<W>(t3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
+  float acc = 0.0f;
+#pragma unroll
+  for (int a = 0; a < W; ++a) {
+    float acc_a = 0.0f;
+#pragma unroll
+    for (int b = 0; b < W; ++b) {
+      const float *row = grid + ((size_t)(i0 + a) * g.p2 + (j0 + b)) * g.p3 + k0;
+      float r = 0.0f;
+#pragma unroll
+      for (int c = 0; c < W; ++c) r = fmaf(w3[c], __ldg(row + c), r);
+      acc_a = fmaf(w2[b], r, acc_a);
+    }
+    acc = fmaf(w1[a], acc_a, acc);
+  }
+  return acc;
+}
+
+template <int W>
+__device__ __forceinline__ void spread_point(float *__restrict__ grid, const GridGeom &g, float t1,
+                                             float t2, float t3, float c) {
+  float w1[W], w2[W], w3[W];
+  int i0 = axis_setup<W>(t1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
+  int j0 = axis_setup<W>(t2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
+  int k0 = axis_setup<W>(t3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
+#pragma unroll
+  for (int c3 = 0; c3 < W; ++c3) w3[c3] *= c;
+#pragma unroll
+  for (int a = 0; a < W; ++a) {
+#pragma unroll
+    for (int b = 0; b < W; ++b) {
+      float wab = w1[a] * w2[b];
+      float *row = grid + ((size_t)(i0 + a) * g.p2 + (j0 + b)) * g.p3 + k0;
+#pragma unroll
+      for (int c3 = 0; c3 < W; ++c3) atomicAdd(row + c3, wab * w3[c3]);
+    }
+  }
+}
+
+// Rotation of pixel position q by the inverse of R(quat) (quat = [w,x,y,z],
+// spinifel/extern/nufft_ext.py:59-60 with eval/geom.py:9-48), scaled.
+__device__ __forceinline__ void rotate_inv(const float *__restrict__ quat, float qx, float qy,
+                                           float qz, float s, float &h, float &k, float &l) {
+  float q0 = quat[0], q1 = quat[1], q2 = quat[2], q3 = quat[3];
+  float r00 = 1.f - 2.f * (q2 * q2 + q3 * q3), r01 = 2.f * (q1 * q2 - q0 * q3),
+        r02 = 2.f * (q1 * q3 + q0 * q2);
+  float r10 = 2.f * (q1 * q2 + q0 * q3), r11 = 1.f - 2.f * (q1 * q1 + q3 * q3),
+        r12 = 2.f * (q2 * q3 - q0 * q1);
+  float r20 = 2.f * (q1 * q3 - q0 * q2), r21 = 2.f * (q2 * q3 + q0 * q1),
+        r22 = 1.f - 2.f * (q1 * q1 + q2 * q2);
+  // R^-1 = R^T for a unit quaternion
+  h = s * (r00 * qx + r10 * qy + r20 * qz);
+  k = s * (r01 * qx + r11 * qy + r21 * qz);
+  l = s * (r02 * qx + r12 * qy + r22 * qz);
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+// b[k mod n] = f_k * support_k / (p1 p2 p3), complex fine grid pre-zeroed.
+__global__ void k_t2_scatter_modes(const float *__restrict__ f, const float *__restrict__ sup,
+                                   int m1, int m2, int m3, int n1, int n2, int n3,
+                                   const float *__restrict__ ip1, const float *__restrict__ ip2,
+                                   const float *__restrict__ ip3, float2 *__restrict__ fine) {
+  int64_t total = (int64_t)m1 * m2 * m3;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int c = (int)(idx % m3);
+    int b = (int)((idx / m3) % m2);
+    int a = (int)(idx / ((int64_t)m2 * m3));
+    float v = f[idx];
+    if (sup) v *= sup[idx];
+    v *= ip1[a] * ip2[b] * ip3[c];
+    int fa = ((a - m1 / 2) % n1 + n1) % n1;
+    int fb = ((b - m2 / 2) % n2 + n2) % n2;
+    int fc = ((c - m3 / 2) % n3 + n3) % n3;
+    fine[((int64_t)fa * n2 + fb) * n3 + fc] = make_float2(v, 0.0f);
+  }
+}
+
+// re_pad[i] = Re fine[(i - off) mod n] (and Im), for every padded cell.
+__global__ void k_t2_fill_padded(const float2 *__restrict__ fine, GridGeom g, float im_sign,
+                                 float *__restrict__ re_pad, float *__restrict__ im_pad) {
+  int64_t total = (int64_t)g.p1 * g.p2 * g.p3;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int k = (int)(idx % g.p3);
+    int j = (int)((idx / g.p3) % g.p2);
+    int i = (int)(idx / ((int64_t)g.p2 * g.p3));
+    int a = ((i - g.off1) % g.n1 + g.n1) % g.n1;
+    int b = ((j - g.off2) % g.n2 + g.n2) % g.n2;
+    int c = ((k - g.off3) % g.n3 + g.n3) % g.n3;
+    float2 v = fine[((int64_t)a * g.n2 + b) * g.n3 + c];
+    re_pad[idx] = v.x;
+    if (im_pad) im_pad[idx] = im_sign * v.y;
+  }
+}
+
+template <int W>
+__global__ void k_t2_interp(const float *__restrict__ re_pad, const float *__restrict__ im_pad,
+                            GridGeom g, const float *__restrict__ x, const float *__restrict__ y,
+                            const float *__restrict__ z, int64_t npts, float *__restrict__ out_re,
+                            float *__restrict__ out_im) {
+  const float sc1 = g.n1 * (float)(0.5 / M_PI), sc2 = g.n2 * (float)(0.5 / M_PI),
+              sc3 = g.n3 * (float)(0.5 / M_PI);
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < npts;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    float t1 = x[j] * sc1, t2 = y[j] * sc2, t3 = z[j] * sc3;
+    out_re[j] = interp_point<W>(re_pad, g, t1, t2, t3);
+    if (out_im) out_im[j] = interp_point<W>(im_pad, g, t1, t2, t3);
+  }
+}
+
+template <int W>
+__global__ void k_slice_t2(const float *__restrict__ re_pad, GridGeom g,
+                           const float *__restrict__ quats, const float *__restrict__ ppr,
+                           int64_t n_pix, float scale1, float scale2, float scale3,
+                           float *__restrict__ out, __nv_bfloat16 *__restrict__ out_bf16) {
+  int64_t o = blockIdx.x;
+  int64_t p = blockIdx.y * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n_pix) return;
+  float h, k, l;
+  rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
+  float v = interp_point<W>(re_pad, g, h * scale1, k * scale2, l * scale3);
+  int64_t idx = o * n_pix + p;
+  out[idx] = v;
+  if (out_bf16) out_bf16[idx] = __float2bfloat16_rn(v);
+}
+
+template <int W>
+__global__ void k_t1_spread(float *__restrict__ acc_pad, GridGeom g, const float *__restrict__ x,
+                            const float *__restrict__ y, const float *__restrict__ z,
+                            const float *__restrict__ c, int64_t npts) {
+  const float sc1 = g.n1 * (float)(0.5 / M_PI), sc2 = g.n2 * (float)(0.5 / M_PI),
+              sc3 = g.n3 * (float)(0.5 / M_PI);
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < npts;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    float cj = c[j];
+    if (cj == 0.0f) continue;
+    spread_point<W>(acc_pad, g, x[j] * sc1, y[j] * sc2, z[j] * sc3, cj);
+  }
+}
+
+template <int W>
+__global__ void k_t1_spread_orient(float *__restrict__ acc_pad, GridGeom g,
+                                   const float *__restrict__ quats, const float *__restrict__ ppr,
+                                   int64_t n_pix, float scale1, float scale2, float scale3,
+                                   const float *__restrict__ c) {
+  int64_t o = blockIdx.x;
+  int64_t p = blockIdx.y * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n_pix) return;
+  float cj = c[o * n_pix + p];
+  if (cj == 0.0f) return;
+  float h, k, l;
+  rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
+  spread_point<W>(acc_pad, g, h * scale1, k * scale2, l * scale3, cj);
+}
+
+// fine[l] = sum of acc_pad[i] over padded i == l + off (mod n)  (Im = 0).
+__global__ void k_t1_fold(const float *__restrict__ acc_pad, GridGeom g,
+                          float2 *__restrict__ fine) {
+  int64_t total = (int64_t)g.n1 * g.n2 * g.n3;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int c = (int)(idx % g.n3);
+    int b = (int)((idx / g.n3) % g.n2);
+    int a = (int)(idx / ((int64_t)g.n2 * g.n3));
+    int ia[2], ib[2], ic[2];
+    int na = 0, nb = 0, nc = 0;
+    int i0 = (a + g.off1) % g.n1;
+    ia[na++] = i0;
+    if (i0 + g.n1 < g.p1) ia[na++] = i0 + g.n1;
+    int j0 = (b + g.off2) % g.n2;
+    ib[nb++] = j0;
+    if (j0 + g.n2 < g.p2) ib[nb++] = j0 + g.n2;
+    int k0 = (c + g.off3) % g.n3;
+    ic[nc++] = k0;
+    if (k0 + g.n3 < g.p3) ic[nc++] = k0 + g.n3;
+    float s = 0.0f;
+    for (int u = 0; u < na; ++u)
+      for (int v = 0; v < nb; ++v)
+        for (int q = 0; q < nc; ++q)
+          s += acc_pad[((int64_t)ia[u] * g.p2 + ib[v]) * g.p3 + ic[q]];
+    fine[idx] = make_float2(s, 0.0f);
+  }
+}
+
+// modes[k] = fine[k mod n] / (p1 p2 p3)
+__global__ void k_t1_extract(const float2 *__restrict__ fine, int m1, int m2, int m3, int n1,
+                             int n2, int n3, const float *__restrict__ ip1,
+                             const float *__restrict__ ip2, const float *__restrict__ ip3,
+                             float *__restrict__ out_re, float *__restrict__ out_im) {
+  int64_t total = (int64_t)m1 * m2 * m3;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int c = (int)(idx % m3);
+    int b = (int)((idx / m3) % m2);
+    int a = (int)(idx / ((int64_t)m2 * m3));
+    int fa = ((a - m1 / 2) % n1 + n1) % n1;
+    int fb = ((b - m2 / 2) % n2 + n2) % n2;
+    int fc = ((c - m3 / 2) % n3 + n3) % n3;
+    float2 v = fine[((int64_t)fa * n2 + fb) * n3 + fc];
+    float s = ip1[a] * ip2[b] * ip3[c];
+    out_re[idx] = v.x * s;
+    if (out_im) out_im[idx] = v.y * s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// dispatch on the kernel width
+// ---------------------------------------------------------------------------
+
+#define SPF_W_DISPATCH(w, KERNEL_CALL)              \
+  switch (w) {                                      \
+    case 3: { constexpr int W = 3; KERNEL_CALL; break; } \
+    case 4: { constexpr int W = 4; KERNEL_CALL; break; } \
+    case 5: { constexpr int W = 5; KERNEL_CALL; break; } \
+    case 6: { constexpr int W = 6; KERNEL_CALL; break; } \
+    case 7: { constexpr int W = 7; KERNEL_CALL; break; } \
+    case 8: { constexpr int W = 8; KERNEL_CALL; break; } \
+    default: set_error("unsupported kernel width %d", w); return SPF_ERR_UNSUPPORTED; \
+  }
+
+static int check_plan(spf_nufft_plan P, const char *what) {
+  if (!P) {
+    set_error("%s: plan is NULL", what);
+    return SPF_ERR_ARG;
+  }
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != P->dev) {
+    set_error("%s: plan was made on device %d, current device is %d", what, P->dev, dev);
+    return SPF_ERR_ARG;
+  }
+  return SPF_OK;
+}
+
+static int fft_exec(spf_nufft_plan P, int isign, cudaStream_t s, const char *what) {
+  if (cufftSetStream(P->fft, s) != CUFFT_SUCCESS) {
+    set_error("%s: cufftSetStream failed", what);
+    return SPF_ERR_CUDA;
+  }
+  cufftResult r = cufftExecC2C(P->fft, reinterpret_cast<cufftComplex *>(P->fine),
+                               reinterpret_cast<cufftComplex *>(P->fine),
+                               isign < 0 ? CUFFT_FORWARD : CUFFT_INVERSE);
+  if (r != CUFFT_SUCCESS) {
+    set_error("%s: cufftExecC2C failed (%d)", what, (int)r);
+    return SPF_ERR_CUDA;
+  }
+  count_launch();
+  return SPF_OK;
+}
+
+}  // namespace spf
+
+using namespace spf;
+
+extern "C" {
+
+int spf_nufft_plan_create(int m1, int m2, int m3, double eps, double upsampfac,
+                          spf_nufft_plan *out) {
+  SPF_REQUIRE(out != nullptr, "spf_nufft_plan_create: out is NULL");
+  *out = nullptr;
+  SPF_REQUIRE(m1 > 0 && m2 > 0 && m3 > 0 && m1 <= 4096 && m2 <= 4096 && m3 <= 4096,
+              "spf_nufft_plan_create: bad mode counts (%d, %d, %d)", m1, m2, m3);
+  SPF_REQUIRE(eps > 0 && eps < 1, "spf_nufft_plan_create: eps must be in (0, 1)");
+  double sigma = upsampfac <= 0 ? 2.0 : upsampfac;
+  SPF_REQUIRE(sigma >= 1.25 && sigma <= 4.0, "spf_nufft_plan_create: upsampfac out of range");
+  auto *P = new spf_nufft_plan_s();
+  cudaGetDevice(&P->dev);
+  P->m[0] = m1; P->m[1] = m2; P->m[2] = m3;
+  P->eps = eps;
+  P->sigma = sigma;
+  P->w = es_width(eps, sigma);
+  P->beta = es_beta(P->w, sigma);
+  P->pad = (P->w + 1) / 2 + 1;
+  for (int d = 0; d < 3; ++d) {
+    int md = P->m[d];
+    int want = (int)ceil(sigma * md);
+    if (want < 2 * P->w) want = 2 * P->w;
+    P->n[d] = next_smooth_even(want);
+    P->np[d] = P->n[d] + 2 * P->pad;
+  }
+  int st = SPF_OK;
+  size_t nfine = (size_t)P->n[0] * P->n[1] * P->n[2];
+  size_t npad = (size_t)P->np[0] * P->np[1] * P->np[2];
+  for (int d = 0; d < 3 && st == SPF_OK; ++d) {
+    auto v = inverse_kernel_ft(P->m[d], P->n[d], P->w, P->beta);
+    st = check_cuda(cudaMalloc(&P->inv_p[d], v.size() * sizeof(float)), "plan_create");
+    if (st == SPF_OK)
+      st = check_cuda(cudaMemcpy(P->inv_p[d], v.data(), v.size() * sizeof(float),
+                                 cudaMemcpyHostToDevice), "plan_create");
+  }
+  if (st == SPF_OK) st = check_cuda(cudaMalloc(&P->fine, nfine * sizeof(float2)), "plan_create");
+  if (st == SPF_OK) st = check_cuda(cudaMalloc(&P->re_pad, npad * sizeof(float)), "plan_create");
+  if (st == SPF_OK) st = check_cuda(cudaMalloc(&P->acc_pad, npad * sizeof(float)), "plan_create");
+  if (st == SPF_OK) {
+    cufftResult r = cufftPlan3d(&P->fft, P->n[0], P->n[1], P->n[2], CUFFT_C2C);
+    if (r != CUFFT_SUCCESS) {
+      set_error("plan_create: cufftPlan3d(%d,%d,%d) failed (%d)", P->n[0], P->n[1], P->n[2], (int)r);
+      st = r == CUFFT_ALLOC_FAILED ? SPF_ERR_OOM : SPF_ERR_CUDA;
+    } else {
+      P->fft_ok = true;
+    }
+  }
+  if (st != SPF_OK) {
+    spf_nufft_plan_destroy(P);
+    return st;
+  }
+  *out = P;
+  return SPF_OK;
+}
+
+int spf_nufft_plan_destroy(spf_nufft_plan P) {
+  if (!P) return SPF_OK;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != P->dev) cudaSetDevice(P->dev);
+  for (int d = 0; d < 3; ++d) cudaFree(P->inv_p[d]);
+  cudaFree(P->fine);
+  cudaFree(P->re_pad);
+  cudaFree(P->im_pad);
+  cudaFree(P->acc_pad);
+  if (P->fft_ok) cufftDestroy(P->fft);
+  if (prev != P->dev && prev >= 0) cudaSetDevice(prev);
+  delete P;
+  return SPF_OK;
+}
+
+int spf_nufft_plan_info(spf_nufft_plan P, int *n_fine, int *width, double *beta, int *n_padded) {
+  SPF_REQUIRE(P != nullptr, "spf_nufft_plan_info: plan is NULL");
+  for (int d = 0; d < 3; ++d) {
+    if (n_fine) n_fine[d] = P->n[d];
+    if (n_padded) n_padded[d] = P->np[d];
+  }
+  if (width) *width = P->w;
+  if (beta) *beta = P->beta;
+  return SPF_OK;
+}
+
+int spf_nufft_t2_set_modes(spf_nufft_plan P, const float *d_modes, const float *d_support,
+                           int isign, int want_imag, void *stream) {
+  SPF_TRY(check_plan(P, "spf_nufft_t2_set_modes"));
+  SPF_REQUIRE(d_modes != nullptr, "spf_nufft_t2_set_modes: modes is NULL");
+  SPF_REQUIRE(isign == 1 || isign == -1, "spf_nufft_t2_set_modes: isign must be +-1");
+  cudaStream_t s = as_stream(stream);
+  size_t nfine = (size_t)P->n[0] * P->n[1] * P->n[2];
+  size_t npad = (size_t)P->np[0] * P->np[1] * P->np[2];
+  if (want_imag && !P->im_pad)
+    SPF_TRY(check_cuda(cudaMalloc(&P->im_pad, npad * sizeof(float)), "spf_nufft_t2_set_modes"));
+  SPF_TRY(check_cuda(cudaMemsetAsync(P->fine, 0, nfine * sizeof(float2), s), "t2_set_modes"));
+  int64_t nm = (int64_t)P->m[0] * P->m[1] * P->m[2];
+  k_t2_scatter_modes<<<grid_for(nm, 256, 8 * 1024), 256, 0, s>>>(
+      d_modes, d_support, P->m[0], P->m[1], P->m[2], P->n[0], P->n[1], P->n[2], P->inv_p[0],
+      P->inv_p[1], P->inv_p[2], P->fine);
+  SPF_TRY(check_launch("k_t2_scatter_modes"));
+  SPF_TRY(fft_exec(P, isign, s, "spf_nufft_t2_set_modes"));
+  GridGeom g = geom_of(P);
+  k_t2_fill_padded<<<grid_for((int64_t)npad, 256, 16 * 1024), 256, 0, s>>>(
+      P->fine, g, 1.0f, P->re_pad, want_imag ? P->im_pad : nullptr);
+  return check_launch("k_t2_fill_padded");
+}
+
+int spf_nufft_t2_interp(spf_nufft_plan P, const float *d_x, const float *d_y, const float *d_z,
+                        int64_t npts, float *d_out_re, float *d_out_im, void *stream) {
+  SPF_TRY(check_plan(P, "spf_nufft_t2_interp"));
+  SPF_REQUIRE(npts >= 0, "spf_nufft_t2_interp: npts < 0");
+  if (npts == 0) return SPF_OK;
+  SPF_REQUIRE(d_x && d_y && d_z && d_out_re, "spf_nufft_t2_interp: NULL pointer");
+  SPF_REQUIRE(!d_out_im || P->im_pad,
+              "spf_nufft_t2_interp: imaginary output needs set_modes(want_imag=1)");
+  cudaStream_t s = as_stream(stream);
+  GridGeom g = geom_of(P);
+  int grid = grid_for(npts, 256, (int64_t)sm_count() * 16);
+  SPF_W_DISPATCH(P->w, (k_t2_interp<W><<<grid, 256, 0, s>>>(P->re_pad, P->im_pad, g, d_x, d_y,
+                                                               d_z, npts, d_out_re, d_out_im)));
+  return check_launch("k_t2_interp");
+}
+
+int spf_slice_t2(spf_nufft_plan P, const float *d_quats, int64_t n_orient, const float *d_ppr,
+                 int64_t n_pix, double scale, float *d_out, void *d_out_bf16, void *stream) {
+  SPF_TRY(check_plan(P, "spf_slice_t2"));
+  SPF_REQUIRE(n_orient >= 0 && n_pix >= 0, "spf_slice_t2: negative size");
+  if (n_orient == 0 || n_pix == 0) return SPF_OK;
+  SPF_REQUIRE(d_quats && d_ppr && d_out, "spf_slice_t2: NULL pointer");
+  SPF_REQUIRE(n_orient < (1LL << 31) && n_pix <= 65535LL * 256, "spf_slice_t2: size too large");
+  cudaStream_t s = as_stream(stream);
+  GridGeom g = geom_of(P);
+  float s1 = (float)(scale * P->n[0] / (2.0 * M_PI));
+  float s2 = (float)(scale * P->n[1] / (2.0 * M_PI));
+  float s3 = (float)(scale * P->n[2] / (2.0 * M_PI));
+  dim3 grid((unsigned)n_orient, (unsigned)((n_pix + 255) / 256));
+  auto *bf = reinterpret_cast<__nv_bfloat16 *>(d_out_bf16);
+  SPF_W_DISPATCH(P->w, (k_slice_t2<W><<<grid, 256, 0, s>>>(P->re_pad, g, d_quats, d_ppr, n_pix,
+                                                              s1, s2, s3, d_out, bf)));
+  return check_launch("k_slice_t2");
+}
+
+int spf_nufft_t1_zero(spf_nufft_plan P, void *stream) {
+  SPF_TRY(check_plan(P, "spf_nufft_t1_zero"));
+  size_t npad = (size_t)P->np[0] * P->np[1] * P->np[2];
+  return check_cuda(cudaMemsetAsync(P->acc_pad, 0, npad * sizeof(float), as_stream(stream)),
+                    "spf_nufft_t1_zero");
+}
+
+int spf_nufft_t1_spread(spf_nufft_plan P, const float *d_x, const float *d_y, const float *d_z,
+                        const float *d_c, int64_t npts, void *stream) {
+  SPF_TRY(check_plan(P, "spf_nufft_t1_spread"));
+  SPF_REQUIRE(npts >= 0, "spf_nufft_t1_spread: npts < 0");
+  if (npts == 0) return SPF_OK;
+  SPF_REQUIRE(d_x && d_y && d_z && d_c, "spf_nufft_t1_spread: NULL pointer");
+  cudaStream_t s = as_stream(stream);
+  GridGeom g = geom_of(P);
+  int grid = grid_for(npts, 256, (int64_t)sm_count() * 16);
+  SPF_W_DISPATCH(P->w, (k_t1_spread<W><<<grid, 256, 0, s>>>(P->acc_pad, g, d_x, d_y, d_z, d_c,
+                                                               npts)));
+  return check_launch("k_t1_spread");
+}
+
+int spf_nufft_t1_spread_orient(spf_nufft_plan P, const float *d_quats, int64_t n_orient,
+                               const float *d_ppr, int64_t n_pix, double scale, const float *d_c,
+                               void *stream) {
+  SPF_TRY(check_plan(P, "spf_nufft_t1_spread_orient"));
+  SPF_REQUIRE(n_orient >= 0 && n_pix >= 0, "spf_nufft_t1_spread_orient: negative size");
+  if (n_orient == 0 || n_pix == 0) return SPF_OK;
+  SPF_REQUIRE(d_quats && d_ppr && d_c, "spf_nufft_t1_spread_orient: NULL pointer");
+  SPF_REQUIRE(n_orient < (1LL << 31) && n_pix <= 65535LL * 256,
+              "spf_nufft_t1_spread_orient: size too large");
+  cudaStream_t s = as_stream(stream);
+  GridGeom g = geom_of(P);
+  float s1 = (float)(scale * P->n[0] / (2.0 * M_PI));
+  float s2 = (float)(scale * P->n[1] / (2.0 * M_PI));
+  float s3 = (float)(scale * P->n[2] / (2.0 * M_PI));
+  dim3 grid((unsigned)n_orient, (unsigned)((n_pix + 255) / 256));
+  SPF_W_DISPATCH(P->w, (k_t1_spread_orient<W><<<grid, 256, 0, s>>>(P->acc_pad, g, d_quats, d_ppr,
+                                                                      n_pix, s1, s2, s3, d_c)));
+  return check_launch("k_t1_spread_orient");
+}
+
+int spf_nufft_t1_finish(spf_nufft_plan P, int isign, float *d_out_re, float *d_out_im,
+                        void *stream) {
+  SPF_TRY(check_plan(P, "spf_nufft_t1_finish"));
+  SPF_REQUIRE(isign == 1 || isign == -1, "spf_nufft_t1_finish: isign must be +-1");
+  SPF_REQUIRE(d_out_re != nullptr, "spf_nufft_t1_finish: out_re is NULL");
+  cudaStream_t s = as_stream(stream);
+  GridGeom g = geom_of(P);
+  int64_t nfine = (int64_t)P->n[0] * P->n[1] * P->n[2];
+  k_t1_fold<<<grid_for(nfine, 256, 16 * 1024), 256, 0, s>>>(P->acc_pad, g, P->fine);
+  SPF_TRY(check_launch("k_t1_fold"));
+  SPF_TRY(fft_exec(P, isign, s, "spf_nufft_t1_finish"));
+  int64_t nm = (int64_t)P->m[0] * P->m[1] * P->m[2];
+  k_t1_extract<<<grid_for(nm, 256, 16 * 1024), 256, 0, s>>>(
+      P->fine, P->m[0], P->m[1], P->m[2], P->n[0], P->n[1], P->n[2], P->inv_p[0], P->inv_p[1],
+      P->inv_p[2], d_out_re, d_out_im);
+  return check_launch("k_t1_extract");
+}
+
+}  // extern "C"

@@ -1,0 +1,124 @@
+"""Device NUFFT plan (type 2 interpolation / type 1 spreading, ES kernel).
+
+Thin owner of a `spf_nufft_plan` from libspinifel_gb300.so.  All arrays are
+torch CUDA tensors; calls are asynchronous on the current torch stream.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import torch
+
+from . import _lib
+
+
+class NufftPlan:
+    def __init__(self, m, eps: float = 1e-6, upsampfac: float = 2.0,
+                 device: torch.device | int | None = None):
+        if isinstance(m, int):
+            m = (m, m, m)
+        self.m = tuple(int(v) for v in m)
+        self.eps = float(eps)
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None \
+            else torch.device("cuda", device if isinstance(device, int) else device.index or 0)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.call("spf_nufft_plan_create", self.m[0], self.m[1], self.m[2], self.eps,
+                      float(upsampfac), ctypes.byref(h))
+        self._h = h
+        n = (ctypes.c_int * 3)()
+        npad = (ctypes.c_int * 3)()
+        w = ctypes.c_int()
+        beta = ctypes.c_double()
+        _lib.call("spf_nufft_plan_info", h, n, ctypes.byref(w), ctypes.byref(beta), npad)
+        self.n_fine = tuple(n)
+        self.n_padded = tuple(npad)
+        self.width = w.value
+        self.beta = beta.value
+        self.has_modes = False
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            with torch.cuda.device(self.device):
+                _lib.lib().spf_nufft_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- type 2 ---------------------------------------------------------
+    def set_modes(self, modes: torch.Tensor, support: torch.Tensor | None = None,
+                  isign: int = -1, want_imag: bool = False):
+        modes = modes.to(device=self.device, dtype=torch.float32).contiguous()
+        if tuple(modes.shape) != self.m:
+            raise ValueError(f"modes shape {tuple(modes.shape)} != plan modes {self.m}")
+        sup = None
+        if support is not None and not (isinstance(support, (int, float)) and support == 1):
+            sup = torch.as_tensor(support, device=self.device, dtype=torch.float32)
+            sup = sup.expand(self.m).contiguous()
+        _lib.call("spf_nufft_t2_set_modes", self._h, _lib.ptr(modes), _lib.ptr(sup), int(isign),
+                  int(bool(want_imag)), _lib.stream_handle())
+        self._keep = (modes, sup)
+        self.has_modes = True
+        self.has_imag = bool(want_imag)
+
+    def interp(self, x: torch.Tensor, y: torch.Tensor, z: torch.Tensor, want_imag=False):
+        x, y, z = (t.to(device=self.device, dtype=torch.float32).contiguous().reshape(-1)
+                   for t in (x, y, z))
+        n = x.numel()
+        re = torch.empty(n, device=self.device, dtype=torch.float32)
+        im = torch.empty(n, device=self.device, dtype=torch.float32) if want_imag else None
+        _lib.call("spf_nufft_t2_interp", self._h, _lib.ptr(x), _lib.ptr(y), _lib.ptr(z), n,
+                  _lib.ptr(re), _lib.ptr(im), _lib.stream_handle())
+        return re, im
+
+    def slice(self, quats: torch.Tensor, ppr: torch.Tensor, scale: float,
+              out: torch.Tensor | None = None, out_bf16: torch.Tensor | None = None):
+        """Slices [n_orient, n_pix] (real part) at the given orientations."""
+        quats = quats.to(device=self.device, dtype=torch.float32).contiguous()
+        ppr = ppr.to(device=self.device, dtype=torch.float32).contiguous().reshape(3, -1)
+        n_o, n_p = quats.shape[0], ppr.shape[1]
+        if out is None:
+            out = torch.empty(n_o, n_p, device=self.device, dtype=torch.float32)
+        _lib.require_cuda(out, "out", torch.float32)
+        if out.numel() != n_o * n_p:
+            raise ValueError("out has the wrong size")
+        if out_bf16 is not None:
+            _lib.require_cuda(out_bf16, "out_bf16", torch.bfloat16)
+        _lib.call("spf_slice_t2", self._h, _lib.ptr(quats), n_o, _lib.ptr(ppr), n_p,
+                  float(scale), _lib.ptr(out), _lib.ptr(out_bf16), _lib.stream_handle())
+        return out
+
+    # ---- type 1 ---------------------------------------------------------
+    def spread_zero(self):
+        _lib.call("spf_nufft_t1_zero", self._h, _lib.stream_handle())
+
+    def spread(self, x, y, z, c):
+        x, y, z, c = (t.to(device=self.device, dtype=torch.float32).contiguous().reshape(-1)
+                      for t in (x, y, z, c))
+        _lib.call("spf_nufft_t1_spread", self._h, _lib.ptr(x), _lib.ptr(y), _lib.ptr(z),
+                  _lib.ptr(c), x.numel(), _lib.stream_handle())
+
+    def spread_orient(self, quats, ppr, scale, c):
+        quats = quats.to(device=self.device, dtype=torch.float32).contiguous()
+        ppr = ppr.to(device=self.device, dtype=torch.float32).contiguous().reshape(3, -1)
+        c = c.to(device=self.device, dtype=torch.float32).contiguous()
+        if c.numel() != quats.shape[0] * ppr.shape[1]:
+            raise ValueError("strengths must be n_orient * n_pix")
+        _lib.call("spf_nufft_t1_spread_orient", self._h, _lib.ptr(quats), quats.shape[0],
+                  _lib.ptr(ppr), ppr.shape[1], float(scale), _lib.ptr(c), _lib.stream_handle())
+
+    def finish(self, isign: int = 1, want_imag=False):
+        re = torch.empty(self.m, device=self.device, dtype=torch.float32)
+        im = torch.empty(self.m, device=self.device, dtype=torch.float32) if want_imag else None
+        _lib.call("spf_nufft_t1_finish", self._h, int(isign), _lib.ptr(re), _lib.ptr(im),
+                  _lib.stream_handle())
+        return re, im

@@ -1,0 +1,74 @@
+"""Seeded inputs of the golden cases, shared by make_golden.py (which runs the
+reference on them) and the tests (which run spinifel_gb300 on them).  Only
+numpy is used, so the inputs are identical on every machine."""
+from __future__ import annotations
+
+import numpy as np
+
+QUAT_SEED = 7001
+
+NN = dict(seed=7002, n_ref=512, n_img=1024, n_pix=16384)  # tests/test_OM.py:51-56 shape
+SNM = dict(seed=7003, M=21, det_shape=(4, 16, 16), n_orient=300, batch=100, n_images=64,
+           photons=2.0)
+OPS = dict(seed=7004, M=15, npts=2000)
+MERGE = dict(seed=7005, M=15, det_shape=(4, 8, 8), n_images=40, maxiter=20, photons=2.0)
+
+
+def nn_inputs():
+    rng = np.random.default_rng(NN["seed"])
+    model_slices = rng.random((NN["n_ref"], NN["n_pix"]))
+    slices = rng.random((NN["n_img"], NN["n_pix"]))
+    return model_slices, slices
+
+
+def _geometry(det_shape):
+    from spinifel_gb300 import geom
+
+    return geom.flat_detector(det_shape[0], det_shape[1], det_shape[2])
+
+
+def _images(model, quats, ppr, pdr, photons, rng):
+    from oracle import nufft as onufft
+    from spinifel_gb300 import geom
+
+    mult = np.pi / pdr.max()
+    H, K, L = geom.hkl(quats, ppr)
+    s = onufft.nufft3d2(H.reshape(-1) * mult, K.reshape(-1) * mult, L.reshape(-1) * mult,
+                        model, -1, 1e-12).real
+    s = np.maximum(s, 0).reshape((len(quats),) + ppr.shape[1:])
+    lam = s * (photons / s.mean())
+    return rng.poisson(lam).astype(np.float64)
+
+
+def snm_inputs():
+    from spinifel_gb300 import geom, synth
+
+    rng = np.random.default_rng(SNM["seed"])
+    ac = synth.intensity_model(SNM["M"], seed=SNM["seed"])
+    ppr, pdr = _geometry(SNM["det_shape"])
+    quats = geom.uniform_quaternions(SNM["n_orient"], rng)
+    img_q = geom.uniform_quaternions(SNM["n_images"], rng)
+    slices_ = _images(ac, img_q, ppr, pdr, SNM["photons"], rng)
+    return ac, ppr, pdr, quats, slices_
+
+
+def ops_inputs():
+    rng = np.random.default_rng(OPS["seed"])
+    M = OPS["M"]
+    ugrid = rng.standard_normal((M, M, M))
+    sup = (rng.random((M, M, M)) > 0.3).astype(np.float64)
+    H_, K_, L_ = rng.uniform(-np.pi, np.pi, (3, OPS["npts"]))
+    nuv = rng.standard_normal(OPS["npts"])
+    return ugrid, sup, H_, K_, L_, nuv
+
+
+def merge_inputs():
+    from spinifel_gb300 import geom, synth
+
+    rng = np.random.default_rng(MERGE["seed"])
+    model = synth.intensity_model(MERGE["M"], seed=MERGE["seed"])
+    ppr, pdr = _geometry(MERGE["det_shape"])
+    orient = geom.uniform_quaternions(MERGE["n_images"], rng)
+    data = _images(model, orient, ppr, pdr, MERGE["photons"], rng)
+    ac_est = model.copy()
+    return data, ppr, pdr, orient, ac_est

@@ -1,0 +1,250 @@
+"""Generate the golden fixtures in tests/golden/ by running the reference's own
+Python code (spinifel, mounted read-only at /root/reference in the build
+container) on seeded inputs.
+
+The reference cannot be installed as-is here: finufft/cufinufft, skopi,
+PyNVTX, callmonitor, toml and matplotlib are absent.  This script stubs only
+those imports (identity decorators, tomllib for toml, a Shoemake quaternion
+sampler and the eval/geom.py rotation formula for skopi, the FP64 ES oracle of
+oracle/nufft.py for the un-vendored finufft) and then calls, unmodified:
+
+  * spinifel.sequential.nearest_neighbor.nearest_neighbor (CPU branch:
+    sklearn euclidean_distances + argmin)            -> golden_nn.npz
+  * spinifel.sequential.orientation_matching.SNM.slicing_and_match
+    (numpy/scipy-dgemm branch)                       -> golden_snm.npz
+  * spinifel.sequential.orientation_matching.slicing_and_match
+    (function path, global std, nearest_neighbor)   -> golden_sam.npz
+  * spinifel.sequential.autocorrelation.Merge.solve_ac (scipy cg)
+                                                     -> golden_merge.npz
+  * spinifel.autocorrelation.forward / adjoint glue  -> golden_ops.npz
+
+Inputs are regenerated from the stored seeds by tests (numpy PCG64 streams are
+stable), so only small outputs are committed.  Run in the build container:
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+import tempfile
+import tomllib
+import types
+
+import numpy as np
+
+REF = "/root/reference"
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from oracle import nufft as onufft  # noqa: E402
+from tests.golden import cases  # noqa: E402
+
+
+def _stub_modules(quat_seed: int):
+    def annotate(*a, **k):
+        def deco(f):
+            return f
+        return deco
+
+    nvtx = types.ModuleType("PyNVTX")
+    nvtx.annotate = annotate
+    nvtx.RangePushA = lambda *a, **k: None
+    nvtx.RangePop = lambda *a, **k: None
+    sys.modules["PyNVTX"] = nvtx
+
+    cm = types.ModuleType("callmonitor")
+    cm.intercept = lambda f: f
+    sys.modules["callmonitor"] = cm
+
+    toml = types.ModuleType("toml")
+    toml.load = lambda path: tomllib.load(open(path, "rb"))
+    sys.modules["toml"] = toml
+
+    mpl = types.ModuleType("matplotlib")
+    plt = types.ModuleType("matplotlib.pyplot")
+    mcm = types.ModuleType("matplotlib.cm")
+    mcol = types.ModuleType("matplotlib.colors")
+    mcol.LogNorm = mcol.SymLogNorm = object
+    mpl.pyplot, mpl.cm, mpl.colors = plt, mcm, mcol
+    sys.modules.update({"matplotlib": mpl, "matplotlib.pyplot": plt, "matplotlib.cm": mcm,
+                        "matplotlib.colors": mcol})
+
+    from spinifel_gb300 import geom
+
+    skp = types.ModuleType("skopi")
+    skp.quaternion2rot3d = lambda q: geom.quaternion2rot3d(np.asarray(q))
+    rng = np.random.default_rng(quat_seed)
+    skp.get_uniform_quat = lambda n, avoid_symmetric=True: geom.uniform_quaternions(n, rng)
+    skp.get_random_quat = lambda n: geom.uniform_quaternions(n, rng)
+    sys.modules["skopi"] = skp
+
+    # spinifel.extern: the package __init__ imports cufinufft unconditionally;
+    # provide the two functions autocorrelation.py takes from it (finufft
+    # call convention: nufft_3d_t2(x, y, z, ugrid, sign, eps, n),
+    # nufft_3d_t1(x, y, z, nuvect, sign, eps, nx, ny, nz)).
+    ext = types.ModuleType("spinifel.extern")
+    ext.__path__ = [os.path.join(REF, "spinifel", "extern")]
+
+    def t2(x, y, z, ugrid, sign, eps, n):
+        out = onufft.nufft3d2(x, y, z, ugrid, sign, 1e-12)
+        assert out.size == n
+        return out
+
+    def t1(x, y, z, nuvect, sign, eps, nx, ny, nz):
+        return onufft.nufft3d1(x, y, z, nuvect, (nx, ny, nz), sign, 1e-12)
+
+    ext.nufft_3d_t1, ext.nufft_3d_t2 = t1, t2
+    sys.modules["spinifel.extern"] = ext
+
+    # spinifel.sequential/__init__.py only imports the CLI driver (main.py:
+    # HDF5 and psana readers, the cufinufft/finufft dispatch); load the
+    # package's modules without running it.
+    seq = types.ModuleType("spinifel.sequential")
+    seq.__path__ = [os.path.join(REF, "spinifel", "sequential")]
+    sys.modules["spinifel.sequential"] = seq
+
+
+def _settings_file(c: dict) -> str:
+    det = "[" + ", ".join(str(v) for v in c["det_shape"]) + "]"
+    text = f"""
+[debug]
+verbose = false
+use_callmonitor = false
+[runtime]
+N_images_per_rank = {c.get("n_images", 10)}
+use_cuda = false
+use_cufinufft = false
+use_cupy = false
+use_single_prec = false
+[algorithm]
+N_clipping = 0
+N_binning = 0
+N_orientations = {c["n_orient"]}
+N_batch_size = {c["batch"]}
+oversampling = 1
+solve_ac_maxiter = {c.get("maxiter", 100)}
+[detector]
+shape = {det}
+"""
+    fd, path = tempfile.mkstemp(suffix=".toml")
+    with os.fdopen(fd, "w") as f:
+        f.write(text)
+    return path
+
+
+class OracleNUFFT:
+    """Stands in for spinifel.extern.nufft_ext.NUFFT (finufft 2.1 branch,
+    nufft_ext.py:420-487) with the FP64 ES oracle at eps 1e-12."""
+
+    def __init__(self, ref_orientations, ppr, pdr, oversampling=1):
+        from spinifel_gb300 import geom
+
+        self.ref_orientations = ref_orientations
+        self.mult = np.pi / (oversampling * pdr.max())
+        H, K, L = geom.hkl(ref_orientations, ppr)
+        self.HKL = np.stack([H, K, L]).reshape(3, len(ref_orientations), -1) * self.mult
+
+    def forward(self, ugrid, st, en, support, use_recip_sym, N):
+        H_, K_, L_ = (self.HKL[i, st:en].reshape(-1) for i in range(3))
+        if support is not None:
+            ugrid = ugrid * support
+        return onufft.nufft3d2(H_, K_, L_, ugrid, -1, 1e-12)
+
+    def adjoint(self, nuvect, H_, K_, L_, support, use_reciprocal_symmetry, M):
+        ugrid = onufft.nufft3d1(H_, K_, L_, np.asarray(nuvect), (M, M, M), -1, 1e-12)
+        ugrid = ugrid * support
+        if use_reciprocal_symmetry:
+            ugrid = ugrid.real
+        return ugrid / M ** 3
+
+
+class _GetArray(np.ndarray):
+    def get(self):
+        return np.asarray(self)
+
+
+def main():
+    sys.path.insert(0, REF)
+    _stub_modules(cases.QUAT_SEED)
+
+    # --- nearest_neighbor (CPU branch) --------------------------------------
+    c = cases.NN
+    sys.argv = ["spinifel", "--mode=sequential", "--settings=" + _settings_file(
+        {"det_shape": (1, 1, c["n_pix"]), "n_orient": c["n_ref"], "batch": c["n_ref"]})]
+    import spinifel.sequential.nearest_neighbor as rnn
+
+    model_slices, slices = cases.nn_inputs()
+    idx = rnn.nearest_neighbor(model_slices, slices, c["n_ref"])
+    np.savez_compressed(os.path.join(HERE, "golden_nn.npz"), index=idx.astype(np.int32))
+    print("nn", idx[:10])
+
+    # --- SNM and the function path -------------------------------------------
+    s = cases.SNM
+    from spinifel import SpinifelSettings
+    st = SpinifelSettings()
+    # refresh the singleton with this case's settings file
+    sys.argv = ["spinifel", "--mode=sequential", "--settings=" + _settings_file(
+        {"det_shape": s["det_shape"], "n_orient": s["n_orient"], "batch": s["batch"]})]
+    st._SpinifelSettings__toml = sys.argv[2].split("=", 1)[1]
+    st._SpinifelSettings__params = []
+    st.refresh()
+    import spinifel.sequential.orientation_matching as rom
+
+    ac, ppr, pdr, quats, slices_ = cases.snm_inputs()
+    nufft = OracleNUFFT(quats, ppr, pdr)
+    snm = rom.SNM(st, slices_, ppr, pdr, nufft)
+    q_snm = snm.slicing_and_match(ac.copy())
+    idx_snm = np.array([np.flatnonzero((quats == q).all(axis=1))[0] for q in q_snm])
+    dist = np.array(snm.dist)
+    np.savez_compressed(os.path.join(HERE, "golden_snm.npz"), index=idx_snm.astype(np.int32),
+                        dist=dist.astype(np.float64))
+    print("snm", idx_snm[:10])
+
+    q_sam = rom.slicing_and_match(ac.copy(), slices_, ppr, pdr, ref_orientations=quats)
+    idx_sam = np.array([np.flatnonzero((quats == q).all(axis=1))[0] for q in q_sam])
+    np.savez_compressed(os.path.join(HERE, "golden_sam.npz"), index=idx_sam.astype(np.int32))
+    print("sam", idx_sam[:10])
+
+    # --- forward / adjoint glue ---------------------------------------------
+    import spinifel.autocorrelation as rac
+
+    o = cases.OPS
+    ugrid, sup, H_, K_, L_, nuv = cases.ops_inputs()
+    fwd = rac.forward(ugrid.copy(), H_, K_, L_, sup, True, H_.size)
+    adj = rac.adjoint(nuv, H_, K_, L_, o["M"], True, sup)
+    np.savez_compressed(os.path.join(HERE, "golden_ops.npz"), forward=fwd, adjoint=adj)
+    print("ops", fwd[:3], adj.ravel()[:3])
+
+    # --- Merge.solve_ac --------------------------------------------------------
+    g = cases.MERGE
+    sys.argv = ["spinifel", "--mode=sequential", "--settings=" + _settings_file(
+        {"det_shape": g["det_shape"], "n_orient": 10, "batch": 10, "maxiter": g["maxiter"]})]
+    st._SpinifelSettings__toml = sys.argv[2].split("=", 1)[1]
+    st.refresh()
+    st._M_override = g["M"]
+    import spinifel.sequential.autocorrelation as rsac
+
+    # Merge reads settings.M / M_ups (Mquat-derived); patch the properties for
+    # the small test grid
+    type(st).M = property(lambda self: g["M"])
+    type(st).M_ups = property(lambda self: 2 * g["M"])
+    orig_cg = rsac.cg
+
+    def cg_get(*a, **k):
+        x, info = orig_cg(*a, **k)
+        return x.view(_GetArray), info
+
+    rsac.cg = cg_get
+    data, ppr, pdr, orient, ac_est = cases.merge_inputs()
+    mquats = orient
+    nufft_m = OracleNUFFT(mquats, ppr, pdr)
+    merge = rsac.Merge(st, data, ppr, pdr, nufft_m)
+    ac_out = merge.solve_ac(0, orient, ac_est.copy())
+    np.savez_compressed(os.path.join(HERE, "golden_merge.npz"), ac=ac_out,
+                        iterations=np.array(merge.callback.counter))
+    print("merge", ac_out.ravel()[:4], merge.callback.counter)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,184 @@
+"""Parity of the CUDA NUFFT kernels (type 2 interpolation / slicing, type 1
+spreading) with the FP64 oracle; tolerance: relative L2 error <= 1e-5 at
+eps = 1e-6 (FP32 on the device)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import nufft as onufft
+from tests.golden import cases
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+@pytest.fixture(scope="module")
+def dev(lib):
+    return torch.device("cuda", 0)
+
+
+def t(a, dev, dtype=torch.float32):
+    return torch.as_tensor(np.asarray(a), dtype=dtype, device=dev)
+
+
+@pytest.mark.parametrize("m", [(9, 9, 9), (10, 11, 12), (21, 21, 21)])
+@pytest.mark.parametrize("isign", [-1, 1])
+def test_type2_interp_matches_direct_sum(dev, m, isign):
+    from spinifel_gb300.nufft import NufftPlan
+
+    rng = np.random.default_rng(10)
+    f = rng.standard_normal(m)
+    x, y, z = rng.uniform(-3 * np.pi + 1e-3, 3 * np.pi - 1e-3, (3, 3000)).astype(np.float32)
+    P = NufftPlan(m, 1e-6)
+    P.set_modes(t(f, dev), isign=isign, want_imag=True)
+    re, im = P.interp(t(x, dev), t(y, dev), t(z, dev), want_imag=True)
+    got = re.cpu().numpy() + 1j * im.cpu().numpy()
+    exact = onufft.nudft3d2(x, y, z, f, isign)
+    assert rel(got, exact) < TOL
+
+
+def test_type2_support_multiplies_modes(dev):
+    from spinifel_gb300.nufft import NufftPlan
+
+    rng = np.random.default_rng(11)
+    m = (11, 11, 11)
+    f = rng.standard_normal(m)
+    sup = (rng.random(m) > 0.5).astype(np.float64)
+    x, y, z = rng.uniform(-np.pi, np.pi, (3, 1000)).astype(np.float32)
+    P = NufftPlan(m, 1e-6)
+    P.set_modes(t(f, dev), t(sup, dev))
+    re, _ = P.interp(t(x, dev), t(y, dev), t(z, dev))
+    assert rel(re.cpu().numpy(), onufft.nudft3d2(x, y, z, f * sup, -1).real) < TOL
+
+
+@pytest.mark.parametrize("m", [(9, 9, 9), (8, 10, 7), (30, 30, 30)])
+@pytest.mark.parametrize("isign", [-1, 1])
+def test_type1_spread_matches_direct_sum(dev, m, isign):
+    from spinifel_gb300.nufft import NufftPlan
+
+    rng = np.random.default_rng(12)
+    x, y, z = rng.uniform(-3 * np.pi + 1e-3, 3 * np.pi - 1e-3, (3, 4000)).astype(np.float32)
+    c = rng.standard_normal(4000).astype(np.float32)
+    P = NufftPlan(m, 1e-6)
+    P.spread_zero()
+    P.spread(t(x, dev), t(y, dev), t(z, dev), t(c, dev))
+    re, im = P.finish(isign, want_imag=True)
+    got = re.cpu().numpy() + 1j * im.cpu().numpy()
+    exact = onufft.nudft3d1(x, y, z, c, m, isign)
+    assert rel(got, exact) < TOL
+
+
+def test_type1_is_adjoint_of_type2(dev):
+    from spinifel_gb300.nufft import NufftPlan
+
+    rng = np.random.default_rng(13)
+    m = (12, 12, 12)
+    f = rng.standard_normal(m)
+    x, y, z = rng.uniform(-np.pi, np.pi, (3, 5000)).astype(np.float32)
+    c = rng.standard_normal(5000).astype(np.float32)
+    P = NufftPlan(m, 1e-6)
+    P.set_modes(t(f, dev), isign=-1, want_imag=True)
+    re, im = P.interp(t(x, dev), t(y, dev), t(z, dev), want_imag=True)
+    P.spread_zero()
+    P.spread(t(x, dev), t(y, dev), t(z, dev), t(c, dev))
+    fr, fi = P.finish(+1, want_imag=True)
+    lhs = np.vdot(c, re.cpu().numpy() + 1j * im.cpu().numpy())
+    rhs = np.vdot(fr.cpu().numpy() + 1j * fi.cpu().numpy(), f)
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+
+
+def _slice_case(M, det, n_orient, seed):
+    from spinifel_gb300 import geom, synth
+
+    rng = np.random.default_rng(seed)
+    model = synth.intensity_model(M, seed=seed)
+    ppr, pdr = geom.flat_detector(*det)
+    quats = geom.uniform_quaternions(n_orient, rng).astype(np.float32)
+    return model, ppr, pdr, quats
+
+
+def _oracle_slices(model, ppr, pdr, quats, eps=1e-12):
+    from spinifel_gb300 import geom
+
+    mult = np.pi / pdr.max()
+    H, K, L = geom.hkl(quats.astype(np.float64), ppr)
+    return onufft.nufft3d2(H.reshape(-1) * mult, K.reshape(-1) * mult, L.reshape(-1) * mult,
+                           model, -1, eps).real.reshape(len(quats), -1)
+
+
+def test_slice_matches_oracle_config1_geometry(dev):
+    """41^3 model, 4 x 32 x 32 detector (the CPU-runnable configuration)."""
+    from spinifel_gb300.nufft import NufftPlan
+
+    model, ppr, pdr, quats = _slice_case(41, (4, 32, 32), 300, 20)
+    P = NufftPlan(41, 1e-6)
+    P.set_modes(t(model, dev))
+    bf = torch.empty(300, ppr[0].size, dtype=torch.bfloat16, device=dev)
+    got = P.slice(t(quats, dev), t(ppr.reshape(3, -1), dev), np.pi / pdr.max(), out_bf16=bf)
+    exact = _oracle_slices(model, ppr, pdr, quats)
+    assert rel(got.cpu().numpy(), exact) < TOL
+    assert torch.equal(bf, got.to(torch.bfloat16))
+
+
+def test_slice_full_size_subset_and_linearity(dev):
+    """81^3 model, 4 x 128 x 128 detector: a subset of orientations against the
+    oracle, and linearity in the model at full batch size."""
+    from spinifel_gb300.nufft import NufftPlan
+
+    model, ppr, pdr, quats = _slice_case(81, (4, 128, 128), 512, 21)
+    ppr_t = t(ppr.reshape(3, -1), dev)
+    mult = np.pi / pdr.max()
+    P = NufftPlan(81, 1e-6)
+    P.set_modes(t(model, dev))
+    full = P.slice(t(quats, dev), ppr_t, mult)
+    sub = [0, 7, 511]
+    exact = _oracle_slices(model, ppr, pdr, quats[sub], eps=1e-9)
+    assert rel(full[sub].cpu().numpy(), exact) < TOL
+    rng = np.random.default_rng(22)
+    g = rng.standard_normal(model.shape)
+    P.set_modes(t(g, dev))
+    sg = P.slice(t(quats, dev), ppr_t, mult)
+    P.set_modes(t(2.0 * model - 3.0 * g, dev))
+    comb = P.slice(t(quats, dev), ppr_t, mult)
+    lin = 2.0 * full.double() - 3.0 * sg.double()
+    assert float((comb.double() - lin).norm() / lin.norm()) < 1e-6
+
+
+def test_spread_orient_equals_spread_points(dev):
+    from spinifel_gb300 import geom
+    from spinifel_gb300.nufft import NufftPlan
+
+    model, ppr, pdr, quats = _slice_case(15, (4, 16, 16), 20, 23)
+    mult = np.pi / pdr.max()
+    rng = np.random.default_rng(24)
+    c = rng.poisson(2.0, (20, ppr[0].size)).astype(np.float32)
+    P = NufftPlan(15, 1e-6)
+    P.spread_zero()
+    P.spread_orient(t(quats, dev), t(ppr.reshape(3, -1), dev), mult, t(c, dev))
+    a, _ = P.finish(+1)
+    H, K, L = geom.hkl(quats.astype(np.float64), ppr)
+    P.spread_zero()
+    P.spread(*(t(v.reshape(-1) * mult, dev) for v in (H, K, L)), t(c, dev))
+    b, _ = P.finish(+1)
+    assert rel(a.cpu().numpy(), b.cpu().numpy()) < 1e-5
+
+
+def test_operator_glue_matches_reference_golden(dev):
+    """autocorrelation.forward / adjoint against the reference's own glue
+    (support, real part, / M^3) run on the FP64 oracle."""
+    from spinifel_gb300 import autocorrelation as ac
+
+    ugrid, sup, H_, K_, L_, nuv = cases.ops_inputs()
+    g = np.load(os.path.join(GOLD, "golden_ops.npz"))
+    fwd = ac.forward(ugrid.copy(), H_, K_, L_, sup, True, H_.size)
+    adj = ac.adjoint(nuv, H_, K_, L_, cases.OPS["M"], True, sup)
+    assert rel(fwd, g["forward"]) < TOL
+    assert rel(adj, g["adjoint"]) < TOL
+    assert adj.dtype in (np.float32, np.float64) and adj.shape == (15, 15, 15)

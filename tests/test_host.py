@@ -1,0 +1,93 @@
+"""Host-side logic that needs no GPU: settings, geometry, synthetic inputs,
+and the C ABI library (it loads, exports every declared symbol, and rejects
+bad arguments before touching the device)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from spinifel_gb300 import Settings, geom, synth
+
+
+def test_settings_derived_values():
+    s = Settings()
+    assert s.Mquat == 20 and s.M == 81 and s.M_ups == 162
+    assert Settings(oversampling=2).M == 161
+    assert Settings(det_shape=(4, 512, 512)).reduced_det_shape == (4, 16, 16)
+    assert Settings(det_shape=(4, 128, 128), N_clipping=0, N_binning=0).reduced_det_shape == \
+        (4, 128, 128)
+    assert Settings(M_override=151).M_ups == 302
+
+
+def test_rotations_orthonormal_and_inverse():
+    rng = np.random.default_rng(0)
+    q = geom.uniform_quaternions(100, rng)
+    np.testing.assert_allclose(np.linalg.norm(q, axis=1), 1.0, atol=1e-12)
+    R = geom.quaternion2rot3d(q)
+    np.testing.assert_allclose(R @ np.swapaxes(R, 1, 2), np.broadcast_to(np.eye(3), R.shape),
+                               atol=1e-12)
+    np.testing.assert_allclose(np.linalg.det(R), 1.0, atol=1e-12)
+    Rinv = geom.inverse_rotmats(q)
+    np.testing.assert_allclose(Rinv, np.linalg.inv(R), atol=1e-12)
+
+
+def test_hkl_matches_reference_einsum():
+    rng = np.random.default_rng(1)
+    q = geom.uniform_quaternions(5, rng)
+    ppr, _ = geom.flat_detector(4, 3, 2)
+    H, K, L = geom.hkl(q, ppr)
+    Rinv = np.array([np.linalg.inv(geom.quaternion2rot3d(x)) for x in q])
+    H2, K2, L2 = np.einsum("ijk,klmn->jilmn", Rinv, ppr)
+    np.testing.assert_allclose(H, H2)
+    np.testing.assert_allclose(L, L2)
+
+
+def test_detector_and_model():
+    ppr, pdr = geom.flat_detector(4, 32, 32)
+    assert ppr.shape == (3, 4, 32, 32) and pdr.shape == (4, 32, 32)
+    np.testing.assert_allclose(np.sqrt((ppr ** 2).sum(0)), pdr)
+    # Ewald sphere: |q + k0|^2 == |k0|^2
+    k0 = 1 / 2.5e-10
+    np.testing.assert_allclose(ppr[0] ** 2 + ppr[1] ** 2 + (ppr[2] + k0) ** 2, k0 ** 2, rtol=1e-10)
+    I = synth.intensity_model(15, seed=3)
+    assert I.shape == (15, 15, 15) and I.max() == 1.0 and I.min() >= 0
+    np.testing.assert_allclose(I, I[::-1, ::-1, ::-1], rtol=1e-9, atol=1e-12)  # Friedel
+
+
+def test_library_exports_every_header_symbol(lib):
+    from spinifel_gb300 import _lib
+
+    declared = _lib.header_symbols()
+    assert len(declared) >= 20
+    for name in declared:
+        assert hasattr(lib, name), f"{name} declared in the header but not exported"
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+    assert lib.spf_version().decode().startswith("spinifel_gb300")
+
+
+def test_library_rejects_bad_arguments_without_a_device(lib):
+    from spinifel_gb300 import _lib
+
+    h = ctypes.c_void_p()
+    assert lib.spf_nufft_plan_create(0, 8, 8, 1e-6, 2.0, ctypes.byref(h)) == _lib.SPF_ERR_ARG
+    assert b"bad mode counts" in lib.spf_last_error()
+    assert lib.spf_nufft_plan_create(8, 8, 8, 0.0, 2.0, ctypes.byref(h)) == _lib.SPF_ERR_ARG
+    assert lib.spf_knn_topk_f32(None, 4, 10, 0, None, None) == _lib.SPF_ERR_ARG
+    assert lib.spf_knn_topk_f32(None, 4, 10, 33, None, None) == _lib.SPF_ERR_ARG
+    assert lib.spf_dist_argmin_f32(None, None, -1, None, None, 4, 4, 0, None, None) == \
+        _lib.SPF_ERR_ARG
+    # empty inputs are a no-op, not an error
+    assert lib.spf_knn_eudist_f32(None, None, 0, 5, 16, None, None) == _lib.SPF_OK
+    assert lib.spf_status_string(_lib.SPF_ERR_TIMEOUT) == b"device wait timed out"
+
+
+def test_product_path_has_no_cpu_fallback(tmp_path):
+    from spinifel_gb300 import _lib
+
+    with pytest.raises(ImportError, match="no CPU fallback"):
+        _lib._lib_backup = _lib._lib
+        try:
+            _lib._lib = None
+            _lib.load(str(tmp_path / "missing.so"))
+        finally:
+            _lib._lib = _lib._lib_backup

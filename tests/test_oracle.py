@@ -1,0 +1,121 @@
+"""The oracle pinned: the FP64 ES NUFFT against exact direct sums, and the
+oracle's matching / merge restatements against golden outputs that the
+reference's own code produced (tests/golden/make_golden.py)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import matching as om
+from oracle import merge as omerge
+from oracle import nufft as onufft
+from tests.golden import cases
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.mark.parametrize("m", [(9, 10, 11), (7, 7, 7), (12, 8, 5)])
+@pytest.mark.parametrize("isign", [-1, 1])
+def test_es_type2_matches_direct_sum(m, isign):
+    rng = np.random.default_rng(1)
+    f = rng.standard_normal(m) + 1j * rng.standard_normal(m)
+    x, y, z = rng.uniform(-np.pi, np.pi, (3, 400))
+    exact = onufft.nudft3d2(x, y, z, f, isign)
+    for eps, tol in ((1e-12, 1e-11), (1e-6, 5e-6)):
+        c = onufft.nufft3d2(x, y, z, f, isign, eps)
+        assert np.linalg.norm(c - exact) / np.linalg.norm(exact) < tol
+
+
+@pytest.mark.parametrize("isign", [-1, 1])
+def test_es_type1_matches_direct_sum(isign):
+    rng = np.random.default_rng(2)
+    m = (8, 9, 10)
+    x, y, z = rng.uniform(-3 * np.pi + 0.01, 3 * np.pi - 0.01, (3, 300))  # full finufft domain
+    c = rng.standard_normal(300) + 1j * rng.standard_normal(300)
+    exact = onufft.nudft3d1(x, y, z, c, m, isign)
+    f = onufft.nufft3d1(x, y, z, c, m, isign, 1e-12)
+    assert np.linalg.norm(f - exact) / np.linalg.norm(exact) < 1e-11
+
+
+def test_direct_sum_convention():
+    """H runs along axis 0, modes centred at m//2, isign -1 in the exponent."""
+    rng = np.random.default_rng(3)
+    f = np.zeros((5, 6, 7), dtype=complex)
+    f[4, 1, 3] = 1.0  # k = (2, -2, 0)
+    x, y, z = rng.uniform(-np.pi, np.pi, (3, 10))
+    c = onufft.nudft3d2(x, y, z, f, -1)
+    np.testing.assert_allclose(c, np.exp(-1j * (2 * x - 2 * y)), atol=1e-14)
+
+
+def test_adjoint_is_transpose_of_forward():
+    rng = np.random.default_rng(4)
+    m = (6, 7, 8)
+    x, y, z = rng.uniform(-np.pi, np.pi, (3, 200))
+    f = rng.standard_normal(m) + 1j * rng.standard_normal(m)
+    c = rng.standard_normal(200) + 1j * rng.standard_normal(200)
+    lhs = np.vdot(c, onufft.nufft3d2(x, y, z, f, -1))
+    rhs = np.vdot(onufft.nufft3d1(x, y, z, c, m, +1), f)
+    assert abs(lhs - rhs) / abs(lhs) < 1e-11
+
+
+def test_oracle_nn_matches_reference_golden():
+    model_slices, slices = cases.nn_inputs()
+    gold = np.load(os.path.join(GOLD, "golden_nn.npz"))["index"]
+    idx, d = om.sklearn_argmin(model_slices, slices)
+    assert np.all(om.ties_equal(idx, gold, d))
+
+
+def test_oracle_knn_semantics():
+    rng = np.random.default_rng(5)
+    ref = rng.random((40, 37))
+    data = rng.random((30, 37))
+    d = onufft.knn_eudist(ref, data)
+    used = (37 // 16) * 16
+    exact = ((data[:, None, :used] - ref[None, :, :used]) ** 2).sum(-1)
+    np.testing.assert_allclose(d, exact, rtol=1e-12)
+    dist = np.array([[3.0, 1.0, 1.0, 0.5, 2.0]])
+    np.testing.assert_array_equal(om.knn_topk(dist, 3), [[3, 1, 2]])
+
+
+def test_oracle_snm_matches_reference_golden():
+    ac, ppr, pdr, quats, slices_ = cases.snm_inputs()
+    from spinifel_gb300 import geom
+
+    g = np.load(os.path.join(GOLD, "golden_snm.npz"))
+    mult = np.pi / pdr.max()
+    B = cases.SNM["batch"]
+    batches = []
+    for st in range(0, cases.SNM["n_orient"], B):
+        H, K, L = geom.hkl(quats[st:st + B], ppr)
+        s = onufft.nufft3d2(H.reshape(-1) * mult, K.reshape(-1) * mult, L.reshape(-1) * mult,
+                            ac, -1, 1e-12).real
+        batches.append(s.reshape(B, -1))
+    idx, dist = om.snm_argmin(batches, slices_.reshape(len(slices_), -1))
+    assert np.all(om.ties_equal(idx, g["index"], dist))
+    np.testing.assert_allclose(dist, g["dist"], rtol=1e-9, atol=1e-9 * np.abs(dist).max())
+
+
+def test_oracle_merge_matches_reference_golden():
+    data, ppr, pdr, orient, ac_est = cases.merge_inputs()
+    from spinifel_gb300 import geom
+
+    g = np.load(os.path.join(GOLD, "golden_merge.npz"))
+    M = cases.MERGE["M"]
+    mo = omerge.MergeOracle(M, 2 * M, data.size, 1, cases.MERGE["maxiter"])
+    H, K, L = geom.hkl(orient, ppr)
+    mult = np.pi / pdr.max()
+    S = omerge.support_from_estimate(ac_est)
+    x0 = (ac_est * S).reshape(-1)
+    x, info, _, _ = mo.solve(data, H.reshape(-1) * mult, K.reshape(-1) * mult,
+                             L.reshape(-1) * mult, S, x0)
+    assert mo.iterations == int(g["iterations"])
+    assert np.linalg.norm(x - g["ac"]) / np.linalg.norm(g["ac"]) < 1e-8
+
+
+def test_oracle_ops_glue_matches_reference_golden():
+    ugrid, sup, H_, K_, L_, nuv = cases.ops_inputs()
+    g = np.load(os.path.join(GOLD, "golden_ops.npz"))
+    fwd = onufft.forward(ugrid, H_, K_, L_, sup, True, H_.size)
+    adj = onufft.adjoint(nuv, H_, K_, L_, cases.OPS["M"], True, sup)
+    np.testing.assert_allclose(fwd, g["forward"], rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(adj, g["adjoint"], rtol=1e-10, atol=1e-12)
