@@ -144,6 +144,45 @@ int spf_dist_argmin_f32(const float *d_img, const float *d_img_sq, int64_t n_img
 int spf_best_unpack(const uint64_t *d_best, int64_t n_img, int32_t *d_idx,
                     float *d_dist, void *stream);
 
+/* ---- BF16 tensor-core matching with exact FP32 re-rank ----------------
+ * The precision form of SNM.euclidean_dist + argmin
+ * (spinifel/sequential/orientation_matching.py:98-109,179): x.s on tcgen05
+ * tensor cores from bf16 copies (FP32 accumulation), the 8 smallest
+ * s2 - 2 x.s per image and 256-reference tile written to the candidate
+ * buffers d_cand_d / d_cand_i, each tiles * n_img * 8 entries with
+ * tiles = spf_dist_topk_bf16_tiles(n_ref) (scratch owned by the caller).
+ * Rows are ld bf16 elements apart (ld >= n_pix, ld % 8 == 0, pad with 0).
+ * Needs sm_103 (GB300). */
+int64_t spf_dist_topk_bf16_tiles(int64_t n_ref);
+int spf_dist_topk_bf16(const void *d_img_bf16, int64_t n_img, const void *d_ref_bf16,
+                       int64_t n_ref, int64_t n_pix, int64_t ld, const float *d_ref_sq,
+                       float *d_cand_d, int32_t *d_cand_i, void *stream);
+
+/* Merge the candidates of all tiles into the per-image top-8, recompute those
+ * 8 distances exactly in FP32 (x2 + s2 - 2 x.s from the FP32 frames and
+ * slices), return the best (d_idx, d_dist; ties to the lower index; index
+ * + ref_offset) and, in d_uncertified (may be NULL), 1 where the bf16 error
+ * bound cannot exclude a reference outside the 8 (the caller then runs the
+ * exact path for that image).  d_img_n4 / ref_n4_max are sqrt(sum x^4) per
+ * frame and its maximum over references (spf_row_norms_f32).  d_top8 (may
+ * be NULL) receives the 8 candidates. */
+int spf_rerank_fp32(const float *d_cand_d, const int32_t *d_cand_i, int64_t n_tiles,
+                    const float *d_img, const float *d_img_sq, const float *d_img_n4,
+                    int64_t n_img, const float *d_ref, const float *d_ref_sq,
+                    float ref_n4_max, int64_t n_ref, int64_t n_pix, int64_t ref_offset,
+                    int32_t *d_idx, float *d_dist, int32_t *d_uncertified,
+                    int32_t *d_top8, void *stream);
+
+/* Row norms: d_sq[r] = sum x^2 and d_n4[r] = sqrt(sum x^4) (either may be
+ * NULL), FP64 accumulation. */
+int spf_row_norms_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_sq,
+                      float *d_n4, void *stream);
+
+/* FP32 -> bf16 with a padded row stride: dst[r*ld + p] = bf16(src[r*n_pix+p])
+ * for p < n_pix, 0 for n_pix <= p < ld. */
+int spf_f32_to_bf16(const float *d_src, int64_t n_rows, int64_t n_pix, void *d_dst,
+                    int64_t ld, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

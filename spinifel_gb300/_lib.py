@@ -70,6 +70,14 @@ SIGNATURES = {
     "spf_dist_argmin_f32": [_c_void_p, _c_void_p, _i64, _c_void_p, _c_void_p, _i64, _i64, _i64,
                             _c_void_p, _c_void_p],
     "spf_best_unpack": [_c_void_p, _i64, _c_void_p, _c_void_p, _c_void_p],
+    "spf_dist_topk_bf16_tiles": [_i64],
+    "spf_dist_topk_bf16": [_c_void_p, _i64, _c_void_p, _i64, _i64, _i64, _c_void_p, _c_void_p,
+                           _c_void_p, _c_void_p],
+    "spf_rerank_fp32": [_c_void_p, _c_void_p, _i64, _c_void_p, _c_void_p, _c_void_p, _i64,
+                        _c_void_p, _c_void_p, ctypes.c_float, _i64, _i64, _i64, _c_void_p,
+                        _c_void_p, _c_void_p, _c_void_p, _c_void_p],
+    "spf_row_norms_f32": [_c_void_p, _i64, _i64, _c_void_p, _c_void_p, _c_void_p],
+    "spf_f32_to_bf16": [_c_void_p, _i64, _i64, _c_void_p, _i64, _c_void_p],
 }
 
 _RESTYPES = {
@@ -77,6 +85,7 @@ _RESTYPES = {
     "spf_status_string": ctypes.c_char_p,
     "spf_last_error": ctypes.c_char_p,
     "spf_launch_count": ctypes.c_uint64,
+    "spf_dist_topk_bf16_tiles": ctypes.c_int64,
 }
 
 _lock = threading.Lock()

@@ -1,0 +1,690 @@
+// BF16 tensor-core orientation matching (tcgen05 + TMEM + TMA) with a fused
+// per-image top-8, and the exact FP32 re-rank that restores the plain path's
+// argmin.
+//
+// Distance: dist(i, r) = ||x_i||^2 + ||s_r||^2 - 2 x_i . s_r.  The x.s term is
+// a GEMM X[n_img, K] . S[n_ref, K]^T, both operands K-major bf16.  One CTA
+// (persistent, one per SM) computes 128 x 256 tiles (images x references):
+//   warp 0   : TMA producer, 4-stage ring of (A 16 KB + B 32 KB) k-blocks of
+//              64 pixels, 128-byte swizzle;
+//   warp 1   : allocates 512 TMEM columns (two 128 x 256 FP32 accumulators)
+//              and issues tcgen05.mma kind::f16 (M128 N256 K16) from one lane;
+//   warps 2-5: epilogue -- each thread owns one image row (TMEM lane), reads
+//              its 256 accumulators with tcgen05.ld, forms s2 - 2 acc and keeps
+//              the 8 smallest (ties to the lower index), then writes them to
+//              the candidate buffer cand[n_tile][image][8].
+// Accumulators are double-buffered so the epilogue of tile t overlaps the
+// main loop of tile t+1.  Every mbarrier wait is bounded (1 s); on timeout
+// the kernel records SPF_ERR_TIMEOUT in the device error word, stops issuing,
+// drains its copies and frees TMEM before returning.
+//
+// The re-rank kernel merges the candidates of all reference tiles into the
+// per-image top-8, recomputes those 8 distances exactly in FP32 from the FP32
+// frames and slices, and certifies the result: the argmin over all
+// references is the re-ranked one when the 8th-best approximate distance
+// exceeds the re-ranked best by more than twice the bf16 error bound
+// (6 sigma of the rounding error, sigma <= 2^-9 sqrt(2/3) ||x||_4^2 max||s||_4^2).
+// Uncertified images are flagged for an exact pass over all references.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "common.cuh"
+
+namespace spf {
+namespace bf16mm {
+
+constexpr int BM = 128;
+constexpr int BN = 256;
+constexpr int BK = 64;  // bf16 elements = 128 bytes = one swizzle atom row
+constexpr int STAGES = 4;
+constexpr int A_BYTES = BM * BK * 2;
+constexpr int B_BYTES = BN * BK * 2;
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int THREADS = 192;
+constexpr int TOPK = 8;
+constexpr int GROUP_M = 16;
+constexpr uint32_t TMEM_COLS = 512;
+constexpr uint64_t TIMEOUT_NS = 1000000000ull;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+
+// Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
+// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait.  Returns false (and raises the CTA abort flag) on timeout or
+// when another role of the CTA has already aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort) {
+  if (mbar_try_wait(bar, parity)) return true;
+  uint64_t t0 = globaltimer();
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255) == 0) {
+      if (*abort) return false;
+      if (globaltimer() - t0 > TIMEOUT_NS) {
+        *abort = 1;
+        return false;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                            int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                    // leading byte offset (unused, swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                    // descriptor version
+  d |= (uint64_t)2 << 61;                    // 128-byte swizzle
+  return d;
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+struct TopK {
+  float d[TOPK];
+  int32_t i[TOPK];
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int k = 0; k < TOPK; ++k) {
+      d[k] = __int_as_float(0x7f800000);  // +inf
+      i[k] = INT32_MAX;
+    }
+  }
+  // insert with ties resolved towards the lower index (callers feed indices
+  // in increasing order, so a strict < on the value keeps the earlier one)
+  __device__ __forceinline__ void push(float v, int32_t j) {
+    if (!(v < d[TOPK - 1])) return;
+    d[TOPK - 1] = v;
+    i[TOPK - 1] = j;
+#pragma unroll
+    for (int k = TOPK - 1; k > 0; --k) {
+      bool sw = d[k] < d[k - 1];
+      float td = sw ? d[k - 1] : d[k];
+      int32_t ti = sw ? i[k - 1] : i[k];
+      d[k - 1] = sw ? d[k] : d[k - 1];
+      i[k - 1] = sw ? i[k] : i[k - 1];
+      d[k] = td;
+      i[k] = ti;
+    }
+  }
+};
+
+__device__ __forceinline__ void tile_of(int64_t t, int64_t n_m, int64_t n_n, int64_t &m,
+                                        int64_t &n) {
+  int64_t per_group = (int64_t)GROUP_M * n_n;
+  int64_t g = t / per_group;
+  int64_t first_m = g * GROUP_M;
+  int64_t gm = n_m - first_m < GROUP_M ? n_m - first_m : GROUP_M;
+  int64_t r = t % per_group;
+  m = first_m + r % gm;
+  n = r / gm;
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_dist_topk_bf16(const __grid_constant__ CUtensorMap tmap_a,
+                     const __grid_constant__ CUtensorMap tmap_b, const float *__restrict__ ref_sq,
+                     int64_t n_img, int64_t n_ref, int64_t n_pix, float *__restrict__ cand_d,
+                     int32_t *__restrict__ cand_i, unsigned int *__restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  uint8_t *sA = smem;
+  uint8_t *sB = smem + STAGES * A_BYTES;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES);
+  uint64_t *full = bars;
+  uint64_t *empty = bars + STAGES;
+  uint64_t *acc_full = bars + 2 * STAGES;
+  uint64_t *acc_empty = bars + 2 * STAGES + 2;
+  uint64_t *done = bars + 2 * STAGES + 4;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 5);
+  volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int64_t n_m = (n_img + BM - 1) / BM;
+  const int64_t n_n = (n_ref + BN - 1) / BN;
+  const int64_t n_tiles = n_m * n_n;
+  const int nkb = (int)((n_pix + BK - 1) / BK);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 128);
+    }
+    mbar_init(done, 1);
+    *abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer ----------------
+      uint32_t it = 0;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+        int64_t m, n;
+        tile_of(t, n_m, n_n, m, n);
+        for (int kb = 0; kb < nkb; ++kb, ++it) {
+          int s = it % STAGES;
+          uint32_t ph = (it / STAGES) & 1;
+          if (!mbar_wait(&empty[s], ph ^ 1, abort)) {
+            ok = false;
+            break;
+          }
+          mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+          tma_load_2d(sA + s * A_BYTES, &tmap_a, &full[s], kb * BK, (int)(m * BM));
+          tma_load_2d(sB + s * B_BYTES, &tmap_b, &full[s], kb * BK, (int)(n * BN));
+        }
+      }
+      // drain: every issued copy must have landed before the CTA exits
+      uint32_t first = it > (uint32_t)STAGES ? it - STAGES : 0;
+      for (uint32_t j = first; j < it; ++j) {
+        int s = j % STAGES;
+        uint32_t ph = (j / STAGES) & 1;
+        uint64_t t0 = globaltimer();
+        while (!mbar_try_wait(&full[s], ph) && globaltimer() - t0 < TIMEOUT_NS) {
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      uint32_t it = 0, tc = 0;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, ++tc) {
+        uint32_t b = tc & 1, use = tc >> 1;
+        if (!mbar_wait(&acc_empty[b], (use & 1) ^ 1, abort)) break;
+        tc_fence_after();
+        uint32_t d_tmem = tmem_base + b * BN;
+        for (int kb = 0; kb < nkb; ++kb, ++it) {
+          int s = it % STAGES;
+          uint32_t ph = (it / STAGES) & 1;
+          if (!mbar_wait(&full[s], ph, abort)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          uint32_t a0 = smem_u32(sA + s * A_BYTES);
+          uint32_t b0 = smem_u32(sB + s * B_BYTES);
+#pragma unroll
+          for (int k = 0; k < BK / 16; ++k) {
+            umma_bf16(d_tmem, sdesc_sw128(a0 + k * 32), sdesc_sw128(b0 + k * 32),
+                      (kb | k) != 0 ? 1u : 0u);
+          }
+          umma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        umma_commit(&acc_full[b]);
+      }
+      // all issued MMAs complete before TMEM is released
+      umma_commit(done);
+      uint64_t t0 = globaltimer();
+      while (!mbar_try_wait(done, 0) && globaltimer() - t0 < TIMEOUT_NS) {
+      }
+    }
+  } else {
+    // ---------------- epilogue (warps 2..5) ----------------
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    uint32_t tc = 0;
+    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x, ++tc) {
+      int64_t m, n;
+      tile_of(t, n_m, n_n, m, n);
+      uint32_t b = tc & 1, use = tc >> 1;
+      // one lane waits, the warp follows (tcgen05.ld below is warp-collective)
+      int ok = 1;
+      if (lane == 0) ok = mbar_wait(&acc_full[b], use & 1, abort) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      tc_fence_after();
+      const int64_t row = m * BM + q * 32 + lane;
+      const int64_t col0 = n * BN;
+      TopK top;
+      top.clear();
+#pragma unroll 1
+      for (int c = 0; c < BN / 32; ++c) {
+        uint32_t r[32];
+        tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + b * BN + c * 32, r);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          int64_t col = col0 + c * 32 + j;
+          if (col < n_ref) {
+            float v = __ldg(ref_sq + col) - 2.0f * __uint_as_float(r[j]);
+            top.push(v, (int32_t)col);
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acc_empty[b]);
+      if (row < n_img) {
+        size_t base = ((size_t)n * n_img + row) * TOPK;
+        float4 *pd = reinterpret_cast<float4 *>(cand_d + base);
+        int4 *pi = reinterpret_cast<int4 *>(cand_i + base);
+        pd[0] = make_float4(top.d[0], top.d[1], top.d[2], top.d[3]);
+        pd[1] = make_float4(top.d[4], top.d[5], top.d[6], top.d[7]);
+        pi[0] = make_int4(top.i[0], top.i[1], top.i[2], top.i[3]);
+        pi[1] = make_int4(top.i[4], top.i[5], top.i[6], top.i[7]);
+      }
+    }
+  }
+
+  __syncthreads();
+  if (threadIdx.x == 0 && *abort) atomicExch(err, (unsigned int)(-SPF_ERR_TIMEOUT));
+  tc_fence_after();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                 "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+// merge + exact FP32 re-rank, one CTA (256 threads) per image
+// ---------------------------------------------------------------------------
+constexpr int RR_THREADS = 256;
+
+__device__ __forceinline__ bool lex_less(float a, int32_t ia, float b, int32_t ib) {
+  return a < b || (a == b && ia < ib);
+}
+
+__global__ void __launch_bounds__(RR_THREADS)
+    k_rerank(const float *__restrict__ cand_d, const int32_t *__restrict__ cand_i, int64_t n_tiles,
+             const float *__restrict__ img, const float *__restrict__ img_sq,
+             const float *__restrict__ img_n4, int64_t n_img, const float *__restrict__ ref,
+             const float *__restrict__ ref_sq, float ref_n4_max, int64_t n_pix,
+             int64_t ref_offset, int32_t *__restrict__ out_idx, float *__restrict__ out_dist,
+             int32_t *__restrict__ uncertified, int32_t *__restrict__ out_top) {
+  __shared__ float s_d[RR_THREADS / 32][TOPK];
+  __shared__ int32_t s_i[RR_THREADS / 32][TOPK];
+  __shared__ float s_top_d[TOPK];
+  __shared__ int32_t s_top_i[TOPK];
+  __shared__ float s_dot[RR_THREADS / 32][TOPK];
+  const int64_t im = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (im >= n_img) return;
+
+  // 1. the 8 smallest candidates over all reference tiles, by (d, index)
+  float d[TOPK];
+  int32_t ix[TOPK];
+#pragma unroll
+  for (int k = 0; k < TOPK; ++k) {
+    d[k] = __int_as_float(0x7f800000);
+    ix[k] = INT32_MAX;
+  }
+  const int64_t total = n_tiles * TOPK;
+  for (int64_t c = tid; c < total; c += RR_THREADS) {
+    int64_t tile = c / TOPK, k = c % TOPK;
+    size_t off = ((size_t)tile * n_img + im) * TOPK + k;
+    float v = cand_d[off];
+    int32_t j = cand_i[off];
+    if (!lex_less(v, j, d[TOPK - 1], ix[TOPK - 1])) continue;
+    d[TOPK - 1] = v;
+    ix[TOPK - 1] = j;
+#pragma unroll
+    for (int q = TOPK - 1; q > 0; --q) {
+      bool sw = lex_less(d[q], ix[q], d[q - 1], ix[q - 1]);
+      float td = sw ? d[q - 1] : d[q];
+      int32_t ti = sw ? ix[q - 1] : ix[q];
+      d[q - 1] = sw ? d[q] : d[q - 1];
+      ix[q - 1] = sw ? ix[q] : ix[q - 1];
+      d[q] = td;
+      ix[q] = ti;
+    }
+  }
+  // warp merge: 8 rounds of a lexicographic warp minimum over list heads
+  int head = 0;
+  for (int r = 0; r < TOPK; ++r) {
+    float hv = head < TOPK ? d[head] : __int_as_float(0x7f800000);
+    int32_t hi = head < TOPK ? ix[head] : INT32_MAX;
+    float bv = hv;
+    int32_t bi = hi;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+      float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      int32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (lex_less(ov, oi, bv, bi)) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if (head < TOPK && hv == bv && hi == bi) ++head;
+    if (lane == 0) {
+      s_d[warp][r] = bv;
+      s_i[warp][r] = bi;
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    // lanes hold 2 of the 64 warp-level entries each
+    float a0 = s_d[lane >> 3][lane & 7], a1 = s_d[4 + (lane >> 3)][lane & 7];
+    int32_t j0 = s_i[lane >> 3][lane & 7], j1 = s_i[4 + (lane >> 3)][lane & 7];
+    if (lex_less(a1, j1, a0, j0)) {
+      float tv = a0; a0 = a1; a1 = tv;
+      int32_t tj = j0; j0 = j1; j1 = tj;
+    }
+    int h = 0;
+    for (int r = 0; r < TOPK; ++r) {
+      float hv = h == 0 ? a0 : (h == 1 ? a1 : __int_as_float(0x7f800000));
+      int32_t hi = h == 0 ? j0 : (h == 1 ? j1 : INT32_MAX);
+      float bv = hv;
+      int32_t bi = hi;
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        int32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (lex_less(ov, oi, bv, bi)) {
+          bv = ov;
+          bi = oi;
+        }
+      }
+      if (h < 2 && hv == bv && hi == bi) ++h;
+      if (lane == 0) {
+        s_top_d[r] = bv;
+        s_top_i[r] = bi;
+      }
+    }
+  }
+  __syncthreads();
+
+  // 2. exact FP32 distances of the 8 candidates
+  int32_t cj[TOPK];
+  bool cv[TOPK];
+#pragma unroll
+  for (int k = 0; k < TOPK; ++k) {
+    cj[k] = s_top_i[k];
+    cv[k] = cj[k] != INT32_MAX;
+  }
+  float acc[TOPK];
+#pragma unroll
+  for (int k = 0; k < TOPK; ++k) acc[k] = 0.0f;
+  const float *x = img + im * n_pix;
+  for (int64_t p = tid; p < n_pix; p += RR_THREADS) {
+    float xv = x[p];
+#pragma unroll
+    for (int k = 0; k < TOPK; ++k)
+      if (cv[k]) acc[k] = fmaf(xv, __ldg(ref + (int64_t)cj[k] * n_pix + p), acc[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < TOPK; ++k) {
+    float v = acc[k];
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s_dot[warp][k] = v;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    float x2 = img_sq[im];
+    float best = __int_as_float(0x7f800000);
+    int32_t bj = INT32_MAX;
+    for (int k = 0; k < TOPK; ++k) {
+      if (!cv[k]) continue;
+      float dot = 0.0f;
+      for (int w = 0; w < RR_THREADS / 32; ++w) dot += s_dot[w][k];
+      float dist = (x2 + ref_sq[cj[k]]) - 2.0f * dot;
+      if (lex_less(dist, cj[k], best, bj)) {
+        best = dist;
+        bj = cj[k];
+      }
+    }
+    out_idx[im] = bj == INT32_MAX ? -1 : (int32_t)(bj + ref_offset);
+    if (out_dist) out_dist[im] = best;
+    if (out_top)
+      for (int k = 0; k < TOPK; ++k)
+        out_top[im * TOPK + k] = cv[k] ? (int32_t)(cj[k] + ref_offset) : -1;
+    // certificate: no reference outside the 8 can beat the re-ranked best
+    int ncand = 0;
+    for (int k = 0; k < TOPK; ++k) ncand += cv[k];
+    int cert = 1;
+    if (ncand == TOPK) {
+      const float u = 1.0f / 512.0f;  // bf16 unit roundoff
+      float sigma = u * 0.8164966f * img_n4[im] * ref_n4_max;
+      float margin = (x2 + s_top_d[TOPK - 1]) - 12.0f * sigma - best;
+      cert = margin > 1e-6f * fabsf(best) ? 1 : 0;
+    }
+    if (uncertified) uncertified[im] = cert ? 0 : 1;
+  }
+}
+
+// sum of squares and sqrt(sum of fourth powers) per row, FP64 accumulation
+__global__ void k_row_norms(const float *__restrict__ x, int64_t n_rows, int64_t n_pix,
+                            float *__restrict__ sq, float *__restrict__ n4) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n_rows; r += nwarps) {
+    const float *p = x + r * n_pix;
+    double s2 = 0.0, s4 = 0.0;
+    for (int64_t k = lane; k < n_pix; k += 32) {
+      double v = p[k];
+      double v2 = v * v;
+      s2 += v2;
+      s4 = fma(v2, v2, s4);
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+      s4 += __shfl_xor_sync(0xffffffffu, s4, o);
+    }
+    if (lane == 0) {
+      if (sq) sq[r] = (float)s2;
+      if (n4) n4[r] = (float)sqrt(s4);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+static int make_map(CUtensorMap *map, const void *base, int64_t rows, int64_t ld, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) {
+    set_error("cuTensorMapEncodeTiled is not available from the driver");
+    return SPF_ERR_UNSUPPORTED;
+  }
+  cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims,
+                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return SPF_ERR_ARG;
+  }
+  return SPF_OK;
+}
+
+}  // namespace bf16mm
+}  // namespace spf
+
+using namespace spf;
+using namespace spf::bf16mm;
+
+extern "C" {
+
+int64_t spf_dist_topk_bf16_tiles(int64_t n_ref) { return (n_ref + BN - 1) / BN; }
+
+int spf_dist_topk_bf16(const void *d_img_bf16, int64_t n_img, const void *d_ref_bf16,
+                       int64_t n_ref, int64_t n_pix, int64_t ld, const float *d_ref_sq,
+                       float *d_cand_d, int32_t *d_cand_i, void *stream) {
+  SPF_REQUIRE(n_img >= 0 && n_ref >= 0 && n_pix >= 0, "spf_dist_topk_bf16: negative size");
+  if (n_img == 0 || n_ref == 0) return SPF_OK;
+  SPF_REQUIRE(d_img_bf16 && d_ref_bf16 && d_ref_sq && d_cand_d && d_cand_i,
+              "spf_dist_topk_bf16: NULL pointer");
+  SPF_REQUIRE(ld >= n_pix && ld % 8 == 0,
+              "spf_dist_topk_bf16: row stride ld must be >= n_pix and a multiple of 8");
+  SPF_REQUIRE(aligned(d_img_bf16, 16) && aligned(d_ref_bf16, 16),
+              "spf_dist_topk_bf16: operands must be 16-byte aligned");
+  SPF_REQUIRE(aligned(d_cand_d, 16) && aligned(d_cand_i, 16),
+              "spf_dist_topk_bf16: candidate buffers must be 16-byte aligned");
+  SPF_REQUIRE(n_img < (1LL << 31) && n_ref < (1LL << 31) && ld < (1LL << 31),
+              "spf_dist_topk_bf16: size too large");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int major = 0, minor = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  if (major != 10 || minor != 3) {
+    set_error("spf_dist_topk_bf16: needs sm_103 (GB300), device is sm_%d%d", major, minor);
+    return SPF_ERR_UNSUPPORTED;
+  }
+  CUtensorMap ma, mb;
+  SPF_TRY(make_map(&ma, d_img_bf16, n_img, ld, BM));
+  SPF_TRY(make_map(&mb, d_ref_bf16, n_ref, ld, BN));
+  static bool attr_set[64] = {false};
+  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    SPF_TRY(check_cuda(cudaFuncSetAttribute(k_dist_topk_bf16,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            SMEM_BYTES),
+                       "spf_dist_topk_bf16"));
+    attr_set[dev] = true;
+  }
+  unsigned int *err = device_error_word();
+  SPF_REQUIRE(err != nullptr, "spf_dist_topk_bf16: no device error word");
+  int64_t tiles = ((n_img + BM - 1) / BM) * ((n_ref + BN - 1) / BN);
+  int grid = (int)(tiles < sm_count() ? tiles : sm_count());
+  k_dist_topk_bf16<<<grid, THREADS, SMEM_BYTES, as_stream(stream)>>>(
+      ma, mb, d_ref_sq, n_img, n_ref, n_pix, d_cand_d, d_cand_i, err);
+  return check_launch("k_dist_topk_bf16");
+}
+
+int spf_rerank_fp32(const float *d_cand_d, const int32_t *d_cand_i, int64_t n_tiles,
+                    const float *d_img, const float *d_img_sq, const float *d_img_n4,
+                    int64_t n_img, const float *d_ref, const float *d_ref_sq, float ref_n4_max,
+                    int64_t n_ref, int64_t n_pix, int64_t ref_offset, int32_t *d_idx,
+                    float *d_dist, int32_t *d_uncertified, int32_t *d_top8, void *stream) {
+  SPF_REQUIRE(n_img >= 0 && n_ref >= 0 && n_pix >= 0 && n_tiles >= 0,
+              "spf_rerank_fp32: negative size");
+  if (n_img == 0) return SPF_OK;
+  SPF_REQUIRE(d_cand_d && d_cand_i && d_img && d_img_sq && d_img_n4 && d_ref && d_ref_sq && d_idx,
+              "spf_rerank_fp32: NULL pointer");
+  SPF_REQUIRE(n_tiles == (n_ref + BN - 1) / BN, "spf_rerank_fp32: n_tiles does not match n_ref");
+  SPF_REQUIRE(n_img < (1LL << 31), "spf_rerank_fp32: too many images");
+  k_rerank<<<(unsigned)n_img, RR_THREADS, 0, as_stream(stream)>>>(
+      d_cand_d, d_cand_i, n_tiles, d_img, d_img_sq, d_img_n4, n_img, d_ref, d_ref_sq, ref_n4_max,
+      n_pix, ref_offset, d_idx, d_dist, d_uncertified, d_top8);
+  return check_launch("k_rerank");
+}
+
+int spf_row_norms_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_sq, float *d_n4,
+                      void *stream) {
+  SPF_REQUIRE(n_rows >= 0 && n_pix >= 0, "spf_row_norms_f32: negative size");
+  if (n_rows == 0) return SPF_OK;
+  SPF_REQUIRE(d_x != nullptr, "spf_row_norms_f32: NULL pointer");
+  int blocks = grid_for(n_rows * 32, 256, (int64_t)sm_count() * 32);
+  k_row_norms<<<blocks, 256, 0, as_stream(stream)>>>(d_x, n_rows, n_pix, d_sq, d_n4);
+  return check_launch("spf_row_norms_f32");
+}
+
+}  // extern "C"

@@ -273,6 +273,16 @@ __global__ void k_ingest_u16(const uint16_t *__restrict__ in, int64_t n_img, int
   }
 }
 
+__global__ void k_f32_to_bf16(const float *__restrict__ src, int64_t n_rows, int64_t n_pix,
+                              __nv_bfloat16 *__restrict__ dst, int64_t ld) {
+  int64_t total = n_rows * ld;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = i / ld, p = i % ld;
+    dst[i] = __float2bfloat16_rn(p < n_pix ? src[r * n_pix + p] : 0.0f);
+  }
+}
+
 // k smallest of each row, ascending, ties to the lower index; warp per row.
 template <typename T>
 __global__ void k_topk(const T *__restrict__ dist, int64_t n_rows, int64_t n_cols, int k,
@@ -412,6 +422,17 @@ int spf_frames_ingest_u16(const uint16_t *d_counts, int64_t n_img, int64_t n_pix
   k_ingest_u16<<<blocks, 256, 0, as_stream(stream)>>>(
       d_counts, n_img, n_pix, d_f32, reinterpret_cast<__nv_bfloat16 *>(d_bf16), d_sq);
   return check_launch("spf_frames_ingest_u16");
+}
+
+int spf_f32_to_bf16(const float *d_src, int64_t n_rows, int64_t n_pix, void *d_dst, int64_t ld,
+                    void *stream) {
+  SPF_REQUIRE(n_rows >= 0 && n_pix >= 0 && ld >= n_pix, "spf_f32_to_bf16: bad sizes");
+  if (n_rows == 0 || ld == 0) return SPF_OK;
+  SPF_REQUIRE(d_src && d_dst, "spf_f32_to_bf16: NULL pointer");
+  k_f32_to_bf16<<<grid_for(n_rows * ld, 256, (int64_t)sm_count() * 64), 256, 0,
+                  as_stream(stream)>>>(d_src, n_rows, n_pix,
+                                       reinterpret_cast<__nv_bfloat16 *>(d_dst), ld);
+  return check_launch("spf_f32_to_bf16");
 }
 
 int spf_best_init(uint64_t *d_best, int64_t n_img, void *stream) {

@@ -93,3 +93,128 @@ def knn_topk(dist: torch.Tensor, k: int) -> torch.Tensor:
     _lib.call(name, _lib.ptr(dist), dist.shape[0], dist.shape[1], int(k), _lib.ptr(out),
               _lib.stream_handle())
     return out
+
+
+# ---------------------------------------------------------------------------
+# BF16 tensor-core path with exact FP32 re-rank
+# ---------------------------------------------------------------------------
+
+def row_norms(x: torch.Tensor):
+    """(sum x^2, sqrt(sum x^4)) per row, FP32 results."""
+    _lib.require_cuda(x, "x", torch.float32)
+    n = x.shape[0]
+    sq = torch.empty(n, device=x.device, dtype=torch.float32)
+    n4 = torch.empty(n, device=x.device, dtype=torch.float32)
+    _lib.call("spf_row_norms_f32", _lib.ptr(x), n, x[0].numel() if n else 0, _lib.ptr(sq),
+              _lib.ptr(n4), _lib.stream_handle())
+    return sq, n4
+
+
+def to_bf16_padded(x: torch.Tensor, ld: int | None = None) -> torch.Tensor:
+    """bf16 copy of [rows, n_pix] FP32 with a row stride that is a multiple of 8."""
+    _lib.require_cuda(x, "x", torch.float32)
+    n, p = x.shape
+    ld = ld or (p + 7) // 8 * 8
+    out = torch.empty(n, ld, device=x.device, dtype=torch.bfloat16)
+    _lib.call("spf_f32_to_bf16", _lib.ptr(x), n, p, _lib.ptr(out), ld, _lib.stream_handle())
+    return out
+
+
+def check_device_error():
+    """Raise if a bounded device wait of this library has timed out."""
+    import ctypes
+
+    code = ctypes.c_int(0)
+    _lib.call("spf_device_error", _lib.stream_handle(), ctypes.byref(code))
+    if code.value:
+        raise _lib.SpfError(-code.value, "device", "a bounded device wait gave up")
+
+
+class ReferenceSet:
+    """Reference slices resident in HBM: FP32 rows (exact re-rank and the plain
+    path), a bf16 copy for the tensor cores (row stride padded to 8), squared
+    norms and the largest sqrt(sum s^4) (for the re-rank certificate)."""
+
+    def __init__(self, refs_f32: torch.Tensor, refs_bf16: torch.Tensor | None = None):
+        _lib.require_cuda(refs_f32, "refs_f32", torch.float32)
+        self.f32 = refs_f32
+        self.n_ref, self.n_pix = refs_f32.shape
+        self.ld = (self.n_pix + 7) // 8 * 8
+        if refs_bf16 is None:
+            refs_bf16 = to_bf16_padded(refs_f32, self.ld)
+        if tuple(refs_bf16.shape) != (self.n_ref, self.ld):
+            raise ValueError("bf16 copy must be [n_ref, ld]")
+        self.bf16 = refs_bf16
+        self.sq, n4 = row_norms(refs_f32)
+        self.n4_max = float(n4.max().item()) if self.n_ref else 0.0
+
+    def rescale(self, factor: float):
+        """Multiply every slice by factor (FP32, bf16 and norms kept consistent)."""
+        self.f32 *= factor
+        self.bf16.copy_(to_bf16_padded(self.f32, self.ld))
+        self.sq, n4 = row_norms(self.f32)
+        self.n4_max = float(n4.max().item()) if self.n_ref else 0.0
+
+
+class FrameSet:
+    """Frames prepared for matching: FP32, bf16 (padded), norms."""
+
+    def __init__(self, f32: torch.Tensor, ld: int | None = None):
+        _lib.require_cuda(f32, "frames", torch.float32)
+        self.f32 = f32
+        self.n, self.n_pix = f32.shape
+        self.ld = ld or (self.n_pix + 7) // 8 * 8
+        self.bf16 = to_bf16_padded(f32, self.ld)
+        self.sq, self.n4 = row_norms(f32)
+
+
+class _Workspace:
+    def __init__(self):
+        self.bufs = {}
+
+    def get(self, name, numel, dtype, device):
+        t = self.bufs.get((name, device))
+        if t is None or t.numel() < numel or t.dtype != dtype:
+            t = torch.empty(max(numel, 1), dtype=dtype, device=device)
+            self.bufs[(name, device)] = t
+        return t[:numel]
+
+
+_ws = _Workspace()
+
+
+def match_bf16(frames: FrameSet, refs: ReferenceSet, exact_fallback: bool = True,
+               stats: dict | None = None, stream=None):
+    """Best reference per frame: bf16 tensor-core distances, per-frame top-8,
+    exact FP32 re-rank; frames the certificate cannot settle are re-matched
+    exactly over all references (plain FP32 path)."""
+    if frames.n_pix != refs.n_pix or frames.ld != refs.ld:
+        raise ValueError("frames and references differ in pixel count")
+    dev = frames.f32.device
+    n_img = frames.n
+    tiles = int(_lib.lib().spf_dist_topk_bf16_tiles(refs.n_ref))
+    cand_d = _ws.get("cand_d", tiles * n_img * 8, torch.float32, dev)
+    cand_i = _ws.get("cand_i", tiles * n_img * 8, torch.int32, dev)
+    idx = torch.empty(n_img, dtype=torch.int32, device=dev)
+    dist = torch.empty(n_img, dtype=torch.float32, device=dev)
+    unc = torch.empty(n_img, dtype=torch.int32, device=dev)
+    sh = _lib.stream_handle(stream)
+    _lib.call("spf_dist_topk_bf16", _lib.ptr(frames.bf16), n_img, _lib.ptr(refs.bf16), refs.n_ref,
+              refs.n_pix, refs.ld, _lib.ptr(refs.sq), _lib.ptr(cand_d), _lib.ptr(cand_i), sh)
+    _lib.call("spf_rerank_fp32", _lib.ptr(cand_d), _lib.ptr(cand_i), tiles, _lib.ptr(frames.f32),
+              _lib.ptr(frames.sq), _lib.ptr(frames.n4), n_img, _lib.ptr(refs.f32),
+              _lib.ptr(refs.sq), float(refs.n4_max), refs.n_ref, refs.n_pix, 0, _lib.ptr(idx),
+              _lib.ptr(dist), _lib.ptr(unc), None, sh)
+    if exact_fallback or stats is not None:
+        bad = torch.nonzero(unc, as_tuple=False).flatten()
+        nbad = int(bad.numel())
+        if stats is not None:
+            stats["uncertified"] = nbad
+        if exact_fallback and nbad:
+            sub = frames.f32.index_select(0, bad).contiguous()
+            tr = BestTracker(nbad, dev)
+            tr.update_fp32(sub, frames.sq.index_select(0, bad).contiguous(), refs.f32, refs.sq, 0)
+            i2, d2 = tr.result()
+            idx.index_copy_(0, bad, i2)
+            dist.index_copy_(0, bad, d2)
+    return idx, dist

@@ -25,8 +25,10 @@ def generate_weights(pixel_position_reciprocal, order=0):
 
 
 def nearest_neighbor(model_slices, slices, batch_size):
-    dt = torch.float64 if np.asarray(slices).dtype == np.float64 and not _arrays.is_torch(slices) \
-        else torch.float32
+    if _arrays.is_torch(slices):
+        dt = torch.float64 if slices.dtype == torch.float64 else torch.float32
+    else:
+        dt = torch.float64 if np.asarray(slices).dtype == np.float64 else torch.float32
     ref = _arrays.to_dev(model_slices, dt)
     dat = _arrays.to_dev(slices, dt)
     n_ref, n_img = ref.shape[0], dat.shape[0]

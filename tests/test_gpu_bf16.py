@@ -1,0 +1,105 @@
+"""BF16 tensor-core distances (tcgen05) with fused top-8 and the exact FP32
+re-rank.  The candidate distances are checked against a torch FP64 product of
+the same bf16-rounded operands (relative tolerance 1e-5 of the distance
+scale), and the final argmin against the plain FP32 path and the FP64 oracle
+(identical, or a tie within 1e-6 relative)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import matching as om
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dev(lib):
+    return torch.device("cuda", 0)
+
+
+def _raw_candidates(frames, refs):
+    from spinifel_gb300 import _lib
+
+    tiles = int(_lib.lib().spf_dist_topk_bf16_tiles(refs.n_ref))
+    cd = torch.empty(tiles * frames.n * 8, dtype=torch.float32, device=frames.f32.device)
+    ci = torch.empty(tiles * frames.n * 8, dtype=torch.int32, device=frames.f32.device)
+    _lib.call("spf_dist_topk_bf16", _lib.ptr(frames.bf16), frames.n, _lib.ptr(refs.bf16),
+              refs.n_ref, refs.n_pix, refs.ld, _lib.ptr(refs.sq), _lib.ptr(cd), _lib.ptr(ci),
+              _lib.stream_handle())
+    torch.cuda.synchronize()
+    return cd.view(tiles, frames.n, 8), ci.view(tiles, frames.n, 8)
+
+
+@pytest.mark.parametrize("shape", [(128, 256, 64), (130, 600, 256), (300, 1000, 1000),
+                                   (7, 3, 8)])
+def test_tcgen05_tile_topk_matches_torch(dev, shape):
+    from spinifel_gb300 import matching
+
+    n_img, n_ref, n_pix = shape
+    g = torch.Generator(device="cpu").manual_seed(40)
+    x = torch.rand(n_img, n_pix, generator=g).to(dev)
+    s = torch.rand(n_ref, n_pix, generator=g).to(dev)
+    fr = matching.FrameSet(x)
+    rs = matching.ReferenceSet(s)
+    cd, ci = _raw_candidates(fr, rs)
+    matching.check_device_error()
+    xb = fr.bf16[:, :n_pix].double()
+    sb = rs.bf16[:, :n_pix].double()
+    approx = rs.sq.double()[None, :] - 2.0 * xb @ sb.T  # [n_img, n_ref]
+    scale = float(approx.abs().max())
+    tiles = cd.shape[0]
+    for t in range(tiles):
+        lo, hi = t * 256, min((t + 1) * 256, n_ref)
+        k = min(8, hi - lo)
+        ref_vals, ref_idx = torch.sort(approx[:, lo:hi], dim=1, stable=True)
+        got_d = cd[t, :, :k].double()
+        got_i = ci[t, :, :k].long()
+        # values agree (FP32 accumulation vs FP64)
+        assert float((got_d - ref_vals[:, :k]).abs().max()) <= 1e-5 * scale
+        # the value the kernel reports for each index is that index's distance
+        recomputed = torch.gather(approx, 1, got_i)
+        assert float((recomputed - got_d).abs().max()) <= 1e-5 * scale
+        if k < 8:
+            assert bool((ci[t, :, k:] == 2**31 - 1).all())
+
+
+@pytest.mark.parametrize("shape", [(500, 3000, 1024), (129, 1000, 4096), (64, 257, 40)])
+def test_bf16_rerank_argmin_equals_plain_fp32(dev, shape):
+    from spinifel_gb300 import matching
+
+    n_img, n_ref, n_pix = shape
+    rng = np.random.default_rng(41)
+    refs = rng.random((n_ref, n_pix)).astype(np.float32)
+    # frames near some references, plus noise: realistic gaps
+    pick = rng.integers(0, n_ref, n_img)
+    imgs = (refs[pick] + 0.3 * rng.random((n_img, n_pix))).astype(np.float32)
+    x = torch.as_tensor(imgs, device=dev)
+    s = torch.as_tensor(refs, device=dev)
+    fr, rs = matching.FrameSet(x), matching.ReferenceSet(s)
+    st = {}
+    idx, dist = matching.match_bf16(fr, rs, stats=st)
+    matching.check_device_error()
+    pidx, pdist = matching.argmin_fp32(x, s)
+    oidx, od = om.sklearn_argmin(refs, imgs)
+    assert np.all(om.ties_equal(idx.cpu().numpy(), oidx, od))
+    assert np.all(om.ties_equal(idx.cpu().numpy(), pidx.cpu().numpy(), od))
+    assert st["uncertified"] <= n_img
+
+
+def test_bf16_poisson_frames_certify(dev):
+    """Integer photon counts are exact in bf16; most frames should certify."""
+    from spinifel_gb300 import matching
+
+    rng = np.random.default_rng(42)
+    n_ref, n_img, n_pix = 2000, 256, 4096
+    refs = rng.gamma(0.5, 1.0, (n_ref, n_pix)).astype(np.float32)
+    pick = rng.integers(0, n_ref, n_img)
+    imgs = rng.poisson(refs[pick]).astype(np.float32)
+    x = torch.as_tensor(imgs, device=dev)
+    s = torch.as_tensor(refs, device=dev)
+    fr, rs = matching.FrameSet(x), matching.ReferenceSet(s)
+    st = {}
+    idx, _ = matching.match_bf16(fr, rs, stats=st)
+    oidx, od = om.sklearn_argmin(refs, imgs)
+    assert np.all(om.ties_equal(idx.cpu().numpy(), oidx, od))
+    assert st["uncertified"] < n_img // 2
