@@ -97,6 +97,16 @@ int spf_nufft_t1_spread_orient(spf_nufft_plan plan, const float *d_quats,
                                double scale, const float *d_c, void *stream);
 int spf_nufft_t1_finish(spf_nufft_plan plan, int isign, float *d_out_re,
                         float *d_out_im, void *stream);
+/* Fused type 2 -> type 1 at orientation points (the direct A^H D A product):
+ * every point interpolates Re of the type-2 fine grid set by
+ * spf_nufft_t2_set_modes, multiplies by d_weights[o*n_pix+p] (NULL = 1) and
+ * spreads the product into the type-1 accumulator (zero it first with
+ * spf_nufft_t1_zero, finish with spf_nufft_t1_finish).  Replaces the
+ * forward / adjoint pair the reference's core_problem composes
+ * (spinifel/autocorrelation.py:161-172). */
+int spf_nufft_interp_spread_orient(spf_nufft_plan plan, const float *d_quats,
+                                   int64_t n_orient, const float *d_ppr, int64_t n_pix,
+                                   double scale, const float *d_weights, void *stream);
 
 /* ---- orientation matching --------------------------------------------- */
 
@@ -143,6 +153,37 @@ int spf_dist_argmin_f32(const float *d_img, const float *d_img_sq, int64_t n_img
                         void *stream);
 int spf_best_unpack(const uint64_t *d_best, int64_t n_img, int32_t *d_idx,
                     float *d_dist, void *stream);
+
+/* ---- autocorrelation merge: operator and device-resident CG -----------
+ * Replaces Merge.setup_linops / W_matvec / cg
+ * (spinifel/sequential/autocorrelation.py:152-225):
+ *   W x = S.conv(S.x) + rlambda x + flambda S.reg(S.x)
+ * with conv the Toeplitz product with ugrid_conv (type 1 of ones onto the
+ * M_ups grid, / M_ups^3, spf_merge_set_kernel) divided by M^3, or (form 1)
+ * the direct Re T1(D T2(.)) / (M_ups^3 M^3) through an attached NUFFT plan;
+ * reg the size-M circular filter by ifftshift(F_antisupport) (:116-128).
+ * d_support and d_antisupport are M^3 floats (C order, centred). */
+typedef struct spf_merge_s *spf_merge;
+int spf_merge_create(int M, int M_ups, double rlambda, double flambda,
+                     const float *d_support, const float *d_antisupport, spf_merge *out);
+int spf_merge_destroy(spf_merge merge);
+int spf_merge_info(spf_merge merge, int *fft_size);
+int spf_merge_set_kernel(spf_merge merge, const float *d_ugrid_conv, int M_ups,
+                         void *stream);
+int spf_merge_set_direct(spf_merge merge, spf_nufft_plan plan, const float *d_quats,
+                         int64_t n_orient, const float *d_ppr, int64_t n_pix,
+                         double coord_scale, const float *d_weights);
+/* d_y = W d_x (M^3 doubles); form 0 = Toeplitz, 1 = direct. */
+int spf_merge_apply(spf_merge merge, int form, const double *d_x, double *d_y,
+                    void *stream);
+/* scipy.sparse.linalg.cg semantics: stop when ||r|| < rtol ||b|| or after
+ * maxiter iterations; d_x holds x0 on entry (x0_is_zero skips W x0) and the
+ * solution on return; FP64 vectors and dot products.  d_hist (maxiter
+ * doubles, may be NULL) gets ||r|| at the start of each iteration and
+ * d_iters (device int, may be NULL) the iteration count.  No host
+ * synchronisation: the launch sequence can be captured in a CUDA graph. */
+int spf_merge_cg(spf_merge merge, int form, const double *d_b, double *d_x, int x0_is_zero,
+                 int maxiter, double rtol, double *d_hist, int *d_iters, void *stream);
 
 /* ---- BF16 tensor-core matching with exact FP32 re-rank ----------------
  * The precision form of SNM.euclidean_dist + argmin

@@ -59,6 +59,17 @@ SIGNATURES = {
     "spf_nufft_t1_spread_orient": [_c_void_p, _c_void_p, _i64, _c_void_p, _i64, _dbl, _c_void_p,
                                    _c_void_p],
     "spf_nufft_t1_finish": [_c_void_p, _int, _c_void_p, _c_void_p, _c_void_p],
+    "spf_nufft_interp_spread_orient": [_c_void_p, _c_void_p, _i64, _c_void_p, _i64, _dbl,
+                                       _c_void_p, _c_void_p],
+    "spf_merge_create": [_int, _int, _dbl, _dbl, _c_void_p, _c_void_p, ctypes.POINTER(_c_void_p)],
+    "spf_merge_destroy": [_c_void_p],
+    "spf_merge_info": [_c_void_p, ctypes.POINTER(_int)],
+    "spf_merge_set_kernel": [_c_void_p, _c_void_p, _int, _c_void_p],
+    "spf_merge_set_direct": [_c_void_p, _c_void_p, _c_void_p, _i64, _c_void_p, _i64, _dbl,
+                             _c_void_p],
+    "spf_merge_apply": [_c_void_p, _int, _c_void_p, _c_void_p, _c_void_p],
+    "spf_merge_cg": [_c_void_p, _int, _c_void_p, _c_void_p, _int, _int, _dbl, _c_void_p,
+                     _c_void_p, _c_void_p],
     "spf_knn_eudist_f32": [_c_void_p, _c_void_p, _i64, _i64, _i64, _c_void_p, _c_void_p],
     "spf_knn_eudist_f64": [_c_void_p, _c_void_p, _i64, _i64, _i64, _c_void_p, _c_void_p],
     "spf_knn_topk_f32": [_c_void_p, _i64, _i64, _int, _c_void_p, _c_void_p],

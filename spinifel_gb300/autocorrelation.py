@@ -64,11 +64,11 @@ def forward(ugrid, H_, K_, L_, support, use_recip_sym, N, eps=DEFAULT_EPS):
 
 
 def adjoint(nuvect, H_, K_, L_, M, use_recip_sym=True, support=None, eps=DEFAULT_EPS,
-            isign=+1):
+            isign=+1, plan=None):
     """Type 1 onto M^3 (isign +1), times support, real part, divided by M^3."""
     if _numel(H_):
         assert _max_abs(H_, K_, L_) < 3 * np.pi
-    P = plan_for(M, eps)
+    P = plan if plan is not None else plan_for(M, eps)
     x, y, z = (_arrays.to_dev(np.asarray(a).reshape(-1) if not _arrays.is_torch(a) else a)
                for a in (H_, K_, L_))
     c = nuvect if _arrays.is_torch(nuvect) else torch.as_tensor(np.asarray(nuvect))

@@ -1,0 +1,536 @@
+// Device-resident conjugate-gradient solve of the autocorrelation merge
+// (spinifel/sequential/autocorrelation.py:152-225):
+//
+//   W x = conv(x) + rlambda x + flambda reg(x),   d = A^H b + rlambda x0,
+//   conv(x) = S . (ugrid_conv (*) (S . x)) / M^3           (Toeplitz form)
+//           = S . Re T1(T2(S . x)) / (M_ups^3 M^3)         (direct form)
+//   reg(x)  = S . Re fftshift(ifftn(fftn(ifftshift(S . x)) . ifftshift(F_anti)))
+//
+// ugrid_conv is the type 1 of ones onto the M_ups grid divided by M_ups^3
+// (:158-166); only its modes -(M-1)..M-1 enter the product, so the circular
+// convolution runs on an FFT grid of any smooth size L >= 2M-1 (R2C / C2R,
+// the kernel's transform is real because ugrid_conv is real and even).  The
+// regulariser is a size-M circular operation and uses exactly M.
+//
+// CG follows scipy.sparse.linalg.cg (the solver the reference calls, :217)
+// step for step: stop when ||r|| < rtol ||b||, at most maxiter iterations.
+// x, r, p, q and every dot product are FP64; the operator is FP32.  Each
+// iteration is a fixed sequence of launches with no host synchronisation
+// (convergence is a device flag that turns later updates into no-ops), so a
+// whole solve can be captured in one CUDA graph.
+#include <cufft.h>
+
+#include "common.cuh"
+
+#include "../../include/spinifel_gb300.h"
+
+struct spf_merge_s {
+  int dev = 0;
+  int M = 0, L = 0;
+  int64_t n = 0;       // M^3
+  int64_t nL = 0;      // L^3
+  int64_t nLh = 0;     // L*L*(L/2+1)
+  int64_t nMh = 0;     // M*M*(M/2+1)
+  double rlambda = 0, flambda = 0;
+  double conv_scale = 0;  // applied after the C2R of the Toeplitz product
+  double direct_scale = 0;
+  float *support = nullptr;    // M^3
+  float *kernel_hat = nullptr; // nLh
+  float *mask_hat = nullptr;   // nMh
+  float *conv_in = nullptr;    // L^3
+  float2 *conv_freq = nullptr; // nLh
+  float *conv_out = nullptr;   // L^3
+  float *reg_in = nullptr;     // M^3
+  float2 *reg_freq = nullptr;  // nMh
+  float *reg_out = nullptr;    // M^3
+  float *modes = nullptr;      // M^3 (direct form input / output)
+  float *t1_out = nullptr;     // M^3
+  double *r = nullptr, *p = nullptr, *q = nullptr;
+  double *partial = nullptr;   // reduction scratch
+  double *scal = nullptr;      // device scalars
+  int *flags = nullptr;        // [0] done, [1] iterations
+  cufftHandle r2c_L = 0, c2r_L = 0, r2c_M = 0, c2r_M = 0;
+  bool plans_ok = false;
+  // direct form
+  spf_nufft_plan_s *nufft = nullptr;
+  const float *quats = nullptr, *ppr = nullptr, *weights = nullptr;
+  int64_t n_orient = 0, n_pix = 0;
+  double coord_scale = 0;
+};
+
+// device scalar slots
+enum { S_RHO = 0, S_RHO_PREV, S_ALPHA, S_BETA, S_PQ, S_ATOL, S_BNORM, S_COUNT };
+
+extern "C" int spf_nufft_t2_set_modes(spf_nufft_plan_s *, const float *, const float *, int, int,
+                                      void *);
+extern "C" int spf_nufft_t1_zero(spf_nufft_plan_s *, void *);
+extern "C" int spf_nufft_t1_finish(spf_nufft_plan_s *, int, float *, float *, void *);
+extern "C" int spf_nufft_interp_spread_orient(spf_nufft_plan_s *, const float *, int64_t,
+                                              const float *, int64_t, double, const float *,
+                                              void *);
+
+namespace spf {
+namespace cg {
+
+constexpr int RED_BLOCKS = 296;  // 2 x 148+; fixed so the reduction order is fixed
+constexpr int RED_THREADS = 256;
+
+static int next_smooth(int n) {
+  for (;; ++n) {
+    int m = n;
+    for (int p : {2, 3, 5, 7})
+      while (m % p == 0) m /= p;
+    if (m == 1) return n;
+  }
+}
+
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double sh[RED_THREADS / 32];
+  for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  v = 0.0;
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < RED_THREADS / 32 ? sh[threadIdx.x] : 0.0;
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  }
+  __syncthreads();
+  return v;
+}
+
+__global__ void __launch_bounds__(RED_THREADS)
+    k_dot_partial(const double *__restrict__ a, const double *__restrict__ b, int64_t n,
+                  double *__restrict__ partial) {
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * RED_THREADS)
+    s = fma(a[i], b[i], s);
+  s = block_sum(s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+__device__ __forceinline__ double sum_partials(const double *partial) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < RED_BLOCKS; i += RED_THREADS) v += partial[i];
+  return block_sum(v);
+}
+
+// stage 0: ||b|| -> atol; zero the counters
+__global__ void k_cg_init(const double *partial, double rtol, double *scal, int *flags) {
+  double bb = sum_partials(partial);
+  if (threadIdx.x == 0) {
+    double bn = sqrt(bb);
+    scal[S_BNORM] = bn;
+    scal[S_ATOL] = rtol * bn;
+    scal[S_RHO_PREV] = 1.0;
+    flags[0] = bn == 0.0 ? 1 : 0;
+    flags[1] = 0;
+  }
+}
+
+// stage 1: rho = r.r, convergence test, beta
+__global__ void k_cg_stage1(const double *partial, int it, double *scal, int *flags,
+                            double *hist) {
+  double rho = sum_partials(partial);
+  if (threadIdx.x == 0) {
+    if (hist) hist[it] = sqrt(rho);
+    if (!flags[0]) {
+      if (sqrt(rho) < scal[S_ATOL]) {
+        flags[0] = 1;
+      } else {
+        scal[S_RHO] = rho;
+        scal[S_BETA] = it > 0 ? rho / scal[S_RHO_PREV] : 0.0;
+      }
+    }
+  }
+}
+
+// stage 2: alpha = rho / p.q
+__global__ void k_cg_stage2(const double *partial, double *scal, const int *flags) {
+  double pq = sum_partials(partial);
+  if (threadIdx.x == 0 && !flags[0]) {
+    scal[S_PQ] = pq;
+    scal[S_ALPHA] = scal[S_RHO] / pq;
+    scal[S_RHO_PREV] = scal[S_RHO];
+  }
+}
+
+// p = r + beta p; operator inputs (S . p in FP32) for both forms
+__global__ void k_cg_update_p(double *__restrict__ p, const double *__restrict__ r,
+                              const double *__restrict__ scal, const int *__restrict__ flags,
+                              const float *__restrict__ S, int M, int L, float *__restrict__ conv_in,
+                              float *__restrict__ reg_in, float *__restrict__ modes) {
+  const bool done = flags[0] != 0;
+  const double beta = scal[S_BETA];
+  const int64_t n = (int64_t)M * M * M;
+  const int h = M / 2;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double pv = p[i];
+    if (!done) {
+      pv = r[i] + beta * pv;
+      p[i] = pv;
+    }
+    float v = (float)(pv * (double)S[i]);
+    int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
+    if (conv_in) conv_in[((int64_t)a * L + b) * L + c] = v;
+    if (modes) modes[i] = v;
+    // ifftshift: reg_in[j] = in[(j + M/2) mod M]  <=>  in[i] lands at j = (i - M/2) mod M
+    int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
+    reg_in[((int64_t)ja * M + jb) * M + jc] = v;
+  }
+}
+
+// apply to a plain vector (x0 or a test vector): same as update_p without the CG update
+__global__ void k_load_input(const double *__restrict__ x, const float *__restrict__ S, int M,
+                             int L, float *__restrict__ conv_in, float *__restrict__ reg_in,
+                             float *__restrict__ modes) {
+  const int64_t n = (int64_t)M * M * M;
+  const int h = M / 2;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float v = (float)(x[i] * (double)S[i]);
+    int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
+    if (conv_in) conv_in[((int64_t)a * L + b) * L + c] = v;
+    if (modes) modes[i] = v;
+    int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
+    reg_in[((int64_t)ja * M + jb) * M + jc] = v;
+  }
+}
+
+__global__ void k_mul_real(float2 *__restrict__ z, const float *__restrict__ w, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float s = w[i];
+    float2 v = z[i];
+    z[i] = make_float2(v.x * s, v.y * s);
+  }
+}
+
+// q = S conv * cs + rlambda x + flambda S reg / M^3, and the partial p.q
+// (conv from the Toeplitz product on the L grid, or from t1_out for the
+// direct form)
+__global__ void __launch_bounds__(RED_THREADS)
+    k_assemble(const double *__restrict__ x, const float *__restrict__ S, int M, int L,
+               const float *__restrict__ conv_out, const float *__restrict__ t1_out,
+               double conv_scale, const float *__restrict__ reg_out, double rlambda,
+               double flambda, double *__restrict__ q, double *__restrict__ partial) {
+  const int64_t n = (int64_t)M * M * M;
+  const int h = M / 2;
+  const double reg_scale = 1.0 / ((double)M * M * M);
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * RED_THREADS) {
+    int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
+    double sv = S[i];
+    double cv = conv_out ? (double)conv_out[((int64_t)a * L + b) * L + c] : (double)t1_out[i];
+    // fftshift: out[i] = reg_out[(i - M/2) mod M]
+    int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
+    double rv = reg_out[((int64_t)ja * M + jb) * M + jc];
+    double xv = x[i];
+    double qv = sv * cv * conv_scale + rlambda * xv + flambda * sv * rv * reg_scale;
+    q[i] = qv;
+    s = fma(xv, qv, s);
+  }
+  s = block_sum(s);
+  if (partial && threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+__global__ void k_cg_update_xr(double *__restrict__ x, double *__restrict__ r,
+                               const double *__restrict__ p, const double *__restrict__ q,
+                               const double *__restrict__ scal, int *__restrict__ flags,
+                               int64_t n) {
+  if (flags[0]) return;
+  const double alpha = scal[S_ALPHA];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = fma(alpha, p[i], x[i]);
+    r[i] = fma(-alpha, q[i], r[i]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) flags[1] += 1;
+}
+
+// r = b - q (q = W x0), or r = b when x0 is zero
+__global__ void k_sub(const double *__restrict__ b, const double *__restrict__ q,
+                      double *__restrict__ r, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    r[i] = q ? b[i] - q[i] : b[i];
+}
+
+// kernel_hat: g[m] = ugrid_conv[d + Mu/2] at m = d mod L for |d| <= M-1
+__global__ void k_embed_kernel(const float *__restrict__ ugrid_conv, int Mu, int M, int L,
+                               float *__restrict__ g) {
+  const int64_t nL = (int64_t)L * L * L;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nL;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int m3 = (int)(i % L), m2 = (int)((i / L) % L), m1 = (int)(i / ((int64_t)L * L));
+    int d1 = m1 <= L / 2 ? m1 : m1 - L;
+    int d2 = m2 <= L / 2 ? m2 : m2 - L;
+    int d3 = m3 <= L / 2 ? m3 : m3 - L;
+    float v = 0.0f;
+    if (abs(d1) <= M - 1 && abs(d2) <= M - 1 && abs(d3) <= M - 1) {
+      int a = d1 + Mu / 2, b = d2 + Mu / 2, c = d3 + Mu / 2;
+      if (a >= 0 && a < Mu && b >= 0 && b < Mu && c >= 0 && c < Mu)
+        v = ugrid_conv[((int64_t)a * Mu + b) * Mu + c];
+    }
+    g[i] = v;
+  }
+}
+
+__global__ void k_real_part(const float2 *__restrict__ z, float *__restrict__ out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = z[i].x;
+}
+
+// mask_hat[m] = F_anti[(m + M/2) mod M] on the R2C half spectrum
+__global__ void k_mask_half(const float *__restrict__ F, int M, float *__restrict__ out) {
+  const int Mh = M / 2 + 1;
+  const int64_t n = (int64_t)M * M * Mh;
+  const int h = M / 2;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int m3 = (int)(i % Mh), m2 = (int)((i / Mh) % M), m1 = (int)(i / ((int64_t)M * Mh));
+    int a = (m1 + h) % M, b = (m2 + h) % M, c = (m3 + h) % M;
+    out[i] = F[((int64_t)a * M + b) * M + c];
+  }
+}
+
+static int cufft_ok(cufftResult r, const char *what) {
+  if (r == CUFFT_SUCCESS) {
+    count_launch();
+    return SPF_OK;
+  }
+  set_error("%s: cuFFT error %d", what, (int)r);
+  return r == CUFFT_ALLOC_FAILED ? SPF_ERR_OOM : SPF_ERR_CUDA;
+}
+
+static int grid1(int64_t n) { return grid_for(n, 256, (int64_t)sm_count() * 8); }
+
+// conv part of the operator from conv_in / reg_in / modes already loaded
+static int apply_operator_core(spf_merge_s *G, bool direct, cudaStream_t s) {
+  cufftSetStream(G->r2c_M, s);
+  cufftSetStream(G->c2r_M, s);
+  if (!direct) {
+    cufftSetStream(G->r2c_L, s);
+    cufftSetStream(G->c2r_L, s);
+    SPF_TRY(cufft_ok(cufftExecR2C(G->r2c_L, G->conv_in, reinterpret_cast<cufftComplex *>(G->conv_freq)),
+                     "conv R2C"));
+    k_mul_real<<<grid1(G->nLh), 256, 0, s>>>(G->conv_freq, G->kernel_hat, G->nLh);
+    SPF_TRY(check_launch("k_mul_real"));
+    SPF_TRY(cufft_ok(cufftExecC2R(G->c2r_L, reinterpret_cast<cufftComplex *>(G->conv_freq), G->conv_out),
+                     "conv C2R"));
+  } else {
+    SPF_TRY(spf_nufft_t2_set_modes(G->nufft, G->modes, nullptr, -1, 0, s));
+    SPF_TRY(spf_nufft_t1_zero(G->nufft, s));
+    SPF_TRY(spf_nufft_interp_spread_orient(G->nufft, G->quats, G->n_orient, G->ppr, G->n_pix,
+                                           G->coord_scale, G->weights, s));
+    SPF_TRY(spf_nufft_t1_finish(G->nufft, +1, G->t1_out, nullptr, s));
+  }
+  SPF_TRY(cufft_ok(cufftExecR2C(G->r2c_M, G->reg_in, reinterpret_cast<cufftComplex *>(G->reg_freq)),
+                   "reg R2C"));
+  k_mul_real<<<grid1(G->nMh), 256, 0, s>>>(G->reg_freq, G->mask_hat, G->nMh);
+  SPF_TRY(check_launch("k_mul_real"));
+  return cufft_ok(cufftExecC2R(G->c2r_M, reinterpret_cast<cufftComplex *>(G->reg_freq), G->reg_out),
+                  "reg C2R");
+}
+
+}  // namespace cg
+}  // namespace spf
+
+using namespace spf;
+using namespace spf::cg;
+
+extern "C" {
+
+int spf_merge_destroy(spf_merge_s *G);
+
+int spf_merge_create(int M, int M_ups, double rlambda, double flambda, const float *d_support,
+                     const float *d_antisupport, spf_merge_s **out) {
+  SPF_REQUIRE(out != nullptr, "spf_merge_create: out is NULL");
+  *out = nullptr;
+  SPF_REQUIRE(M >= 3 && M <= 1024 && M_ups >= 2 * M - 1, "spf_merge_create: bad M / M_ups");
+  SPF_REQUIRE(d_support && d_antisupport, "spf_merge_create: NULL pointer");
+  auto *G = new spf_merge_s();
+  cudaGetDevice(&G->dev);
+  G->M = M;
+  G->L = next_smooth(2 * M - 1);
+  G->n = (int64_t)M * M * M;
+  G->nL = (int64_t)G->L * G->L * G->L;
+  G->nLh = (int64_t)G->L * G->L * (G->L / 2 + 1);
+  G->nMh = (int64_t)M * M * (M / 2 + 1);
+  G->rlambda = rlambda;
+  G->flambda = flambda;
+  G->conv_scale = 1.0 / ((double)M * M * M) / (double)G->nL;
+  G->direct_scale = 1.0 / ((double)M_ups * M_ups * M_ups) / ((double)M * M * M);
+  int st = SPF_OK;
+  auto alloc = [&](void **p, size_t bytes) {
+    if (st == SPF_OK) st = check_cuda(cudaMalloc(p, bytes), "spf_merge_create");
+  };
+  alloc((void **)&G->support, G->n * sizeof(float));
+  alloc((void **)&G->kernel_hat, G->nLh * sizeof(float));
+  alloc((void **)&G->mask_hat, G->nMh * sizeof(float));
+  alloc((void **)&G->conv_in, G->nL * sizeof(float));
+  alloc((void **)&G->conv_freq, G->nLh * sizeof(float2));
+  alloc((void **)&G->conv_out, G->nL * sizeof(float));
+  alloc((void **)&G->reg_in, G->n * sizeof(float));
+  alloc((void **)&G->reg_freq, G->nMh * sizeof(float2));
+  alloc((void **)&G->reg_out, G->n * sizeof(float));
+  alloc((void **)&G->modes, G->n * sizeof(float));
+  alloc((void **)&G->t1_out, G->n * sizeof(float));
+  alloc((void **)&G->r, G->n * sizeof(double));
+  alloc((void **)&G->p, G->n * sizeof(double));
+  alloc((void **)&G->q, G->n * sizeof(double));
+  alloc((void **)&G->partial, RED_BLOCKS * sizeof(double));
+  alloc((void **)&G->scal, S_COUNT * sizeof(double));
+  alloc((void **)&G->flags, 2 * sizeof(int));
+  if (st == SPF_OK) {
+    bool ok = cufftPlan3d(&G->r2c_L, G->L, G->L, G->L, CUFFT_R2C) == CUFFT_SUCCESS &&
+              cufftPlan3d(&G->c2r_L, G->L, G->L, G->L, CUFFT_C2R) == CUFFT_SUCCESS &&
+              cufftPlan3d(&G->r2c_M, M, M, M, CUFFT_R2C) == CUFFT_SUCCESS &&
+              cufftPlan3d(&G->c2r_M, M, M, M, CUFFT_C2R) == CUFFT_SUCCESS;
+    G->plans_ok = ok;
+    if (!ok) {
+      set_error("spf_merge_create: cufftPlan3d failed (L = %d, M = %d)", G->L, M);
+      st = SPF_ERR_CUDA;
+    }
+  }
+  if (st == SPF_OK) {
+    st = check_cuda(cudaMemcpy(G->support, d_support, G->n * sizeof(float),
+                               cudaMemcpyDeviceToDevice), "spf_merge_create");
+  }
+  if (st == SPF_OK) {
+    cudaMemset(G->conv_in, 0, G->nL * sizeof(float));
+    cudaMemset(G->kernel_hat, 0, G->nLh * sizeof(float));
+    k_mask_half<<<grid1(G->nMh), 256>>>(d_antisupport, M, G->mask_hat);
+    st = check_launch("k_mask_half");
+  }
+  if (st == SPF_OK) st = check_cuda(cudaDeviceSynchronize(), "spf_merge_create");
+  if (st != SPF_OK) {
+    spf_merge_destroy(G);
+    return st;
+  }
+  *out = G;
+  return SPF_OK;
+}
+
+int spf_merge_destroy(spf_merge_s *G) {
+  if (!G) return SPF_OK;
+  void *bufs[] = {G->support, G->kernel_hat, G->mask_hat, G->conv_in, G->conv_freq,
+                  G->conv_out, G->reg_in, G->reg_freq, G->reg_out, G->modes, G->t1_out,
+                  G->r, G->p, G->q, G->partial, G->scal, G->flags};
+  for (void *b : bufs) cudaFree(b);
+  if (G->plans_ok) {
+    cufftDestroy(G->r2c_L);
+    cufftDestroy(G->c2r_L);
+    cufftDestroy(G->r2c_M);
+    cufftDestroy(G->c2r_M);
+  }
+  delete G;
+  return SPF_OK;
+}
+
+int spf_merge_info(spf_merge_s *G, int *fft_size) {
+  SPF_REQUIRE(G != nullptr, "spf_merge_info: NULL");
+  if (fft_size) *fft_size = G->L;
+  return SPF_OK;
+}
+
+int spf_merge_set_kernel(spf_merge_s *G, const float *d_ugrid_conv, int M_ups, void *stream) {
+  SPF_REQUIRE(G && d_ugrid_conv, "spf_merge_set_kernel: NULL pointer");
+  SPF_REQUIRE(M_ups >= 2 * G->M - 1, "spf_merge_set_kernel: M_ups < 2M-1");
+  cudaStream_t s = as_stream(stream);
+  k_embed_kernel<<<grid1(G->nL), 256, 0, s>>>(d_ugrid_conv, M_ups, G->M, G->L, G->conv_out);
+  SPF_TRY(check_launch("k_embed_kernel"));
+  cufftSetStream(G->r2c_L, s);
+  SPF_TRY(cufft_ok(cufftExecR2C(G->r2c_L, G->conv_out, reinterpret_cast<cufftComplex *>(G->conv_freq)),
+                   "kernel R2C"));
+  k_real_part<<<grid1(G->nLh), 256, 0, s>>>(G->conv_freq, G->kernel_hat, G->nLh);
+  return check_launch("k_real_part");
+}
+
+int spf_merge_set_direct(spf_merge_s *G, spf_nufft_plan_s *plan, const float *d_quats,
+                         int64_t n_orient, const float *d_ppr, int64_t n_pix, double coord_scale,
+                         const float *d_weights) {
+  SPF_REQUIRE(G && plan && d_quats && d_ppr, "spf_merge_set_direct: NULL pointer");
+  G->nufft = plan;
+  G->quats = d_quats;
+  G->ppr = d_ppr;
+  G->weights = d_weights;
+  G->n_orient = n_orient;
+  G->n_pix = n_pix;
+  G->coord_scale = coord_scale;
+  return SPF_OK;
+}
+
+// y = W x (form: 0 Toeplitz, 1 direct)
+int spf_merge_apply(spf_merge_s *G, int form, const double *d_x, double *d_y, void *stream) {
+  SPF_REQUIRE(G && d_x && d_y, "spf_merge_apply: NULL pointer");
+  SPF_REQUIRE(form == 0 || (form == 1 && G->nufft), "spf_merge_apply: bad form / no direct set-up");
+  cudaStream_t s = as_stream(stream);
+  bool direct = form == 1;
+  k_load_input<<<grid1(G->n), 256, 0, s>>>(d_x, G->support, G->M, G->L,
+                                           direct ? nullptr : G->conv_in, G->reg_in,
+                                           direct ? G->modes : nullptr);
+  SPF_TRY(check_launch("k_load_input"));
+  SPF_TRY(apply_operator_core(G, direct, s));
+  k_assemble<<<RED_BLOCKS, RED_THREADS, 0, s>>>(
+      d_x, G->support, G->M, G->L, direct ? nullptr : G->conv_out, G->t1_out,
+      direct ? G->direct_scale : G->conv_scale, G->reg_out, G->rlambda, G->flambda, d_y, nullptr);
+  return check_launch("k_assemble");
+}
+
+// CG from x (x0 in, solution out).  hist (maxiter floats of ||r||, may be
+// NULL) and the iteration count are left on the device; iters_out (device
+// int, may be NULL) receives the count.
+int spf_merge_cg(spf_merge_s *G, int form, const double *d_b, double *d_x, int x0_is_zero,
+                 int maxiter, double rtol, double *d_hist, int *d_iters_out, void *stream) {
+  SPF_REQUIRE(G && d_b && d_x, "spf_merge_cg: NULL pointer");
+  SPF_REQUIRE(maxiter >= 0, "spf_merge_cg: maxiter < 0");
+  SPF_REQUIRE(form == 0 || (form == 1 && G->nufft), "spf_merge_cg: bad form / no direct set-up");
+  cudaStream_t s = as_stream(stream);
+  bool direct = form == 1;
+  const int64_t n = G->n;
+  // r = b - W x0
+  if (x0_is_zero) {
+    k_sub<<<grid1(n), 256, 0, s>>>(d_b, nullptr, G->r, n);
+    SPF_TRY(check_launch("k_sub"));
+  } else {
+    SPF_TRY(spf_merge_apply(G, form, d_x, G->q, stream));
+    k_sub<<<grid1(n), 256, 0, s>>>(d_b, G->q, G->r, n);
+    SPF_TRY(check_launch("k_sub"));
+  }
+  k_dot_partial<<<RED_BLOCKS, RED_THREADS, 0, s>>>(d_b, d_b, n, G->partial);
+  SPF_TRY(check_launch("k_dot_partial"));
+  k_cg_init<<<1, RED_THREADS, 0, s>>>(G->partial, rtol, G->scal, G->flags);
+  SPF_TRY(check_launch("k_cg_init"));
+  SPF_TRY(check_cuda(cudaMemsetAsync(G->p, 0, n * sizeof(double), s), "spf_merge_cg"));
+  for (int it = 0; it < maxiter; ++it) {
+    k_dot_partial<<<RED_BLOCKS, RED_THREADS, 0, s>>>(G->r, G->r, n, G->partial);
+    SPF_TRY(check_launch("k_dot_partial"));
+    k_cg_stage1<<<1, RED_THREADS, 0, s>>>(G->partial, it, G->scal, G->flags, d_hist);
+    SPF_TRY(check_launch("k_cg_stage1"));
+    k_cg_update_p<<<grid1(n), 256, 0, s>>>(G->p, G->r, G->scal, G->flags, G->support, G->M, G->L,
+                                           direct ? nullptr : G->conv_in, G->reg_in,
+                                           direct ? G->modes : nullptr);
+    SPF_TRY(check_launch("k_cg_update_p"));
+    SPF_TRY(apply_operator_core(G, direct, s));
+    k_assemble<<<RED_BLOCKS, RED_THREADS, 0, s>>>(
+        G->p, G->support, G->M, G->L, direct ? nullptr : G->conv_out, G->t1_out,
+        direct ? G->direct_scale : G->conv_scale, G->reg_out, G->rlambda, G->flambda, G->q,
+        G->partial);
+    SPF_TRY(check_launch("k_assemble"));
+    k_cg_stage2<<<1, RED_THREADS, 0, s>>>(G->partial, G->scal, G->flags);
+    SPF_TRY(check_launch("k_cg_stage2"));
+    k_cg_update_xr<<<grid1(n), 256, 0, s>>>(d_x, G->r, G->p, G->q, G->scal, G->flags, n);
+    SPF_TRY(check_launch("k_cg_update_xr"));
+  }
+  if (d_iters_out)
+    SPF_TRY(check_cuda(cudaMemcpyAsync(d_iters_out, G->flags + 1, sizeof(int),
+                                       cudaMemcpyDeviceToDevice, s), "spf_merge_cg"));
+  return SPF_OK;
+}
+
+}  // extern "C"

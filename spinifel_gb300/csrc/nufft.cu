@@ -325,6 +325,55 @@ __global__ void k_t1_spread_orient(float *__restrict__ acc_pad, GridGeom g,
   spread_point<W>(acc_pad, g, h * scale1, k * scale2, l * scale3, cj);
 }
 
+// Fused type 2 -> type 1 at the same points (the direct A^H D A operator):
+// each point interpolates Re of the type-2 fine grid, multiplies by its
+// weight and spreads the result back with the same kernel weights.
+template <int W>
+__global__ void k_interp_spread_orient(const float *__restrict__ re_pad,
+                                       float *__restrict__ acc_pad, GridGeom g,
+                                       const float *__restrict__ quats,
+                                       const float *__restrict__ ppr, int64_t n_pix, float scale1,
+                                       float scale2, float scale3,
+                                       const float *__restrict__ weights) {
+  int64_t o = blockIdx.x;
+  int64_t p = blockIdx.y * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n_pix) return;
+  float h, k, l;
+  rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
+  float w1[W], w2[W], w3[W];
+  int i0 = axis_setup<W>(h * scale1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
+  int j0 = axis_setup<W>(k * scale2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
+  int k0 = axis_setup<W>(l * scale3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
+  float acc = 0.0f;
+#pragma unroll
+  for (int a = 0; a < W; ++a) {
+    float acc_a = 0.0f;
+#pragma unroll
+    for (int b = 0; b < W; ++b) {
+      const float *row = re_pad + ((size_t)(i0 + a) * g.p2 + (j0 + b)) * g.p3 + k0;
+      float r = 0.0f;
+#pragma unroll
+      for (int c = 0; c < W; ++c) r = fmaf(w3[c], __ldg(row + c), r);
+      acc_a = fmaf(w2[b], r, acc_a);
+    }
+    acc = fmaf(w1[a], acc_a, acc);
+  }
+  if (weights) acc *= weights[o * n_pix + p];
+  if (acc == 0.0f) return;
+#pragma unroll
+  for (int c = 0; c < W; ++c) w3[c] *= acc;
+#pragma unroll
+  for (int a = 0; a < W; ++a) {
+#pragma unroll
+    for (int b = 0; b < W; ++b) {
+      float wab = w1[a] * w2[b];
+      float *row = acc_pad + ((size_t)(i0 + a) * g.p2 + (j0 + b)) * g.p3 + k0;
+#pragma unroll
+      for (int c = 0; c < W; ++c) atomicAdd(row + c, wab * w3[c]);
+    }
+  }
+}
+
 // fine[l] = sum of acc_pad[i] over padded i == l + off (mod n)  (Im = 0).
 __global__ void k_t1_fold(const float *__restrict__ acc_pad, GridGeom g,
                           float2 *__restrict__ fine) {
@@ -604,6 +653,27 @@ int spf_nufft_t1_spread_orient(spf_nufft_plan P, const float *d_quats, int64_t n
   SPF_W_DISPATCH(P->w, (k_t1_spread_orient<W><<<grid, 256, 0, s>>>(P->acc_pad, g, d_quats, d_ppr,
                                                                       n_pix, s1, s2, s3, d_c)));
   return check_launch("k_t1_spread_orient");
+}
+
+int spf_nufft_interp_spread_orient(spf_nufft_plan P, const float *d_quats, int64_t n_orient,
+                                   const float *d_ppr, int64_t n_pix, double scale,
+                                   const float *d_weights, void *stream) {
+  SPF_TRY(check_plan(P, "spf_nufft_interp_spread_orient"));
+  SPF_REQUIRE(n_orient >= 0 && n_pix >= 0, "spf_nufft_interp_spread_orient: negative size");
+  if (n_orient == 0 || n_pix == 0) return SPF_OK;
+  SPF_REQUIRE(d_quats && d_ppr, "spf_nufft_interp_spread_orient: NULL pointer");
+  SPF_REQUIRE(n_orient < (1LL << 31) && n_pix <= 65535LL * 256,
+              "spf_nufft_interp_spread_orient: size too large");
+  cudaStream_t s = as_stream(stream);
+  GridGeom g = geom_of(P);
+  float s1 = (float)(scale * P->n[0] / (2.0 * M_PI));
+  float s2 = (float)(scale * P->n[1] / (2.0 * M_PI));
+  float s3 = (float)(scale * P->n[2] / (2.0 * M_PI));
+  dim3 grid((unsigned)n_orient, (unsigned)((n_pix + 255) / 256));
+  SPF_W_DISPATCH(P->w, (k_interp_spread_orient<W><<<grid, 256, 0, s>>>(
+                           P->re_pad, P->acc_pad, g, d_quats, d_ppr, n_pix, s1, s2, s3,
+                           d_weights)));
+  return check_launch("k_interp_spread_orient");
 }
 
 int spf_nufft_t1_finish(spf_nufft_plan P, int isign, float *d_out_re, float *d_out_im,

@@ -97,9 +97,13 @@ class NUFFT:
         return torch.complex(re, im)
 
     def adjoint(self, nuvect, H_, K_, L_, support, use_reciprocal_symmetry, M):
+        """Type 1 onto M^3 (isign -1), times support, real part, / M^3
+        (nufft_ext.py:287-327); returns a device tensor."""
         from .. import autocorrelation as ac
 
-        assert np.shape(H_) == np.shape(K_) == np.shape(L_)
-        out = ac.adjoint(nuvect, H_, K_, L_, M, use_recip_sym=use_reciprocal_symmetry,
-                         support=support, eps=self.eps, isign=self.isign)
-        return out if _arrays.is_torch(out) else torch.as_tensor(out, device=_arrays.device())
+        assert tuple(np.shape(H_)) == tuple(np.shape(K_)) == tuple(np.shape(L_))
+        c = nuvect if _arrays.is_torch(nuvect) else torch.as_tensor(np.asarray(nuvect),
+                                                                    device=_arrays.device())
+        out = ac.adjoint(c, H_, K_, L_, M, use_recip_sym=use_reciprocal_symmetry,
+                         support=support, eps=self.eps, isign=self.isign, plan=self.plan(M))
+        return out
