@@ -4,8 +4,10 @@ Workload (the plain-FP32-at-scale configuration): a 81^3 float32 model,
 4 x 128 x 128 = 65,536-pixel frames, 100,000 reference orientations sliced by
 the type-2 NUFFT at eps 1e-6 and kept resident on the device, 10,000 Poisson
 frames (mean 0.5 photons/pixel, uint16 counts).  One step = orient every
-frame: distance to every reference + best index (the BF16 tensor-core path
-with top-8 FP32 re-rank when available, else the plain FP32 path).
+frame: bf16 tensor-core distances to every reference (tcgen05), per-frame
+top-8, exact FP32 re-rank and certificate (uncertified frames re-matched
+exactly).  The plain FP32 path is timed on the same frames in the same run
+and the two argmins compared.
 
 value : frames/s with frames and references resident in HBM;
 e2e   : frames/s through the host API: uint16 frames copied from pinned host
@@ -221,7 +223,6 @@ def main():
     e1.record()
     barrier()
     slice_ms = e0.elapsed_time(e1)
-    refs_sq = matching.row_sqnorm(refs)
 
     # --- frames: Poisson counts of slices at other orientations -------------
     imgs_f = torch.empty(W["n_img"], n_pix, dtype=torch.float32, device=dev)
@@ -231,72 +232,104 @@ def main():
     lam *= W["photons"] / lam.mean()
     gen = torch.Generator(device=dev)
     gen.manual_seed(W["seed"] + 17 + rank)
-    counts = torch.poisson(lam, generator=gen).clamp_(max=65535)
-    # uint16 counts on the host (stored in an int16 tensor: same bytes)
-    c32 = counts.to(torch.int32)
-    imgs_u16_host = torch.where(c32 > 32767, c32 - 65536, c32).to(torch.int16).cpu().pin_memory()
-    imgs = counts.float().contiguous()
-    del c32
-    del lam, counts, imgs_f
-    # SNM scales the references by the std ratio (orientation_matching.py:165)
-    refs *= (imgs.double().std() / refs.double().std()).float()
-    refs_sq = matching.row_sqnorm(refs)
+    counts = torch.poisson(lam, generator=gen).clamp_(max=65535).to(torch.int32)
+    del lam, imgs_f
+    # uint16 counts (stored in an int16 tensor: same bytes)
+    counts16 = torch.where(counts > 32767, counts - 65536, counts).to(torch.int16)
+    del counts
+    imgs_u16_host = counts16.cpu().pin_memory()
+    frames = matching.FrameSet.from_counts(counts16)
+    del counts16
+    # SNM scales the references to the frames' std (orientation_matching.py:165)
+    refs *= (frames.f32.double().std() / refs.double().std()).float()
+    rset = matching.ReferenceSet(refs)
+    torch.cuda.synchronize()
 
-    def step_plain(x):
-        return matching.argmin_fp32(x, refs, refs_sq=refs_sq)
+    # --- BF16 tensor cores + exact FP32 re-rank (the measured path) ---------
+    st_bf = {}
 
-    step = step_plain
-    path = "plain-fp32"
+    def step_bf16(fr):
+        return matching.match_bf16(fr, rset, stats=st_bf)
 
-    # --- device-resident timing ---------------------------------------------
     for _ in range(args.warmup):
-        step(imgs)
+        step_bf16(frames)
     barrier()
     l0 = _lib.launch_count()
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         t0.record()
         for _ in range(args.steps):
-            idx, _ = step(imgs)
+            idx_bf, _ = step_bf16(frames)
         t1.record()
         barrier()
-    launches = (_lib.launch_count() - l0)
+    launches = (_lib.launch_count() - l0) // max(args.steps, 1) * args.steps
     ms = t0.elapsed_time(t1) / args.steps
     ms_t = torch.tensor([ms], device=dev)
     if world > 1:
         dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
     ms = float(ms_t.item())
     value = W["n_img"] * world / (ms / 1e3)
+    matching.check_device_error()
 
     # --- dominant kernel alone (CUDA events on its stream) ------------------
-    isq = matching.row_sqnorm(imgs)
-    tr = matching.BestTracker(W["n_img"], dev)
+    tiles = int(_lib.lib().spf_dist_topk_bf16_tiles(rset.n_ref))
+    cd = torch.empty(tiles * frames.n * 8, dtype=torch.float32, device=dev)
+    ci = torch.empty(tiles * frames.n * 8, dtype=torch.int32, device=dev)
     k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    k0.record()
-    tr.update_fp32(imgs, isq, refs, refs_sq, 0)
-    k1.record()
-    torch.cuda.synchronize()
-    k_ms = k0.elapsed_time(k1)
+    k_ms_all = []
+    for _ in range(3):
+        k0.record()
+        _lib.call("spf_dist_topk_bf16", _lib.ptr(frames.bf16), frames.n, _lib.ptr(rset.bf16),
+                  rset.n_ref, rset.n_pix, rset.ld, _lib.ptr(rset.sq), _lib.ptr(cd), _lib.ptr(ci),
+                  _lib.stream_handle())
+        k1.record()
+        torch.cuda.synchronize()
+        k_ms_all.append(k0.elapsed_time(k1))
+    k_ms = float(np.median(k_ms_all))
+    del cd, ci
     flops = 2.0 * W["n_img"] * W["n_ref"] * n_pix
     peaks, peak_src = load_peaks()
-    sm_clock = 2070.0
-    fp32_peak = 152 * 128 * 2 * sm_clock * 1e6 / 1e12  # nominal SIMT FP32 at max clock
-    roofline = {"bound": "fp32-simt", "achieved": flops / (k_ms / 1e3) / 1e12,
-                "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": flops / (k_ms / 1e3) / 1e12 / fp32_peak, "traffic": None,
-                "kernel": "k_dist_argmin_f32", "peak_source": "nominal (152 SM x 128 FMA x 2 "
-                "x 2070 MHz); measured peaks cover HBM and bf16 only"}
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    achieved = flops / (k_ms / 1e3) / 1e12
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None, "kernel": "k_dist_topk_bf16",
+                "kernel_ms": k_ms, "peak_source": f"bf16_tflops ({peak_src}, burst)"}
+
+    # --- the plain FP32 path on the same GPU, same frames -------------------
+    def step_plain(fr):
+        return matching.argmin_fp32(fr.f32, rset.f32, images_sq=fr.sq, refs_sq=rset.sq)
+
+    step_plain(frames)
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p_steps = max(1, min(args.steps, 2))
+    p0.record()
+    for _ in range(p_steps):
+        idx_pl, _ = step_plain(frames)
+    p1.record()
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1) / p_steps
+    # argmin identity: equal, or a tie within 1e-6 relative in FP64
+    diff = torch.nonzero(idx_bf != idx_pl).flatten()
+    n_diff = int(diff.numel())
+    n_nontie = 0
+    if n_diff:
+        xs = frames.f32.index_select(0, diff).double()
+        ra = rset.f32.index_select(0, idx_bf.index_select(0, diff).long()).double()
+        rb = rset.f32.index_select(0, idx_pl.index_select(0, diff).long()).double()
+        da = ((xs - ra) ** 2).sum(1)
+        db = ((xs - rb) ** 2).sum(1)
+        n_nontie = int(((da - db).abs() > 1e-6 * torch.maximum(da, db)).sum().item())
 
     # --- end to end through the host API ------------------------------------
     out_host = torch.empty(W["n_img"], dtype=torch.int32).pin_memory()
-
     u16_dev = torch.empty_like(imgs_u16_host, device=dev)
-    x_dev = torch.empty(W["n_img"], n_pix, dtype=torch.float32, device=dev)
+    fr_e2e = matching.FrameSet.from_counts(u16_dev.copy_(imgs_u16_host))
 
     def e2e_step():
         u16_dev.copy_(imgs_u16_host, non_blocking=True)
-        matching.ingest_u16(u16_dev, x_dev)
-        i, _ = step(x_dev)
+        matching.FrameSet.from_counts(u16_dev, out=fr_e2e)
+        i, _ = step_bf16(fr_e2e)
         out_host.copy_(i, non_blocking=True)
 
     for _ in range(max(1, args.warmup)):
@@ -311,6 +344,7 @@ def main():
     e2e = {"value": W["n_img"] * world / (e2e_ms / 1e3), "unit": "frames/s",
            "h2d_bytes_per_step": int(imgs_u16_host.numel() * 2),
            "d2h_bytes_per_step": int(out_host.numel() * 4)}
+    same_e2e = bool(torch.equal(out_host.to(dev), idx_bf))
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -320,10 +354,17 @@ def main():
         out = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "dtype": "f32" if path == "plain-fp32" else "bf16", "data": "synthetic",
-               "config": config_dict(W), "path": path,
+               "dtype": "bf16", "data": "synthetic", "config": config_dict(W),
+               "path": "bf16-tcgen05 + top-8 + exact fp32 re-rank",
                "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
                "gpu_launches": int(launches), "clocks": clk.summary(),
+               "plain_fp32": {"value": W["n_img"] / (plain_ms / 1e3), "unit": "frames/s",
+                              "ms_per_step": plain_ms,
+                              "tflops": flops / (plain_ms / 1e3) / 1e12},
+               "speedup_vs_plain_fp32": plain_ms / ms,
+               "argmin": {"differs_from_plain": n_diff, "non_tie_differences": n_nontie,
+                          "identical": n_nontie == 0, "uncertified_frames":
+                              st_bf.get("uncertified"), "e2e_equals_device": same_e2e},
                "slicing": {"ms_all_refs": slice_ms,
                            "points_per_s": W["n_ref"] * n_pix / (slice_ms / 1e3)},
                "peaks_source": peak_src}

@@ -129,11 +129,13 @@ int spf_knn_topk_f64(const double *d_dist, int64_t n_data, int64_t n_ref, int k,
                      int32_t *d_idx, void *stream);
 
 /* Frame ingest: uint16 photon counts [n_img][n_pix] -> FP32 copy, and
- * optionally a bf16 copy and the FP32 squared norm of each frame (NULL to
- * skip).  Replaces the host-side cast of the data images in SNM.__init__
+ * optionally a bf16 copy (row stride ld >= n_pix, padding zeroed), the FP32
+ * squared norm and sqrt(sum x^4) of each frame (NULL to skip).  Replaces
+ * the host-side cast of the data images in SNM.__init__
  * (spinifel/sequential/orientation_matching.py:70-75). */
 int spf_frames_ingest_u16(const uint16_t *d_counts, int64_t n_img, int64_t n_pix,
-                          float *d_f32, void *d_bf16, float *d_sq, void *stream);
+                          float *d_f32, void *d_bf16, int64_t ld, float *d_sq, float *d_n4,
+                          void *stream);
 
 /* Squared norms of rows: d_out[r] = sum_p x[r,p]^2 (FP32 data, FP32 result
  * accumulated in FP64 then rounded). */

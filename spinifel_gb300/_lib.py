@@ -74,8 +74,8 @@ SIGNATURES = {
     "spf_knn_eudist_f64": [_c_void_p, _c_void_p, _i64, _i64, _i64, _c_void_p, _c_void_p],
     "spf_knn_topk_f32": [_c_void_p, _i64, _i64, _int, _c_void_p, _c_void_p],
     "spf_knn_topk_f64": [_c_void_p, _i64, _i64, _int, _c_void_p, _c_void_p],
-    "spf_frames_ingest_u16": [_c_void_p, _i64, _i64, _c_void_p, _c_void_p, _c_void_p,
-                              _c_void_p],
+    "spf_frames_ingest_u16": [_c_void_p, _i64, _i64, _c_void_p, _c_void_p, _i64, _c_void_p,
+                              _c_void_p, _c_void_p],
     "spf_row_sqnorm_f32": [_c_void_p, _i64, _i64, _c_void_p, _c_void_p],
     "spf_best_init": [_c_void_p, _i64, _c_void_p],
     "spf_dist_argmin_f32": [_c_void_p, _c_void_p, _i64, _c_void_p, _c_void_p, _i64, _i64, _i64,

@@ -249,26 +249,34 @@ __global__ void k_row_sqnorm(const float *__restrict__ x, int64_t n_rows, int64_
   }
 }
 
-// uint16 counts -> f32 (+ bf16) (+ squared norm); one warp per frame
+// uint16 counts -> f32 (+ bf16) (+ squared norm, 4-norm); one warp per frame
 __global__ void k_ingest_u16(const uint16_t *__restrict__ in, int64_t n_img, int64_t n_pix,
-                             float *__restrict__ f32, __nv_bfloat16 *__restrict__ bf,
-                             float *__restrict__ sq) {
+                             float *__restrict__ f32, __nv_bfloat16 *__restrict__ bf, int64_t ld,
+                             float *__restrict__ sq, float *__restrict__ n4) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int64_t r = warp; r < n_img; r += nwarps) {
     const uint16_t *p = in + r * n_pix;
-    double s = 0.0;
+    double s2 = 0.0, s4 = 0.0;
     for (int64_t k = lane; k < n_pix; k += 32) {
       float v = (float)p[k];
       f32[r * n_pix + k] = v;
-      if (bf) bf[r * n_pix + k] = __float2bfloat16_rn(v);
-      s = fma((double)v, (double)v, s);
+      if (bf) bf[r * ld + k] = __float2bfloat16_rn(v);
+      double v2 = (double)v * (double)v;
+      s2 += v2;
+      s4 = fma(v2, v2, s4);
     }
-    if (sq) {
+    if (bf)
+      for (int64_t k = n_pix + lane; k < ld; k += 32) bf[r * ld + k] = __float2bfloat16_rn(0.0f);
 #pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) sq[r] = (float)s;
+    for (int o = 16; o >= 1; o >>= 1) {
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+      s4 += __shfl_xor_sync(0xffffffffu, s4, o);
+    }
+    if (lane == 0) {
+      if (sq) sq[r] = (float)s2;
+      if (n4) n4[r] = (float)sqrt(s4);
     }
   }
 }
@@ -414,13 +422,14 @@ int spf_row_sqnorm_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d
 }
 
 int spf_frames_ingest_u16(const uint16_t *d_counts, int64_t n_img, int64_t n_pix, float *d_f32,
-                          void *d_bf16, float *d_sq, void *stream) {
+                          void *d_bf16, int64_t ld, float *d_sq, float *d_n4, void *stream) {
   SPF_REQUIRE(n_img >= 0 && n_pix >= 0, "spf_frames_ingest_u16: negative size");
+  SPF_REQUIRE(!d_bf16 || ld >= n_pix, "spf_frames_ingest_u16: ld < n_pix");
   if (n_img == 0 || n_pix == 0) return SPF_OK;
   SPF_REQUIRE(d_counts && d_f32, "spf_frames_ingest_u16: NULL pointer");
   int blocks = grid_for(n_img * 32, 256, (int64_t)sm_count() * 32);
   k_ingest_u16<<<blocks, 256, 0, as_stream(stream)>>>(
-      d_counts, n_img, n_pix, d_f32, reinterpret_cast<__nv_bfloat16 *>(d_bf16), d_sq);
+      d_counts, n_img, n_pix, d_f32, reinterpret_cast<__nv_bfloat16 *>(d_bf16), ld, d_sq, d_n4);
   return check_launch("spf_frames_ingest_u16");
 }
 

@@ -23,9 +23,11 @@ def row_sqnorm(x: torch.Tensor) -> torch.Tensor:
     return out
 
 
-def ingest_u16(counts: torch.Tensor, out_f32: torch.Tensor, out_bf16=None, out_sq=None):
+def ingest_u16(counts: torch.Tensor, out_f32: torch.Tensor, out_bf16=None, out_sq=None,
+               out_n4=None):
     """uint16 photon counts (held in an int16 or uint16 tensor) -> FP32 frames
-    (and optionally bf16 frames and FP32 squared norms)."""
+    (and optionally bf16 frames with a padded row stride, FP32 squared norms
+    and sqrt(sum x^4))."""
     if counts.dtype not in (torch.int16, torch.uint16):
         raise TypeError("counts must be a 16-bit integer tensor (uint16 bit pattern)")
     _lib.require_cuda(counts, "counts")
@@ -34,8 +36,9 @@ def ingest_u16(counts: torch.Tensor, out_f32: torch.Tensor, out_bf16=None, out_s
         raise ValueError("out_f32 size differs from counts")
     n_img = counts.shape[0]
     n_pix = counts.numel() // max(n_img, 1)
+    ld = out_bf16.shape[-1] if out_bf16 is not None else n_pix
     _lib.call("spf_frames_ingest_u16", _lib.ptr(counts), n_img, n_pix, _lib.ptr(out_f32),
-              _lib.ptr(out_bf16), _lib.ptr(out_sq), _lib.stream_handle())
+              _lib.ptr(out_bf16), ld, _lib.ptr(out_sq), _lib.ptr(out_n4), _lib.stream_handle())
     return out_f32
 
 
@@ -159,13 +162,32 @@ class ReferenceSet:
 class FrameSet:
     """Frames prepared for matching: FP32, bf16 (padded), norms."""
 
-    def __init__(self, f32: torch.Tensor, ld: int | None = None):
+    def __init__(self, f32: torch.Tensor, ld: int | None = None, bf16=None, sq=None, n4=None):
         _lib.require_cuda(f32, "frames", torch.float32)
         self.f32 = f32
         self.n, self.n_pix = f32.shape
         self.ld = ld or (self.n_pix + 7) // 8 * 8
-        self.bf16 = to_bf16_padded(f32, self.ld)
-        self.sq, self.n4 = row_norms(f32)
+        self.bf16 = bf16 if bf16 is not None else to_bf16_padded(f32, self.ld)
+        if sq is None or n4 is None:
+            sq, n4 = row_norms(f32)
+        self.sq, self.n4 = sq, n4
+
+    @classmethod
+    def from_counts(cls, counts: torch.Tensor, ld: int | None = None, out=None):
+        """Frames from uint16 photon counts (int16/uint16 tensor on the device);
+        `out` (a FrameSet of the same shape) is reused when given."""
+        n, p = counts.shape
+        ld = ld or (p + 7) // 8 * 8
+        if out is None:
+            dev = counts.device
+            out = cls.__new__(cls)
+            out.n, out.n_pix, out.ld = n, p, ld
+            out.f32 = torch.empty(n, p, dtype=torch.float32, device=dev)
+            out.bf16 = torch.empty(n, ld, dtype=torch.bfloat16, device=dev)
+            out.sq = torch.empty(n, dtype=torch.float32, device=dev)
+            out.n4 = torch.empty(n, dtype=torch.float32, device=dev)
+        ingest_u16(counts, out.f32, out.bf16, out.sq, out.n4)
+        return out
 
 
 class _Workspace:

@@ -1,0 +1,133 @@
+"""The merge operator and device CG against the FP64 oracle restatement and
+the reference's own Merge.solve_ac (golden, run on the FP64 NUFFT oracle).
+Tolerance: operator rel-L2 <= 1e-5 (FP32 operator); CG solution rel-L2 vs
+the FP64 reference <= 1e-3 after the same number of iterations (FP32 operator
+error amplified by the iteration)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import merge as omerge
+from tests.golden import cases
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def rel(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def setup(lib):
+    from spinifel_gb300 import Settings, geom
+    from spinifel_gb300.extern.nufft_ext import NUFFT
+
+    data, ppr, pdr, orient, ac_est = cases.merge_inputs()
+    M = cases.MERGE["M"]
+    st = Settings(det_shape=cases.MERGE["det_shape"], N_clipping=0, N_binning=0, M_override=M,
+                  solve_ac_maxiter=cases.MERGE["maxiter"], N_orientations=len(orient),
+                  N_batch_size=len(orient))
+    nufft = NUFFT(st, ppr, pdr, ref_orientations=orient)
+    H, K, L = geom.hkl(orient, ppr)
+    mult = np.pi / pdr.max()
+    return dict(data=data, ppr=ppr, pdr=pdr, orient=orient, ac_est=ac_est, M=M, st=st,
+                nufft=nufft, H=H * mult, K=K * mult, L=L * mult)
+
+
+def _operator(setup, S):
+    from spinifel_gb300.merge import MergeOperator, antisupport
+
+    M = setup["M"]
+    dev = torch.device("cuda", 0)
+    mo = omerge.MergeOracle(M, 2 * M, setup["data"].size)
+    op = MergeOperator(M, 2 * M, mo.rlambda, mo.flambda,
+                       torch.as_tensor(S, dtype=torch.float32, device=dev), antisupport(M, 1))
+    ones = np.ones(setup["H"].size)
+    from oracle import nufft as onufft
+
+    ugrid_conv = onufft.adjoint(ones, setup["H"], setup["K"], setup["L"], 2 * M, True, None)
+    op.set_kernel(torch.as_tensor(ugrid_conv, dtype=torch.float32, device=dev))
+    return op, mo, mo.kernel(setup["H"], setup["K"], setup["L"])
+
+
+def test_toeplitz_operator_matches_oracle(setup):
+    M = setup["M"]
+    S = omerge.support_from_estimate(setup["ac_est"])
+    S[0, 1, 2] = 0.0
+    op, mo, F_conv = _operator(setup, S)
+    rng = np.random.default_rng(50)
+    x = rng.standard_normal(M ** 3)
+    got = op.apply(torch.as_tensor(x, device="cuda")).cpu().numpy()
+    ref = mo.conv(x, F_conv, S) + mo.rlambda * x + mo.flambda * mo.reg(x, S)
+    assert rel(got, ref) < 1e-5
+    # the two parts separately: conv alone (flambda = 0 via the regulariser-free vector)
+    assert rel(got - mo.rlambda * x - mo.flambda * mo.reg(x, S), mo.conv(x, F_conv, S)) < 1e-4
+
+
+def test_direct_form_equals_toeplitz_for_centrosymmetric_x(setup):
+    from spinifel_gb300.nufft import NufftPlan
+
+    M = setup["M"]
+    S = np.ones((M,) * 3)
+    op, mo, _ = _operator(setup, S)
+    dev = torch.device("cuda", 0)
+    plan = NufftPlan(M, 1e-6)
+    op.set_direct(plan, torch.as_tensor(setup["orient"], device=dev),
+                  torch.as_tensor(setup["ppr"].reshape(3, -1), device=dev),
+                  float(np.pi / setup["pdr"].max()))
+    rng = np.random.default_rng(51)
+    x = rng.standard_normal((M,) * 3)
+    x = 0.5 * (x + x[::-1, ::-1, ::-1])  # centrosymmetric
+    xt = torch.as_tensor(x.reshape(-1).copy(), device=dev)
+    a = op.apply(xt, form=0).cpu().numpy()
+    b = op.apply(xt, form=1).cpu().numpy()
+    assert rel(b, a) < 1e-5
+
+
+def test_solve_ac_matches_reference_golden(setup):
+    from spinifel_gb300.sequential.autocorrelation import Merge
+
+    g = np.load(os.path.join(GOLD, "golden_merge.npz"))
+    merge = Merge(setup["st"], setup["data"], setup["ppr"], setup["pdr"], setup["nufft"])
+    ac = merge.solve_ac(0, setup["orient"], setup["ac_est"].copy())
+    assert merge.iterations == int(g["iterations"])
+    assert rel(ac, g["ac"]) < 1e-3
+    # residuals decrease overall
+    r = merge.residuals
+    assert r[-1] < r[0]
+
+
+def test_solve_ac_direct_form_close_to_toeplitz(setup):
+    from spinifel_gb300.sequential.autocorrelation import Merge
+
+    a = Merge(setup["st"], setup["data"], setup["ppr"], setup["pdr"], setup["nufft"])
+    b = Merge(setup["st"], setup["data"], setup["ppr"], setup["pdr"], setup["nufft"],
+              form="direct")
+    xa = a.solve_ac(0, setup["orient"], setup["ac_est"].copy())
+    xb = b.solve_ac(0, setup["orient"], setup["ac_est"].copy())
+    assert a.iterations == b.iterations
+    assert rel(xb, xa) < 1e-3
+
+
+def test_cg_stops_on_rtol(setup):
+    """The device CG stops by scipy's rule (||r|| < rtol ||b||) before
+    maxiter, and then the true residual is below that threshold."""
+    M = setup["M"]
+    S = np.ones((M,) * 3)
+    op, mo, _ = _operator(setup, S)
+    rng = np.random.default_rng(52)
+    xs = rng.standard_normal((M,) * 3)
+    xs = 0.5 * (xs + xs[::-1, ::-1, ::-1])
+    dev = torch.device("cuda", 0)
+    b = op.apply(torch.as_tensor(xs.reshape(-1).copy(), device=dev))
+    x, iters, hist = op.cg(b, torch.zeros_like(b), maxiter=400, rtol=0.05)
+    n = int(iters.item())
+    assert 0 < n < 400
+    h = hist.cpu().numpy()
+    assert h[n] < 0.05 * float(b.norm()) <= h[n - 1]
+    r = b - op.apply(x)
+    assert float(r.norm() / b.norm()) < 0.06
