@@ -201,20 +201,27 @@ int spf_dist_topk_bf16(const void *d_img_bf16, int64_t n_img, const void *d_ref_
                        int64_t n_ref, int64_t n_pix, int64_t ld, const float *d_ref_sq,
                        float *d_cand_d, int32_t *d_cand_i, void *stream);
 
-/* Merge the candidates of all tiles into the per-image top-8, recompute those
- * 8 distances exactly in FP32 (x2 + s2 - 2 x.s from the FP32 frames and
- * slices), return the best (d_idx, d_dist; ties to the lower index; index
- * + ref_offset) and, in d_uncertified (may be NULL), 1 where the bf16 error
- * bound cannot exclude a reference outside the 8 (the caller then runs the
- * exact path for that image).  d_img_n4 / ref_n4_max are sqrt(sum x^4) per
- * frame and its maximum over references (spf_row_norms_f32).  d_top8 (may
- * be NULL) receives the 8 candidates. */
-int spf_rerank_fp32(const float *d_cand_d, const int32_t *d_cand_i, int64_t n_tiles,
-                    const float *d_img, const float *d_img_sq, const float *d_img_n4,
-                    int64_t n_img, const float *d_ref, const float *d_ref_sq,
-                    float ref_n4_max, int64_t n_ref, int64_t n_pix, int64_t ref_offset,
-                    int32_t *d_idx, float *d_dist, int32_t *d_uncertified,
+/* Merge the candidates of all tiles into the per-frame top-8 (written over
+ * tile 0 of the candidate buffers, so each candidate set is re-ranked once),
+ * recompute those 8 distances in FP32 with exactly the arithmetic of
+ * spf_dist_argmin_f32 (acc = fma(x_p, s_p, acc) in pixel order, then
+ * (x2 + s2) - 2 acc: bit-identical values), return the best (d_idx, d_dist;
+ * ties to the lower index; index + ref_offset) and, in d_uncertified (may be
+ * NULL), 1 where the bf16 error bound cannot exclude a reference outside the
+ * 8 (the caller then runs the exact path for that frame).  d_ref_m2 is the
+ * per-pixel max over references of s^2 (spf_col_maxsq_f32), ref_sq_max the
+ * largest s2; d_work is scratch of n_img floats.  d_top8 (may be NULL)
+ * receives the 8 candidates. */
+int spf_rerank_fp32(float *d_cand_d, int32_t *d_cand_i, int64_t n_tiles,
+                    const float *d_img, const float *d_img_sq, int64_t n_img,
+                    const float *d_ref, const float *d_ref_sq, const float *d_ref_m2,
+                    float ref_sq_max, int64_t n_ref, int64_t n_pix, int64_t ref_offset,
+                    float *d_work, int32_t *d_idx, float *d_dist, int32_t *d_uncertified,
                     int32_t *d_top8, void *stream);
+
+/* d_out[p] = max over rows r of x[r, p]^2 (n_pix floats). */
+int spf_col_maxsq_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_out,
+                      void *stream);
 
 /* Row norms: d_sq[r] = sum x^2 and d_n4[r] = sqrt(sum x^4) (either may be
  * NULL), FP64 accumulation. */

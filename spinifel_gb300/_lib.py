@@ -84,9 +84,10 @@ SIGNATURES = {
     "spf_dist_topk_bf16_tiles": [_i64],
     "spf_dist_topk_bf16": [_c_void_p, _i64, _c_void_p, _i64, _i64, _i64, _c_void_p, _c_void_p,
                            _c_void_p, _c_void_p],
-    "spf_rerank_fp32": [_c_void_p, _c_void_p, _i64, _c_void_p, _c_void_p, _c_void_p, _i64,
+    "spf_rerank_fp32": [_c_void_p, _c_void_p, _i64, _c_void_p, _c_void_p, _i64, _c_void_p,
                         _c_void_p, _c_void_p, ctypes.c_float, _i64, _i64, _i64, _c_void_p,
-                        _c_void_p, _c_void_p, _c_void_p, _c_void_p],
+                        _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p],
+    "spf_col_maxsq_f32": [_c_void_p, _i64, _i64, _c_void_p, _c_void_p],
     "spf_row_norms_f32": [_c_void_p, _i64, _i64, _c_void_p, _c_void_p, _c_void_p],
     "spf_f32_to_bf16": [_c_void_p, _i64, _i64, _c_void_p, _i64, _c_void_p],
 }

@@ -10,7 +10,8 @@
 // (:158-166); only its modes -(M-1)..M-1 enter the product, so the circular
 // convolution runs on an FFT grid of any smooth size L >= 2M-1 (R2C / C2R,
 // the kernel's transform is real because ugrid_conv is real and even).  The
-// regulariser is a size-M circular operation and uses exactly M.
+// regulariser is a size-M circular operation and uses exactly M; it runs in
+// FP64 because flambda = 1e3 scales its FP32 rounding above the data term.
 //
 // CG follows scipy.sparse.linalg.cg (the solver the reference calls, :217)
 // step for step: stop when ||r|| < rtol ||b||, at most maxiter iterations.
@@ -36,13 +37,13 @@ struct spf_merge_s {
   double direct_scale = 0;
   float *support = nullptr;    // M^3
   float *kernel_hat = nullptr; // nLh
-  float *mask_hat = nullptr;   // nMh
+  double *mask_hat = nullptr;  // nMh
   float *conv_in = nullptr;    // L^3
   float2 *conv_freq = nullptr; // nLh
   float *conv_out = nullptr;   // L^3
-  float *reg_in = nullptr;     // M^3
-  float2 *reg_freq = nullptr;  // nMh
-  float *reg_out = nullptr;    // M^3
+  double *reg_in = nullptr;    // M^3 (the regulariser runs in FP64: flambda = 1e3 would
+  double2 *reg_freq = nullptr; // nMh  otherwise bury the data term in FP32 rounding)
+  double *reg_out = nullptr;   // M^3
   float *modes = nullptr;      // M^3 (direct form input / output)
   float *t1_out = nullptr;     // M^3
   double *r = nullptr, *p = nullptr, *q = nullptr;
@@ -160,7 +161,7 @@ __global__ void k_cg_stage2(const double *partial, double *scal, const int *flag
 __global__ void k_cg_update_p(double *__restrict__ p, const double *__restrict__ r,
                               const double *__restrict__ scal, const int *__restrict__ flags,
                               const float *__restrict__ S, int M, int L, float *__restrict__ conv_in,
-                              float *__restrict__ reg_in, float *__restrict__ modes) {
+                              double *__restrict__ reg_in, float *__restrict__ modes) {
   const bool done = flags[0] != 0;
   const double beta = scal[S_BETA];
   const int64_t n = (int64_t)M * M * M;
@@ -172,30 +173,32 @@ __global__ void k_cg_update_p(double *__restrict__ p, const double *__restrict__
       pv = r[i] + beta * pv;
       p[i] = pv;
     }
-    float v = (float)(pv * (double)S[i]);
+    double vd = pv * (double)S[i];
+    float v = (float)vd;
     int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
     if (conv_in) conv_in[((int64_t)a * L + b) * L + c] = v;
     if (modes) modes[i] = v;
     // ifftshift: reg_in[j] = in[(j + M/2) mod M]  <=>  in[i] lands at j = (i - M/2) mod M
     int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
-    reg_in[((int64_t)ja * M + jb) * M + jc] = v;
+    reg_in[((int64_t)ja * M + jb) * M + jc] = vd;
   }
 }
 
 // apply to a plain vector (x0 or a test vector): same as update_p without the CG update
 __global__ void k_load_input(const double *__restrict__ x, const float *__restrict__ S, int M,
-                             int L, float *__restrict__ conv_in, float *__restrict__ reg_in,
+                             int L, float *__restrict__ conv_in, double *__restrict__ reg_in,
                              float *__restrict__ modes) {
   const int64_t n = (int64_t)M * M * M;
   const int h = M / 2;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    float v = (float)(x[i] * (double)S[i]);
+    double vd = x[i] * (double)S[i];
+    float v = (float)vd;
     int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
     if (conv_in) conv_in[((int64_t)a * L + b) * L + c] = v;
     if (modes) modes[i] = v;
     int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
-    reg_in[((int64_t)ja * M + jb) * M + jc] = v;
+    reg_in[((int64_t)ja * M + jb) * M + jc] = vd;
   }
 }
 
@@ -208,13 +211,22 @@ __global__ void k_mul_real(float2 *__restrict__ z, const float *__restrict__ w, 
   }
 }
 
+__global__ void k_mul_real_d(double2 *__restrict__ z, const double *__restrict__ w, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double s = w[i];
+    double2 v = z[i];
+    z[i] = make_double2(v.x * s, v.y * s);
+  }
+}
+
 // q = S conv * cs + rlambda x + flambda S reg / M^3, and the partial p.q
 // (conv from the Toeplitz product on the L grid, or from t1_out for the
 // direct form)
 __global__ void __launch_bounds__(RED_THREADS)
     k_assemble(const double *__restrict__ x, const float *__restrict__ S, int M, int L,
                const float *__restrict__ conv_out, const float *__restrict__ t1_out,
-               double conv_scale, const float *__restrict__ reg_out, double rlambda,
+               double conv_scale, const double *__restrict__ reg_out, double rlambda,
                double flambda, double *__restrict__ q, double *__restrict__ partial) {
   const int64_t n = (int64_t)M * M * M;
   const int h = M / 2;
@@ -286,7 +298,7 @@ __global__ void k_real_part(const float2 *__restrict__ z, float *__restrict__ ou
 }
 
 // mask_hat[m] = F_anti[(m + M/2) mod M] on the R2C half spectrum
-__global__ void k_mask_half(const float *__restrict__ F, int M, float *__restrict__ out) {
+__global__ void k_mask_half(const float *__restrict__ F, int M, double *__restrict__ out) {
   const int Mh = M / 2 + 1;
   const int64_t n = (int64_t)M * M * Mh;
   const int h = M / 2;
@@ -329,12 +341,14 @@ static int apply_operator_core(spf_merge_s *G, bool direct, cudaStream_t s) {
                                            G->coord_scale, G->weights, s));
     SPF_TRY(spf_nufft_t1_finish(G->nufft, +1, G->t1_out, nullptr, s));
   }
-  SPF_TRY(cufft_ok(cufftExecR2C(G->r2c_M, G->reg_in, reinterpret_cast<cufftComplex *>(G->reg_freq)),
-                   "reg R2C"));
-  k_mul_real<<<grid1(G->nMh), 256, 0, s>>>(G->reg_freq, G->mask_hat, G->nMh);
-  SPF_TRY(check_launch("k_mul_real"));
-  return cufft_ok(cufftExecC2R(G->c2r_M, reinterpret_cast<cufftComplex *>(G->reg_freq), G->reg_out),
-                  "reg C2R");
+  SPF_TRY(cufft_ok(cufftExecD2Z(G->r2c_M, G->reg_in,
+                                reinterpret_cast<cufftDoubleComplex *>(G->reg_freq)),
+                   "reg D2Z"));
+  k_mul_real_d<<<grid1(G->nMh), 256, 0, s>>>(G->reg_freq, G->mask_hat, G->nMh);
+  SPF_TRY(check_launch("k_mul_real_d"));
+  return cufft_ok(cufftExecZ2D(G->c2r_M, reinterpret_cast<cufftDoubleComplex *>(G->reg_freq),
+                               G->reg_out),
+                  "reg Z2D");
 }
 
 }  // namespace cg
@@ -371,13 +385,13 @@ int spf_merge_create(int M, int M_ups, double rlambda, double flambda, const flo
   };
   alloc((void **)&G->support, G->n * sizeof(float));
   alloc((void **)&G->kernel_hat, G->nLh * sizeof(float));
-  alloc((void **)&G->mask_hat, G->nMh * sizeof(float));
+  alloc((void **)&G->mask_hat, G->nMh * sizeof(double));
   alloc((void **)&G->conv_in, G->nL * sizeof(float));
   alloc((void **)&G->conv_freq, G->nLh * sizeof(float2));
   alloc((void **)&G->conv_out, G->nL * sizeof(float));
-  alloc((void **)&G->reg_in, G->n * sizeof(float));
-  alloc((void **)&G->reg_freq, G->nMh * sizeof(float2));
-  alloc((void **)&G->reg_out, G->n * sizeof(float));
+  alloc((void **)&G->reg_in, G->n * sizeof(double));
+  alloc((void **)&G->reg_freq, G->nMh * sizeof(double2));
+  alloc((void **)&G->reg_out, G->n * sizeof(double));
   alloc((void **)&G->modes, G->n * sizeof(float));
   alloc((void **)&G->t1_out, G->n * sizeof(float));
   alloc((void **)&G->r, G->n * sizeof(double));
@@ -389,8 +403,8 @@ int spf_merge_create(int M, int M_ups, double rlambda, double flambda, const flo
   if (st == SPF_OK) {
     bool ok = cufftPlan3d(&G->r2c_L, G->L, G->L, G->L, CUFFT_R2C) == CUFFT_SUCCESS &&
               cufftPlan3d(&G->c2r_L, G->L, G->L, G->L, CUFFT_C2R) == CUFFT_SUCCESS &&
-              cufftPlan3d(&G->r2c_M, M, M, M, CUFFT_R2C) == CUFFT_SUCCESS &&
-              cufftPlan3d(&G->c2r_M, M, M, M, CUFFT_C2R) == CUFFT_SUCCESS;
+              cufftPlan3d(&G->r2c_M, M, M, M, CUFFT_D2Z) == CUFFT_SUCCESS &&
+              cufftPlan3d(&G->c2r_M, M, M, M, CUFFT_Z2D) == CUFFT_SUCCESS;
     G->plans_ok = ok;
     if (!ok) {
       set_error("spf_merge_create: cufftPlan3d failed (L = %d, M = %d)", G->L, M);

@@ -18,13 +18,14 @@
 // the kernel records SPF_ERR_TIMEOUT in the device error word, stops issuing,
 // drains its copies and frees TMEM before returning.
 //
-// The re-rank kernel merges the candidates of all reference tiles into the
-// per-image top-8, recomputes those 8 distances exactly in FP32 from the FP32
-// frames and slices, and certifies the result: the argmin over all
-// references is the re-ranked one when the 8th-best approximate distance
-// exceeds the re-ranked best by more than twice the bf16 error bound
-// (6 sigma of the rounding error, sigma <= 2^-9 sqrt(2/3) ||x||_4^2 max||s||_4^2).
-// Uncertified images are flagged for an exact pass over all references.
+// The re-rank merges the candidates of all reference tiles into the per-frame
+// top-8, recomputes those 8 distances in FP32 with exactly the plain path's
+// arithmetic (so the values are bit-identical to it), and certifies the
+// result: no reference outside the 8 can beat the re-ranked best when the
+// 8th-best approximate distance exceeds it by more than the bf16 rounding
+// error (10 sigma, sigma = 2 (u/sqrt 3) sqrt(sum_p x_p^2 max_r s_rp^2),
+// u = 2^-8) plus the FP32 accumulation error of both paths.  Uncertified
+// frames are flagged for an exact pass over all references.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -374,31 +375,32 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
-// merge + exact FP32 re-rank, one CTA (256 threads) per image
+// merge + exact FP32 re-rank
 // ---------------------------------------------------------------------------
 constexpr int RR_THREADS = 256;
+constexpr float U_BF16 = 1.0f / 256.0f;    // unit roundoff of bf16 (8 significant bits)
+constexpr float U_FP32 = 5.9604645e-8f;    // 2^-24
+constexpr float CERT_SIGMAS = 10.0f;
 
 __device__ __forceinline__ bool lex_less(float a, int32_t ia, float b, int32_t ib) {
   return a < b || (a == b && ia < ib);
 }
 
+// Block per frame: the 8 smallest candidates over all reference tiles (by
+// distance, then index), written over cand[tile 0][frame]; and the frame's
+// bf16 error variance term V = sum_p x_p^2 max_r s_rp^2 (negated when some
+// x_p is not exact in bf16) into work[frame].
 __global__ void __launch_bounds__(RR_THREADS)
-    k_rerank(const float *__restrict__ cand_d, const int32_t *__restrict__ cand_i, int64_t n_tiles,
-             const float *__restrict__ img, const float *__restrict__ img_sq,
-             const float *__restrict__ img_n4, int64_t n_img, const float *__restrict__ ref,
-             const float *__restrict__ ref_sq, float ref_n4_max, int64_t n_pix,
-             int64_t ref_offset, int32_t *__restrict__ out_idx, float *__restrict__ out_dist,
-             int32_t *__restrict__ uncertified, int32_t *__restrict__ out_top) {
+    k_merge_top8(float *__restrict__ cand_d, int32_t *__restrict__ cand_i, int64_t n_tiles,
+                 const float *__restrict__ img, int64_t n_img, const float *__restrict__ m2,
+                 int64_t n_pix, float *__restrict__ work) {
   __shared__ float s_d[RR_THREADS / 32][TOPK];
   __shared__ int32_t s_i[RR_THREADS / 32][TOPK];
-  __shared__ float s_top_d[TOPK];
-  __shared__ int32_t s_top_i[TOPK];
-  __shared__ float s_dot[RR_THREADS / 32][TOPK];
+  __shared__ float s_v[RR_THREADS / 32];
+  __shared__ int s_x[RR_THREADS / 32];
   const int64_t im = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (im >= n_img) return;
-
-  // 1. the 8 smallest candidates over all reference tiles, by (d, index)
   float d[TOPK];
   int32_t ix[TOPK];
 #pragma unroll
@@ -426,7 +428,16 @@ __global__ void __launch_bounds__(RR_THREADS)
       ix[q] = ti;
     }
   }
-  // warp merge: 8 rounds of a lexicographic warp minimum over list heads
+  // frame error term (coalesced pass over the frame)
+  float V = 0.0f;
+  int inexact = 0;
+  const float *x = img + im * n_pix;
+  for (int64_t p = tid; p < n_pix; p += RR_THREADS) {
+    float xv = x[p];
+    V = fmaf(xv * xv, __ldg(m2 + p), V);
+    inexact |= (__bfloat162float(__float2bfloat16_rn(xv)) != xv);
+  }
+  // warp merge of the per-thread lists: 8 rounds of a lexicographic minimum
   int head = 0;
   for (int r = 0; r < TOPK; ++r) {
     float hv = head < TOPK ? d[head] : __int_as_float(0x7f800000);
@@ -448,9 +459,17 @@ __global__ void __launch_bounds__(RR_THREADS)
       s_i[warp][r] = bi;
     }
   }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    V += __shfl_xor_sync(0xffffffffu, V, o);
+    inexact |= __shfl_xor_sync(0xffffffffu, inexact, o);
+  }
+  if (lane == 0) {
+    s_v[warp] = V;
+    s_x[warp] = inexact;
+  }
   __syncthreads();
   if (warp == 0) {
-    // lanes hold 2 of the 64 warp-level entries each
     float a0 = s_d[lane >> 3][lane & 7], a1 = s_d[4 + (lane >> 3)][lane & 7];
     int32_t j0 = s_i[lane >> 3][lane & 7], j1 = s_i[4 + (lane >> 3)][lane & 7];
     if (lex_less(a1, j1, a0, j0)) {
@@ -474,69 +493,109 @@ __global__ void __launch_bounds__(RR_THREADS)
       }
       if (h < 2 && hv == bv && hi == bi) ++h;
       if (lane == 0) {
-        s_top_d[r] = bv;
-        s_top_i[r] = bi;
+        size_t off = (size_t)im * TOPK + r;  // tile 0's slot of this frame
+        cand_d[off] = bv;
+        cand_i[off] = bi;
       }
     }
+    if (lane == 0) {
+      float vt = 0.0f;
+      int ex = 0;
+      for (int w = 0; w < RR_THREADS / 32; ++w) {
+        vt += s_v[w];
+        ex |= s_x[w];
+      }
+      work[im] = ex ? -vt : vt;
+    }
   }
-  __syncthreads();
+}
 
-  // 2. exact FP32 distances of the 8 candidates
-  int32_t cj[TOPK];
-  bool cv[TOPK];
-#pragma unroll
-  for (int k = 0; k < TOPK; ++k) {
-    cj[k] = s_top_i[k];
-    cv[k] = cj[k] != INT32_MAX;
-  }
-  float acc[TOPK];
-#pragma unroll
-  for (int k = 0; k < TOPK; ++k) acc[k] = 0.0f;
-  const float *x = img + im * n_pix;
-  for (int64_t p = tid; p < n_pix; p += RR_THREADS) {
-    float xv = x[p];
-#pragma unroll
-    for (int k = 0; k < TOPK; ++k)
-      if (cv[k]) acc[k] = fmaf(xv, __ldg(ref + (int64_t)cj[k] * n_pix + p), acc[k]);
-  }
-#pragma unroll
-  for (int k = 0; k < TOPK; ++k) {
-    float v = acc[k];
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) s_dot[warp][k] = v;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    float x2 = img_sq[im];
-    float best = __int_as_float(0x7f800000);
-    int32_t bj = INT32_MAX;
-    for (int k = 0; k < TOPK; ++k) {
-      if (!cv[k]) continue;
-      float dot = 0.0f;
-      for (int w = 0; w < RR_THREADS / 32; ++w) dot += s_dot[w][k];
-      float dist = (x2 + ref_sq[cj[k]]) - 2.0f * dot;
-      if (lex_less(dist, cj[k], best, bj)) {
-        best = dist;
-        bj = cj[k];
+// 8 lanes per frame, one candidate each: the exact FP32 distance computed
+// with the arithmetic of the plain kernel (k_dist_argmin_f32): acc =
+// fma(x_p, s_p, acc) for p = 0 .. n_pix-1 in order, then (x2 + s2) - 2 acc,
+// so the re-ranked values are bit-identical to the plain path's.  Lane 0 of
+// the group keeps the lexicographic minimum and evaluates the certificate.
+__global__ void __launch_bounds__(RR_THREADS)
+    k_rerank_exact(const float *__restrict__ cand_d, const int32_t *__restrict__ cand_i,
+                   const float *__restrict__ img, const float *__restrict__ img_sq,
+                   int64_t n_img, const float *__restrict__ ref, const float *__restrict__ ref_sq,
+                   float ref_sq_max, int64_t n_pix, int64_t ref_offset,
+                   const float *__restrict__ work, int32_t *__restrict__ out_idx,
+                   float *__restrict__ out_dist, int32_t *__restrict__ uncertified,
+                   int32_t *__restrict__ out_top) {
+  const int64_t gt = blockIdx.x * (int64_t)RR_THREADS + threadIdx.x;
+  const int64_t im = gt / TOPK;
+  const int c = (int)(gt % TOPK);
+  const bool live = im < n_img;
+  const int64_t imc = live ? im : 0;
+  int32_t j = cand_i[(size_t)imc * TOPK + c];
+  const bool valid = live && j != INT32_MAX;
+  float acc = 0.0f;
+  if (valid) {
+    const float *x = img + imc * n_pix;
+    const float *sr = ref + (int64_t)j * n_pix;
+    int64_t p = 0;
+    if ((n_pix & 3) == 0 && aligned(x, 16) && aligned(sr, 16)) {
+      for (; p < n_pix; p += 4) {
+        float4 a = *reinterpret_cast<const float4 *>(x + p);
+        float4 b = __ldg(reinterpret_cast<const float4 *>(sr + p));
+        acc = fmaf(a.x, b.x, acc);
+        acc = fmaf(a.y, b.y, acc);
+        acc = fmaf(a.z, b.z, acc);
+        acc = fmaf(a.w, b.w, acc);
       }
     }
-    out_idx[im] = bj == INT32_MAX ? -1 : (int32_t)(bj + ref_offset);
-    if (out_dist) out_dist[im] = best;
-    if (out_top)
-      for (int k = 0; k < TOPK; ++k)
-        out_top[im * TOPK + k] = cv[k] ? (int32_t)(cj[k] + ref_offset) : -1;
-    // certificate: no reference outside the 8 can beat the re-ranked best
-    int ncand = 0;
-    for (int k = 0; k < TOPK; ++k) ncand += cv[k];
-    int cert = 1;
-    if (ncand == TOPK) {
-      const float u = 1.0f / 512.0f;  // bf16 unit roundoff
-      float sigma = u * 0.8164966f * img_n4[im] * ref_n4_max;
-      float margin = (x2 + s_top_d[TOPK - 1]) - 12.0f * sigma - best;
-      cert = margin > 1e-6f * fabsf(best) ? 1 : 0;
+    for (; p < n_pix; ++p) acc = fmaf(x[p], __ldg(sr + p), acc);
+  }
+  float x2 = live ? img_sq[imc] : 0.0f;
+  float dist = valid ? __fsub_rn(__fadd_rn(x2, ref_sq[j]), __fmul_rn(2.0f, acc))
+                     : __int_as_float(0x7f800000);
+  int32_t jj = valid ? j : INT32_MAX;
+  // lexicographic minimum over the 8 lanes of this frame
+#pragma unroll
+  for (int o = 4; o >= 1; o >>= 1) {
+    float od = __shfl_xor_sync(0xffffffffu, dist, o, TOPK);
+    int32_t oj = __shfl_xor_sync(0xffffffffu, jj, o, TOPK);
+    if (lex_less(od, oj, dist, jj)) {
+      dist = od;
+      jj = oj;
     }
-    if (uncertified) uncertified[im] = cert ? 0 : 1;
+  }
+  if (!live) return;
+  if (out_top) out_top[im * TOPK + c] = (j == INT32_MAX) ? -1 : (int32_t)(j + ref_offset);
+  if (c != 0) return;
+  out_idx[im] = jj == INT32_MAX ? -1 : (int32_t)(jj + ref_offset);
+  if (out_dist) out_dist[im] = dist;
+  if (!uncertified) return;
+  // certificate: every reference outside the 8 has approximate distance
+  // >= d8 (+ x2), and its plain-path distance differs from that by at most
+  // the bf16 rounding error (CERT_SIGMAS sigma, per-pixel bound) plus the
+  // FP32 accumulation error of both paths; the re-ranked best must lie below
+  int32_t j7 = cand_i[(size_t)im * TOPK + TOPK - 1];
+  int cert = 1;
+  if (j7 != INT32_MAX) {
+    float d8 = cand_d[(size_t)im * TOPK + TOPK - 1] + x2;
+    float V = work[im];
+    float vs = V < 0.0f ? -2.0f * V : V;  // x rounding doubles the variance term
+    float sig16 = 2.0f * U_BF16 * 0.57735027f * sqrtf(vs);
+    float sig32 = U_FP32 * sqrtf((float)n_pix) * (x2 + ref_sq_max);
+    float margin = d8 - CERT_SIGMAS * (sig16 + 2.0f * sig32) - dist;
+    cert = margin > 0.0f ? 1 : 0;
+  }
+  uncertified[im] = cert ? 0 : 1;
+}
+
+// column maxima of squares: out[p] = max_r x[r, p]^2
+__global__ void k_col_maxsq(const float *__restrict__ x, int64_t n_rows, int64_t n_pix,
+                            float *__restrict__ out) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n_pix;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    float m = 0.0f;
+    for (int64_t r = 0; r < n_rows; ++r) {
+      float v = x[r * n_pix + p];
+      m = fmaxf(m, v * v);
+    }
+    out[p] = m;
   }
 }
 
@@ -659,22 +718,39 @@ int spf_dist_topk_bf16(const void *d_img_bf16, int64_t n_img, const void *d_ref_
   return check_launch("k_dist_topk_bf16");
 }
 
-int spf_rerank_fp32(const float *d_cand_d, const int32_t *d_cand_i, int64_t n_tiles,
-                    const float *d_img, const float *d_img_sq, const float *d_img_n4,
-                    int64_t n_img, const float *d_ref, const float *d_ref_sq, float ref_n4_max,
-                    int64_t n_ref, int64_t n_pix, int64_t ref_offset, int32_t *d_idx,
-                    float *d_dist, int32_t *d_uncertified, int32_t *d_top8, void *stream) {
+int spf_rerank_fp32(float *d_cand_d, int32_t *d_cand_i, int64_t n_tiles, const float *d_img,
+                    const float *d_img_sq, int64_t n_img, const float *d_ref,
+                    const float *d_ref_sq, const float *d_ref_m2, float ref_sq_max,
+                    int64_t n_ref, int64_t n_pix, int64_t ref_offset, float *d_work,
+                    int32_t *d_idx, float *d_dist, int32_t *d_uncertified, int32_t *d_top8,
+                    void *stream) {
   SPF_REQUIRE(n_img >= 0 && n_ref >= 0 && n_pix >= 0 && n_tiles >= 0,
               "spf_rerank_fp32: negative size");
   if (n_img == 0) return SPF_OK;
-  SPF_REQUIRE(d_cand_d && d_cand_i && d_img && d_img_sq && d_img_n4 && d_ref && d_ref_sq && d_idx,
+  SPF_REQUIRE(d_cand_d && d_cand_i && d_img && d_img_sq && d_ref && d_ref_sq && d_ref_m2 &&
+                  d_work && d_idx,
               "spf_rerank_fp32: NULL pointer");
   SPF_REQUIRE(n_tiles == (n_ref + BN - 1) / BN, "spf_rerank_fp32: n_tiles does not match n_ref");
-  SPF_REQUIRE(n_img < (1LL << 31), "spf_rerank_fp32: too many images");
-  k_rerank<<<(unsigned)n_img, RR_THREADS, 0, as_stream(stream)>>>(
-      d_cand_d, d_cand_i, n_tiles, d_img, d_img_sq, d_img_n4, n_img, d_ref, d_ref_sq, ref_n4_max,
-      n_pix, ref_offset, d_idx, d_dist, d_uncertified, d_top8);
-  return check_launch("k_rerank");
+  SPF_REQUIRE(n_img < (1LL << 28), "spf_rerank_fp32: too many images");
+  cudaStream_t s = as_stream(stream);
+  k_merge_top8<<<(unsigned)n_img, RR_THREADS, 0, s>>>(d_cand_d, d_cand_i, n_tiles, d_img, n_img,
+                                                      d_ref_m2, n_pix, d_work);
+  SPF_TRY(check_launch("k_merge_top8"));
+  int64_t threads = n_img * TOPK;
+  k_rerank_exact<<<(unsigned)((threads + RR_THREADS - 1) / RR_THREADS), RR_THREADS, 0, s>>>(
+      d_cand_d, d_cand_i, d_img, d_img_sq, n_img, d_ref, d_ref_sq, ref_sq_max, n_pix, ref_offset,
+      d_work, d_idx, d_dist, d_uncertified, d_top8);
+  return check_launch("k_rerank_exact");
+}
+
+int spf_col_maxsq_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_out,
+                      void *stream) {
+  SPF_REQUIRE(n_rows >= 0 && n_pix >= 0, "spf_col_maxsq_f32: negative size");
+  if (n_pix == 0) return SPF_OK;
+  SPF_REQUIRE(d_x && d_out, "spf_col_maxsq_f32: NULL pointer");
+  k_col_maxsq<<<grid_for(n_pix, 256, 4096), 256, 0, as_stream(stream)>>>(d_x, n_rows, n_pix,
+                                                                          d_out);
+  return check_launch("spf_col_maxsq_f32");
 }
 
 int spf_row_norms_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_sq, float *d_n4,

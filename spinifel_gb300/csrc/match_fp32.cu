@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(TB_THREADS) k_dist_argmin_f32(
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       if (rr[j] < n_ref) {
-        float dist = (x2 + s2[j]) - 2.0f * acc[i][j];
+        float dist = __fsub_rn(__fadd_rn(x2, s2[j]), __fmul_rn(2.0f, acc[i][j]));
         unsigned long long k2 =
             ((unsigned long long)float_key(dist) << 32) | (unsigned long long)(rr[j] + ref_offset);
         key = k2 < key ? k2 : key;

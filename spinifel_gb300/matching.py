@@ -136,7 +136,8 @@ def check_device_error():
 class ReferenceSet:
     """Reference slices resident in HBM: FP32 rows (exact re-rank and the plain
     path), a bf16 copy for the tensor cores (row stride padded to 8), squared
-    norms and the largest sqrt(sum s^4) (for the re-rank certificate)."""
+    norms, and for the re-rank certificate the per-pixel max of s^2 and the
+    largest squared norm."""
 
     def __init__(self, refs_f32: torch.Tensor, refs_bf16: torch.Tensor | None = None):
         _lib.require_cuda(refs_f32, "refs_f32", torch.float32)
@@ -148,15 +149,20 @@ class ReferenceSet:
         if tuple(refs_bf16.shape) != (self.n_ref, self.ld):
             raise ValueError("bf16 copy must be [n_ref, ld]")
         self.bf16 = refs_bf16
-        self.sq, n4 = row_norms(refs_f32)
-        self.n4_max = float(n4.max().item()) if self.n_ref else 0.0
+        self._stats()
+
+    def _stats(self):
+        self.sq = row_sqnorm(self.f32)
+        self.m2 = torch.empty(self.n_pix, dtype=torch.float32, device=self.f32.device)
+        _lib.call("spf_col_maxsq_f32", _lib.ptr(self.f32), self.n_ref, self.n_pix,
+                  _lib.ptr(self.m2), _lib.stream_handle())
+        self.sq_max = float(self.sq.max().item()) if self.n_ref else 0.0
 
     def rescale(self, factor: float):
-        """Multiply every slice by factor (FP32, bf16 and norms kept consistent)."""
+        """Multiply every slice by factor (FP32, bf16 and statistics kept consistent)."""
         self.f32 *= factor
         self.bf16.copy_(to_bf16_padded(self.f32, self.ld))
-        self.sq, n4 = row_norms(self.f32)
-        self.n4_max = float(n4.max().item()) if self.n_ref else 0.0
+        self._stats()
 
 
 class FrameSet:
@@ -208,8 +214,8 @@ _ws = _Workspace()
 def match_bf16(frames: FrameSet, refs: ReferenceSet, exact_fallback: bool = True,
                stats: dict | None = None, stream=None):
     """Best reference per frame: bf16 tensor-core distances, per-frame top-8,
-    exact FP32 re-rank; frames the certificate cannot settle are re-matched
-    exactly over all references (plain FP32 path)."""
+    exact FP32 re-rank (bit-identical to the plain path's values); frames the
+    certificate cannot settle are re-matched exactly over all references."""
     if frames.n_pix != refs.n_pix or frames.ld != refs.ld:
         raise ValueError("frames and references differ in pixel count")
     dev = frames.f32.device
@@ -217,6 +223,7 @@ def match_bf16(frames: FrameSet, refs: ReferenceSet, exact_fallback: bool = True
     tiles = int(_lib.lib().spf_dist_topk_bf16_tiles(refs.n_ref))
     cand_d = _ws.get("cand_d", tiles * n_img * 8, torch.float32, dev)
     cand_i = _ws.get("cand_i", tiles * n_img * 8, torch.int32, dev)
+    work = _ws.get("rerank_work", n_img, torch.float32, dev)
     idx = torch.empty(n_img, dtype=torch.int32, device=dev)
     dist = torch.empty(n_img, dtype=torch.float32, device=dev)
     unc = torch.empty(n_img, dtype=torch.int32, device=dev)
@@ -224,9 +231,9 @@ def match_bf16(frames: FrameSet, refs: ReferenceSet, exact_fallback: bool = True
     _lib.call("spf_dist_topk_bf16", _lib.ptr(frames.bf16), n_img, _lib.ptr(refs.bf16), refs.n_ref,
               refs.n_pix, refs.ld, _lib.ptr(refs.sq), _lib.ptr(cand_d), _lib.ptr(cand_i), sh)
     _lib.call("spf_rerank_fp32", _lib.ptr(cand_d), _lib.ptr(cand_i), tiles, _lib.ptr(frames.f32),
-              _lib.ptr(frames.sq), _lib.ptr(frames.n4), n_img, _lib.ptr(refs.f32),
-              _lib.ptr(refs.sq), float(refs.n4_max), refs.n_ref, refs.n_pix, 0, _lib.ptr(idx),
-              _lib.ptr(dist), _lib.ptr(unc), None, sh)
+              _lib.ptr(frames.sq), n_img, _lib.ptr(refs.f32), _lib.ptr(refs.sq),
+              _lib.ptr(refs.m2), float(refs.sq_max), refs.n_ref, refs.n_pix, 0, _lib.ptr(work),
+              _lib.ptr(idx), _lib.ptr(dist), _lib.ptr(unc), None, sh)
     if exact_fallback or stats is not None:
         bad = torch.nonzero(unc, as_tuple=False).flatten()
         nbad = int(bad.numel())
