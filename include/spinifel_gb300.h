@@ -210,7 +210,8 @@ int spf_dist_topk_bf16(const void *d_img_bf16, int64_t n_img, const void *d_ref_
  * NULL), 1 where the bf16 error bound cannot exclude a reference outside the
  * 8 (the caller then runs the exact path for that frame).  d_ref_m2 is the
  * per-pixel max over references of s^2 (spf_col_maxsq_f32), ref_sq_max the
- * largest s2; d_work is scratch of n_img floats.  d_top8 (may be NULL)
+ * largest s2; d_work (n_img floats) is scratch that on return holds each
+ * frame's search bound for spf_dist_range_bf16.  d_top8 (may be NULL)
  * receives the 8 candidates. */
 int spf_rerank_fp32(float *d_cand_d, int32_t *d_cand_i, int64_t n_tiles,
                     const float *d_img, const float *d_img_sq, int64_t n_img,
@@ -218,6 +219,23 @@ int spf_rerank_fp32(float *d_cand_d, int32_t *d_cand_i, int64_t n_tiles,
                     float ref_sq_max, int64_t n_ref, int64_t n_pix, int64_t ref_offset,
                     float *d_work, int32_t *d_idx, float *d_dist, int32_t *d_uncertified,
                     int32_t *d_top8, void *stream);
+
+/* Certified completion for frames the top-8 certificate left open: after
+ * spf_rerank_fp32, d_work[i] holds the frame's search bound T_i (re-ranked
+ * best minus x2 plus the error band).  spf_dist_range_bf16 runs the same
+ * tensor-core GEMM and appends every reference r with s2_r - 2 x.s_r <= T_i
+ * to d_list[i*cap ..] (d_count[i] = number found, zeroed by the call; a count
+ * above cap means the list overflowed); spf_rerank_list_fp32 computes the
+ * listed distances with the plain path's arithmetic and folds the
+ * lexicographic minimum into d_best (the spf_best_* format). */
+int spf_dist_range_bf16(const void *d_img_bf16, int64_t n_img, const void *d_ref_bf16,
+                        int64_t n_ref, int64_t n_pix, int64_t ld, const float *d_ref_sq,
+                        const float *d_thresh, int32_t *d_list, int32_t *d_count, int cap,
+                        void *stream);
+int spf_rerank_list_fp32(const int32_t *d_list, const int32_t *d_count, int cap,
+                         const float *d_img, const float *d_img_sq, int64_t n_img,
+                         const float *d_ref, const float *d_ref_sq, int64_t n_pix,
+                         int64_t ref_offset, uint64_t *d_best, void *stream);
 
 /* d_out[p] = max over rows r of x[r, p]^2 (n_pix floats). */
 int spf_col_maxsq_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_out,

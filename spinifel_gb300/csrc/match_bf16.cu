@@ -202,11 +202,18 @@ __device__ __forceinline__ void tile_of(int64_t t, int64_t n_m, int64_t n_n, int
   n = r / gm;
 }
 
+// RANGE = false: per-tile top-8 into cand_d / cand_i.
+// RANGE = true : every reference with s2 - 2 acc <= thresh[row] is appended to
+//                list[row * cap ..] (count[row] holds the number found, which
+//                may exceed cap: the caller then treats the row as overflowed).
+template <bool RANGE>
 __global__ void __launch_bounds__(THREADS, 1)
     k_dist_topk_bf16(const __grid_constant__ CUtensorMap tmap_a,
                      const __grid_constant__ CUtensorMap tmap_b, const float *__restrict__ ref_sq,
                      int64_t n_img, int64_t n_ref, int64_t n_pix, float *__restrict__ cand_d,
-                     int32_t *__restrict__ cand_i, unsigned int *__restrict__ err) {
+                     int32_t *__restrict__ cand_i, const float *__restrict__ thresh,
+                     int32_t *__restrict__ list, int32_t *__restrict__ count, int cap,
+                     unsigned int *__restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -335,31 +342,53 @@ __global__ void __launch_bounds__(THREADS, 1)
       tc_fence_after();
       const int64_t row = m * BM + q * 32 + lane;
       const int64_t col0 = n * BN;
-      TopK top;
-      top.clear();
+      if constexpr (RANGE) {
+        const float thr = row < n_img ? thresh[row] : -__int_as_float(0x7f800000);
 #pragma unroll 1
-      for (int c = 0; c < BN / 32; ++c) {
-        uint32_t r[32];
-        tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + b * BN + c * 32, r);
+        for (int c = 0; c < BN / 32; ++c) {
+          uint32_t r[32];
+          tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + b * BN + c * 32, r);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          int64_t col = col0 + c * 32 + j;
-          if (col < n_ref) {
-            float v = __ldg(ref_sq + col) - 2.0f * __uint_as_float(r[j]);
-            top.push(v, (int32_t)col);
+          for (int j = 0; j < 32; ++j) {
+            int64_t col = col0 + c * 32 + j;
+            if (col < n_ref) {
+              float v = __ldg(ref_sq + col) - 2.0f * __uint_as_float(r[j]);
+              if (v <= thr) {
+                int pos = atomicAdd(count + row, 1);
+                if (pos < cap) list[row * cap + pos] = (int32_t)col;
+              }
+            }
           }
         }
-      }
-      tc_fence_before();
-      mbar_arrive(&acc_empty[b]);
-      if (row < n_img) {
-        size_t base = ((size_t)n * n_img + row) * TOPK;
-        float4 *pd = reinterpret_cast<float4 *>(cand_d + base);
-        int4 *pi = reinterpret_cast<int4 *>(cand_i + base);
-        pd[0] = make_float4(top.d[0], top.d[1], top.d[2], top.d[3]);
-        pd[1] = make_float4(top.d[4], top.d[5], top.d[6], top.d[7]);
-        pi[0] = make_int4(top.i[0], top.i[1], top.i[2], top.i[3]);
-        pi[1] = make_int4(top.i[4], top.i[5], top.i[6], top.i[7]);
+        tc_fence_before();
+        mbar_arrive(&acc_empty[b]);
+      } else {
+        TopK top;
+        top.clear();
+#pragma unroll 1
+        for (int c = 0; c < BN / 32; ++c) {
+          uint32_t r[32];
+          tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + b * BN + c * 32, r);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            int64_t col = col0 + c * 32 + j;
+            if (col < n_ref) {
+              float v = __ldg(ref_sq + col) - 2.0f * __uint_as_float(r[j]);
+              top.push(v, (int32_t)col);
+            }
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(&acc_empty[b]);
+        if (row < n_img) {
+          size_t base = ((size_t)n * n_img + row) * TOPK;
+          float4 *pd = reinterpret_cast<float4 *>(cand_d + base);
+          int4 *pi = reinterpret_cast<int4 *>(cand_i + base);
+          pd[0] = make_float4(top.d[0], top.d[1], top.d[2], top.d[3]);
+          pd[1] = make_float4(top.d[4], top.d[5], top.d[6], top.d[7]);
+          pi[0] = make_int4(top.i[0], top.i[1], top.i[2], top.i[3]);
+          pi[1] = make_int4(top.i[4], top.i[5], top.i[6], top.i[7]);
+        }
       }
     }
   }
@@ -520,7 +549,7 @@ __global__ void __launch_bounds__(RR_THREADS)
                    const float *__restrict__ img, const float *__restrict__ img_sq,
                    int64_t n_img, const float *__restrict__ ref, const float *__restrict__ ref_sq,
                    float ref_sq_max, int64_t n_pix, int64_t ref_offset,
-                   const float *__restrict__ work, int32_t *__restrict__ out_idx,
+                   float *__restrict__ work, int32_t *__restrict__ out_idx,
                    float *__restrict__ out_dist, int32_t *__restrict__ uncertified,
                    int32_t *__restrict__ out_top) {
   const int64_t gt = blockIdx.x * (int64_t)RR_THREADS + threadIdx.x;
@@ -573,16 +602,56 @@ __global__ void __launch_bounds__(RR_THREADS)
   // FP32 accumulation error of both paths; the re-ranked best must lie below
   int32_t j7 = cand_i[(size_t)im * TOPK + TOPK - 1];
   int cert = 1;
+  float V = work[im];
+  float vs = V < 0.0f ? -2.0f * V : V;  // x rounding doubles the variance term
+  float sig16 = 2.0f * U_BF16 * 0.57735027f * sqrtf(vs);
+  float sig32 = U_FP32 * sqrtf((float)n_pix) * (x2 + ref_sq_max);
+  float band = CERT_SIGMAS * (sig16 + 2.0f * sig32);
   if (j7 != INT32_MAX) {
     float d8 = cand_d[(size_t)im * TOPK + TOPK - 1] + x2;
-    float V = work[im];
-    float vs = V < 0.0f ? -2.0f * V : V;  // x rounding doubles the variance term
-    float sig16 = 2.0f * U_BF16 * 0.57735027f * sqrtf(vs);
-    float sig32 = U_FP32 * sqrtf((float)n_pix) * (x2 + ref_sq_max);
-    float margin = d8 - CERT_SIGMAS * (sig16 + 2.0f * sig32) - dist;
-    cert = margin > 0.0f ? 1 : 0;
+    cert = (d8 - band - dist) > 0.0f ? 1 : 0;
   }
   uncertified[im] = cert ? 0 : 1;
+  // the range that must be searched when the frame is not certified: every
+  // reference whose approximate distance (without x2) lies within the band
+  // of the re-ranked best
+  work[im] = (dist - x2) + band;
+}
+
+// Exact FP32 distances (plain-path arithmetic) for every listed candidate of
+// every frame; the per-frame lexicographic minimum is folded into best[]
+// (packed order key << 32 | index, as spf_dist_argmin_f32 keeps it).
+__global__ void __launch_bounds__(RR_THREADS)
+    k_rerank_list(const int32_t *__restrict__ list, const int32_t *__restrict__ count, int cap,
+                  const float *__restrict__ img, const float *__restrict__ img_sq, int64_t n_img,
+                  const float *__restrict__ ref, const float *__restrict__ ref_sq, int64_t n_pix,
+                  int64_t ref_offset, unsigned long long *__restrict__ best) {
+  const int64_t gt = blockIdx.x * (int64_t)RR_THREADS + threadIdx.x;
+  const int64_t im = gt / cap;
+  const int c = (int)(gt % cap);
+  if (im >= n_img) return;
+  int cnt = count[im];
+  if (c >= cnt || c >= cap) return;
+  int32_t j = list[im * cap + c];
+  const float *x = img + im * n_pix;
+  const float *sr = ref + (int64_t)j * n_pix;
+  float acc = 0.0f;
+  int64_t p = 0;
+  if ((n_pix & 3) == 0 && aligned(x, 16) && aligned(sr, 16)) {
+    for (; p < n_pix; p += 4) {
+      float4 a = *reinterpret_cast<const float4 *>(x + p);
+      float4 b = __ldg(reinterpret_cast<const float4 *>(sr + p));
+      acc = fmaf(a.x, b.x, acc);
+      acc = fmaf(a.y, b.y, acc);
+      acc = fmaf(a.z, b.z, acc);
+      acc = fmaf(a.w, b.w, acc);
+    }
+  }
+  for (; p < n_pix; ++p) acc = fmaf(x[p], __ldg(sr + p), acc);
+  float dist = __fsub_rn(__fadd_rn(img_sq[im], ref_sq[j]), __fmul_rn(2.0f, acc));
+  unsigned long long key =
+      ((unsigned long long)float_key(dist) << 32) | (unsigned long long)(j + ref_offset);
+  atomicMin(best + im, key);
 }
 
 // column maxima of squares: out[p] = max_r x[r, p]^2
@@ -674,48 +743,98 @@ extern "C" {
 
 int64_t spf_dist_topk_bf16_tiles(int64_t n_ref) { return (n_ref + BN - 1) / BN; }
 
-int spf_dist_topk_bf16(const void *d_img_bf16, int64_t n_img, const void *d_ref_bf16,
+static int launch_bf16(bool range, const void *d_img_bf16, int64_t n_img, const void *d_ref_bf16,
                        int64_t n_ref, int64_t n_pix, int64_t ld, const float *d_ref_sq,
-                       float *d_cand_d, int32_t *d_cand_i, void *stream) {
-  SPF_REQUIRE(n_img >= 0 && n_ref >= 0 && n_pix >= 0, "spf_dist_topk_bf16: negative size");
+                       float *d_cand_d, int32_t *d_cand_i, const float *d_thresh,
+                       int32_t *d_list, int32_t *d_count, int cap, void *stream,
+                       const char *name) {
+  SPF_REQUIRE(n_img >= 0 && n_ref >= 0 && n_pix >= 0, "%s: negative size", name);
   if (n_img == 0 || n_ref == 0) return SPF_OK;
-  SPF_REQUIRE(d_img_bf16 && d_ref_bf16 && d_ref_sq && d_cand_d && d_cand_i,
-              "spf_dist_topk_bf16: NULL pointer");
+  SPF_REQUIRE(d_img_bf16 && d_ref_bf16 && d_ref_sq, "%s: NULL pointer", name);
   SPF_REQUIRE(ld >= n_pix && ld % 8 == 0,
-              "spf_dist_topk_bf16: row stride ld must be >= n_pix and a multiple of 8");
+              "%s: row stride ld must be >= n_pix and a multiple of 8", name);
   SPF_REQUIRE(aligned(d_img_bf16, 16) && aligned(d_ref_bf16, 16),
-              "spf_dist_topk_bf16: operands must be 16-byte aligned");
-  SPF_REQUIRE(aligned(d_cand_d, 16) && aligned(d_cand_i, 16),
-              "spf_dist_topk_bf16: candidate buffers must be 16-byte aligned");
+              "%s: operands must be 16-byte aligned", name);
   SPF_REQUIRE(n_img < (1LL << 31) && n_ref < (1LL << 31) && ld < (1LL << 31),
-              "spf_dist_topk_bf16: size too large");
+              "%s: size too large", name);
   int dev = 0;
   cudaGetDevice(&dev);
   int major = 0, minor = 0;
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
   cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
   if (major != 10 || minor != 3) {
-    set_error("spf_dist_topk_bf16: needs sm_103 (GB300), device is sm_%d%d", major, minor);
+    set_error("%s: needs sm_103 (GB300), device is sm_%d%d", name, major, minor);
     return SPF_ERR_UNSUPPORTED;
   }
   CUtensorMap ma, mb;
   SPF_TRY(make_map(&ma, d_img_bf16, n_img, ld, BM));
   SPF_TRY(make_map(&mb, d_ref_bf16, n_ref, ld, BN));
-  static bool attr_set[64] = {false};
-  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-    SPF_TRY(check_cuda(cudaFuncSetAttribute(k_dist_topk_bf16,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            SMEM_BYTES),
-                       "spf_dist_topk_bf16"));
-    attr_set[dev] = true;
+  static bool attr_set[2][64] = {{false}};
+  if (dev >= 0 && dev < 64 && !attr_set[range][dev]) {
+    cudaError_t e = range ? cudaFuncSetAttribute(k_dist_topk_bf16<true>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 SMEM_BYTES)
+                          : cudaFuncSetAttribute(k_dist_topk_bf16<false>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 SMEM_BYTES);
+    SPF_TRY(check_cuda(e, name));
+    attr_set[range][dev] = true;
   }
   unsigned int *err = device_error_word();
-  SPF_REQUIRE(err != nullptr, "spf_dist_topk_bf16: no device error word");
+  SPF_REQUIRE(err != nullptr, "%s: no device error word", name);
   int64_t tiles = ((n_img + BM - 1) / BM) * ((n_ref + BN - 1) / BN);
   int grid = (int)(tiles < sm_count() ? tiles : sm_count());
-  k_dist_topk_bf16<<<grid, THREADS, SMEM_BYTES, as_stream(stream)>>>(
-      ma, mb, d_ref_sq, n_img, n_ref, n_pix, d_cand_d, d_cand_i, err);
-  return check_launch("k_dist_topk_bf16");
+  if (range)
+    k_dist_topk_bf16<true><<<grid, THREADS, SMEM_BYTES, as_stream(stream)>>>(
+        ma, mb, d_ref_sq, n_img, n_ref, n_pix, nullptr, nullptr, d_thresh, d_list, d_count, cap,
+        err);
+  else
+    k_dist_topk_bf16<false><<<grid, THREADS, SMEM_BYTES, as_stream(stream)>>>(
+        ma, mb, d_ref_sq, n_img, n_ref, n_pix, d_cand_d, d_cand_i, nullptr, nullptr, nullptr, 0,
+        err);
+  return check_launch(name);
+}
+
+int spf_dist_topk_bf16(const void *d_img_bf16, int64_t n_img, const void *d_ref_bf16,
+                       int64_t n_ref, int64_t n_pix, int64_t ld, const float *d_ref_sq,
+                       float *d_cand_d, int32_t *d_cand_i, void *stream) {
+  SPF_REQUIRE(n_img == 0 || n_ref == 0 || (d_cand_d && d_cand_i),
+              "spf_dist_topk_bf16: NULL candidate buffer");
+  SPF_REQUIRE(aligned(d_cand_d, 16) && aligned(d_cand_i, 16),
+              "spf_dist_topk_bf16: candidate buffers must be 16-byte aligned");
+  return launch_bf16(false, d_img_bf16, n_img, d_ref_bf16, n_ref, n_pix, ld, d_ref_sq, d_cand_d,
+                     d_cand_i, nullptr, nullptr, nullptr, 0, stream, "spf_dist_topk_bf16");
+}
+
+int spf_dist_range_bf16(const void *d_img_bf16, int64_t n_img, const void *d_ref_bf16,
+                        int64_t n_ref, int64_t n_pix, int64_t ld, const float *d_ref_sq,
+                        const float *d_thresh, int32_t *d_list, int32_t *d_count, int cap,
+                        void *stream) {
+  SPF_REQUIRE(cap >= 1 && cap <= 4096, "spf_dist_range_bf16: cap must be in [1, 4096]");
+  SPF_REQUIRE(n_img == 0 || n_ref == 0 || (d_thresh && d_list && d_count),
+              "spf_dist_range_bf16: NULL pointer");
+  if (n_img > 0)
+    SPF_TRY(check_cuda(cudaMemsetAsync(d_count, 0, n_img * sizeof(int32_t), as_stream(stream)),
+                       "spf_dist_range_bf16"));
+  return launch_bf16(true, d_img_bf16, n_img, d_ref_bf16, n_ref, n_pix, ld, d_ref_sq, nullptr,
+                     nullptr, d_thresh, d_list, d_count, cap, stream, "spf_dist_range_bf16");
+}
+
+int spf_rerank_list_fp32(const int32_t *d_list, const int32_t *d_count, int cap,
+                         const float *d_img, const float *d_img_sq, int64_t n_img,
+                         const float *d_ref, const float *d_ref_sq, int64_t n_pix,
+                         int64_t ref_offset, uint64_t *d_best, void *stream) {
+  SPF_REQUIRE(n_img >= 0 && n_pix >= 0 && cap >= 1, "spf_rerank_list_fp32: bad size");
+  if (n_img == 0) return SPF_OK;
+  SPF_REQUIRE(d_list && d_count && d_img && d_img_sq && d_ref && d_ref_sq && d_best,
+              "spf_rerank_list_fp32: NULL pointer");
+  int64_t threads = n_img * (int64_t)cap;
+  SPF_REQUIRE(threads / RR_THREADS < (1LL << 31), "spf_rerank_list_fp32: too large");
+  k_rerank_list<<<(unsigned)((threads + RR_THREADS - 1) / RR_THREADS), RR_THREADS, 0,
+                  as_stream(stream)>>>(d_list, d_count, cap, d_img, d_img_sq, n_img, d_ref,
+                                       d_ref_sq, n_pix, ref_offset,
+                                       reinterpret_cast<unsigned long long *>(d_best));
+  return check_launch("k_rerank_list");
 }
 
 int spf_rerank_fp32(float *d_cand_d, int32_t *d_cand_i, int64_t n_tiles, const float *d_img,

@@ -240,10 +240,47 @@ def match_bf16(frames: FrameSet, refs: ReferenceSet, exact_fallback: bool = True
         if stats is not None:
             stats["uncertified"] = nbad
         if exact_fallback and nbad:
-            sub = frames.f32.index_select(0, bad).contiguous()
-            tr = BestTracker(nbad, dev)
-            tr.update_fp32(sub, frames.sq.index_select(0, bad).contiguous(), refs.f32, refs.sq, 0)
-            i2, d2 = tr.result()
+            i2, d2 = _complete_range(frames, refs, bad, work.index_select(0, bad).contiguous(),
+                                     stats, sh)
             idx.index_copy_(0, bad, i2)
             dist.index_copy_(0, bad, d2)
     return idx, dist
+
+
+RANGE_CAP = 64
+
+
+def _complete_range(frames: FrameSet, refs: ReferenceSet, rows: torch.Tensor,
+                    thresh: torch.Tensor, stats, sh):
+    """Exact answer for frames the top-8 certificate left open: collect every
+    reference inside the frame's error band with the tensor-core GEMM, re-rank
+    that list with the plain path's arithmetic; a list that overflows falls
+    back to the plain FP32 pass over all references."""
+    dev = frames.f32.device
+    n = int(rows.numel())
+    bf = frames.bf16.index_select(0, rows).contiguous()
+    f32 = frames.f32.index_select(0, rows).contiguous()
+    sq = frames.sq.index_select(0, rows).contiguous()
+    lst = _ws.get("range_list", n * RANGE_CAP, torch.int32, dev)
+    cnt = _ws.get("range_count", n, torch.int32, dev)
+    _lib.call("spf_dist_range_bf16", _lib.ptr(bf), n, _lib.ptr(refs.bf16), refs.n_ref, refs.n_pix,
+              refs.ld, _lib.ptr(refs.sq), _lib.ptr(thresh), _lib.ptr(lst), _lib.ptr(cnt),
+              RANGE_CAP, sh)
+    tr = BestTracker(n, dev)
+    _lib.call("spf_rerank_list_fp32", _lib.ptr(lst), _lib.ptr(cnt), RANGE_CAP, _lib.ptr(f32),
+              _lib.ptr(sq), n, _lib.ptr(refs.f32), _lib.ptr(refs.sq), refs.n_pix, 0,
+              _lib.ptr(tr.best), sh)
+    i2, d2 = tr.result()
+    over = torch.nonzero(cnt > RANGE_CAP, as_tuple=False).flatten()
+    n_over = int(over.numel())
+    if stats is not None:
+        stats["range_overflow"] = n_over
+        stats["range_max_list"] = int(cnt.max().item()) if n else 0
+    if n_over:
+        t2 = BestTracker(n_over, dev)
+        t2.update_fp32(f32.index_select(0, over).contiguous(), sq.index_select(0, over).contiguous(),
+                       refs.f32, refs.sq, 0)
+        i3, d3 = t2.result()
+        i2.index_copy_(0, over, i3)
+        d2.index_copy_(0, over, d3)
+    return i2, d2

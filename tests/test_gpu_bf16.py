@@ -103,3 +103,40 @@ def test_bf16_poisson_frames_certify(dev):
     oidx, od = om.sklearn_argmin(refs, imgs)
     assert np.all(om.ties_equal(idx.cpu().numpy(), oidx, od))
     assert st["uncertified"] < n_img // 2
+
+
+def test_range_completion_when_gaps_are_tiny(dev):
+    """References in clusters of near-duplicates: the top-8 certificate cannot
+    separate them, the range query + list re-rank must still give exactly the
+    plain FP32 argmin."""
+    from spinifel_gb300 import matching
+
+    rng = np.random.default_rng(43)
+    base = rng.gamma(0.5, 1.0, (60, 2048)).astype(np.float32)
+    refs = np.repeat(base, 12, axis=0) * (1 + 1e-4 * rng.standard_normal((720, 2048))).astype(
+        np.float32)
+    refs = refs.astype(np.float32)
+    pick = rng.integers(0, 720, 300)
+    imgs = rng.poisson(refs[pick]).astype(np.float32)
+    x = torch.as_tensor(imgs, device=dev)
+    s = torch.as_tensor(refs, device=dev)
+    fr, rs = matching.FrameSet(x), matching.ReferenceSet(s)
+    st = {}
+    idx, dist = matching.match_bf16(fr, rs, stats=st)
+    pidx, pdist = matching.argmin_fp32(x, s)
+    assert st["uncertified"] > 0
+    assert torch.equal(idx, pidx)
+    assert torch.equal(dist, pdist)  # bit-identical distances
+
+
+def test_rerank_distances_bit_identical_to_plain(dev):
+    from spinifel_gb300 import matching
+
+    rng = np.random.default_rng(44)
+    refs = rng.random((700, 1000)).astype(np.float32)
+    imgs = (refs[rng.integers(0, 700, 200)] + 0.2 * rng.random((200, 1000))).astype(np.float32)
+    x = torch.as_tensor(imgs, device=dev)
+    s = torch.as_tensor(refs, device=dev)
+    idx, dist = matching.match_bf16(matching.FrameSet(x), matching.ReferenceSet(s))
+    pidx, pdist = matching.argmin_fp32(x, s)
+    assert torch.equal(idx, pidx) and torch.equal(dist, pdist)
