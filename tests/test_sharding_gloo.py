@@ -72,7 +72,7 @@ def test_reference_sharded_argmin_equals_single_rank(world):
     refs[30] = refs[3]  # duplicate across shards: the lower index must win
     frames = torch.as_tensor(rng.random((11, 16)))
     frames[0] = refs[3]
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()
     out = mgr.dict()
     mp.start_processes(_worker, args=(world, _free_port(), refs, frames, out), nprocs=world,
                        join=True, start_method="spawn")
