@@ -237,6 +237,29 @@ int spf_rerank_list_fp32(const int32_t *d_list, const int32_t *d_count, int cap,
                          const float *d_ref, const float *d_ref_sq, int64_t n_pix,
                          int64_t ref_offset, uint64_t *d_best, void *stream);
 
+/* Matching for callers that cannot allocate device memory: code that records
+ * its work inside a CUDA stream capture (an allocation breaks the capture)
+ * and online data-acquisition processes that fix their GPU memory at start-up.
+ * No counterpart in the reference.  Same result as spf_dist_topk_bf16 +
+ * spf_rerank_fp32 (best index, exact FP32 distance, uncertified flags; the
+ * caller completes uncertified frames), but all scratch lives in a static
+ * device array of the library: 16 MiB + 64 KiB held by every GPU that loads
+ * the library until the process exits.  Limits per call: n_img <=
+ * SPF_STATIC_MAX_FRAMES and ceil(n_ref/256) * n_img <=
+ * SPF_STATIC_MAX_TILE_FRAMES; larger calls are rejected with SPF_ERR_ARG.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) and sets the kernel's shared-memory limit; make it
+ * before any stream capture.  It calls no cudaMalloc or cudaFree.  All calls
+ * on a device share the array: calls that overlap on the GPU race, so
+ * serialise them. */
+#define SPF_STATIC_MAX_FRAMES 4096
+#define SPF_STATIC_MAX_TILE_FRAMES 262144
+int spf_match_bf16_static(const void *d_img_bf16, const float *d_img, const float *d_img_sq,
+                          int64_t n_img, const void *d_ref_bf16, const float *d_ref,
+                          const float *d_ref_sq, const float *d_ref_m2, float ref_sq_max,
+                          int64_t n_ref, int64_t n_pix, int64_t ld, int32_t *d_idx,
+                          float *d_dist, int32_t *d_uncertified, void *stream);
+
 /* d_out[p] = max over rows r of x[r, p]^2 (n_pix floats). */
 int spf_col_maxsq_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_out,
                       void *stream);

@@ -90,6 +90,9 @@ SIGNATURES = {
     "spf_col_maxsq_f32": [_c_void_p, _i64, _i64, _c_void_p, _c_void_p],
     "spf_dist_range_bf16": [_c_void_p, _i64, _c_void_p, _i64, _i64, _i64, _c_void_p, _c_void_p,
                             _c_void_p, _c_void_p, _int, _c_void_p],
+    "spf_match_bf16_static": [_c_void_p, _c_void_p, _c_void_p, _i64, _c_void_p, _c_void_p,
+                              _c_void_p, _c_void_p, ctypes.c_float, _i64, _i64, _i64, _c_void_p,
+                              _c_void_p, _c_void_p, _c_void_p],
     "spf_rerank_list_fp32": [_c_void_p, _c_void_p, _int, _c_void_p, _c_void_p, _i64, _c_void_p,
                              _c_void_p, _i64, _i64, _c_void_p, _c_void_p],
     "spf_row_norms_f32": [_c_void_p, _i64, _i64, _c_void_p, _c_void_p, _c_void_p],

@@ -29,6 +29,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <mutex>
+
 #include "common.cuh"
 
 namespace spf {
@@ -883,3 +885,128 @@ int spf_row_norms_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Matching without device allocation.
+//
+// Some callers cannot call cudaMalloc: code that records its work inside a
+// CUDA stream capture (an allocation there breaks the capture), and online
+// data-acquisition processes that fix their GPU memory when they start and
+// must not allocate while frames stream in.  spf_match_bf16_static gives them
+// the bf16 tensor-core top-8 + exact FP32 re-rank with its scratch (the
+// candidate buffer, the re-rank work area and the device error word) in the
+// file-scope array below instead of caller- or library-allocated memory.
+// The array is part of this library's device image: every GPU that loads the
+// library holds it (16 MiB + 64 KiB) until the process exits.  All calls on a
+// device share it and it keeps the last call's contents, so calls that overlap
+// on the GPU (different streams, or different host threads) race; serialise
+// them.  Every byte a call reads is written earlier in the same call except
+// the error word, which the call clears first.
+// ---------------------------------------------------------------------------
+namespace spf {
+namespace bf16mm {
+
+constexpr int64_t STATIC_MAX_TILE_FRAMES = SPF_STATIC_MAX_TILE_FRAMES;  // tiles(n_ref) * n_img
+constexpr int64_t STATIC_MAX_FRAMES = SPF_STATIC_MAX_FRAMES;
+constexpr size_t STATIC_CAND_BYTES = (size_t)STATIC_MAX_TILE_FRAMES * TOPK * 4;
+constexpr size_t STATIC_WORK_BYTES = (size_t)STATIC_MAX_FRAMES * 4;
+constexpr size_t STATIC_SCRATCH_BYTES = 2 * STATIC_CAND_BYTES + STATIC_WORK_BYTES + 256;
+
+static __device__ __align__(256) unsigned char g_match_scratch[STATIC_SCRATCH_BYTES];
+
+// Device address of g_match_scratch per device, looked up once with the
+// device current (host code cannot use the symbol itself as an address).
+static std::mutex g_static_mu;
+static unsigned char *g_static_ptr[64] = {nullptr};
+static bool g_static_attr[64] = {false};
+
+static int static_scratch(int dev, unsigned char **out) {
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_ptr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_match_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      set_error("spf_match_bf16_static: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return SPF_ERR_CUDA;
+    }
+    g_static_ptr[dev] = static_cast<unsigned char *>(p);
+  }
+  if (!g_static_attr[dev]) {
+    SPF_TRY(check_cuda(cudaFuncSetAttribute(k_dist_topk_bf16<false>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            SMEM_BYTES),
+                       "spf_match_bf16_static"));
+    g_static_attr[dev] = true;
+  }
+  *out = g_static_ptr[dev];
+  return SPF_OK;
+}
+
+}  // namespace bf16mm
+}  // namespace spf
+
+extern "C" int spf_match_bf16_static(const void *d_img_bf16, const float *d_img,
+                                     const float *d_img_sq, int64_t n_img,
+                                     const void *d_ref_bf16, const float *d_ref,
+                                     const float *d_ref_sq, const float *d_ref_m2,
+                                     float ref_sq_max, int64_t n_ref, int64_t n_pix, int64_t ld,
+                                     int32_t *d_idx, float *d_dist, int32_t *d_uncertified,
+                                     void *stream) {
+  using namespace spf;
+  using namespace spf::bf16mm;
+  const char *name = "spf_match_bf16_static";
+  SPF_REQUIRE(n_img >= 0 && n_ref >= 0 && n_pix >= 0, "%s: negative size", name);
+  if (n_img == 0) return SPF_OK;
+  SPF_REQUIRE(n_ref > 0, "%s: no references", name);
+  const int64_t tiles = (n_ref + BN - 1) / BN;
+  SPF_REQUIRE(n_img <= STATIC_MAX_FRAMES,
+              "%s: %lld frames exceed the static scratch limit of %lld frames per call", name,
+              (long long)n_img, (long long)STATIC_MAX_FRAMES);
+  SPF_REQUIRE(tiles * n_img <= STATIC_MAX_TILE_FRAMES,
+              "%s: ceil(n_ref/256) * n_img = %lld exceeds the static scratch limit of %lld "
+              "(split the references or the frames)",
+              name, (long long)(tiles * n_img), (long long)STATIC_MAX_TILE_FRAMES);
+  SPF_REQUIRE(d_img_bf16 && d_img && d_img_sq && d_ref_bf16 && d_ref && d_ref_sq && d_ref_m2 &&
+                  d_idx,
+              "%s: NULL pointer", name);
+  SPF_REQUIRE(ld >= n_pix && ld % 8 == 0, "%s: ld must be >= n_pix and a multiple of 8", name);
+  SPF_REQUIRE(aligned(d_img_bf16, 16) && aligned(d_ref_bf16, 16),
+              "%s: bf16 operands must be 16-byte aligned", name);
+  SPF_REQUIRE(n_ref < (1LL << 31) && ld < (1LL << 31), "%s: size too large", name);
+  int dev = 0;
+  SPF_TRY(check_cuda(cudaGetDevice(&dev), name));
+  SPF_REQUIRE(dev >= 0 && dev < 64, "%s: device index out of range", name);
+  int major = 0, minor = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  if (major != 10 || minor != 3) {
+    set_error("%s: needs sm_103 (GB300), device is sm_%d%d", name, major, minor);
+    return SPF_ERR_UNSUPPORTED;
+  }
+  unsigned char *base = nullptr;
+  SPF_TRY(static_scratch(dev, &base));
+  float *cand_d = reinterpret_cast<float *>(base);
+  int32_t *cand_i = reinterpret_cast<int32_t *>(base + STATIC_CAND_BYTES);
+  float *work = reinterpret_cast<float *>(base + 2 * STATIC_CAND_BYTES);
+  unsigned int *err =
+      reinterpret_cast<unsigned int *>(base + 2 * STATIC_CAND_BYTES + STATIC_WORK_BYTES);
+  cudaStream_t s = as_stream(stream);
+  SPF_TRY(check_cuda(cudaMemsetAsync(err, 0, sizeof(unsigned int), s), name));
+  CUtensorMap ma, mb;
+  SPF_TRY(make_map(&ma, d_img_bf16, n_img, ld, BM));
+  SPF_TRY(make_map(&mb, d_ref_bf16, n_ref, ld, BN));
+  int64_t gemm_tiles = ((n_img + BM - 1) / BM) * tiles;
+  int grid = (int)(gemm_tiles < sm_count() ? gemm_tiles : sm_count());
+  k_dist_topk_bf16<false><<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, d_ref_sq, n_img, n_ref,
+                                                            n_pix, cand_d, cand_i, nullptr,
+                                                            nullptr, nullptr, 0, err);
+  SPF_TRY(check_launch("k_dist_topk_bf16 (static scratch)"));
+  k_merge_top8<<<(unsigned)n_img, RR_THREADS, 0, s>>>(cand_d, cand_i, tiles, d_img, n_img,
+                                                      d_ref_m2, n_pix, work);
+  SPF_TRY(check_launch("k_merge_top8 (static scratch)"));
+  int64_t threads = n_img * TOPK;
+  k_rerank_exact<<<(unsigned)((threads + RR_THREADS - 1) / RR_THREADS), RR_THREADS, 0, s>>>(
+      cand_d, cand_i, d_img, d_img_sq, n_img, d_ref, d_ref_sq, ref_sq_max, n_pix, 0, work, d_idx,
+      d_dist, d_uncertified, nullptr);
+  return check_launch("k_rerank_exact (static scratch)");
+}

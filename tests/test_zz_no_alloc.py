@@ -1,0 +1,93 @@
+"""spf_match_bf16_static: matching for callers that cannot allocate device
+memory (work recorded inside a CUDA stream capture, or a data-acquisition
+process whose GPU memory is fixed at start-up).  Called through the C ABI, it
+must give exactly what the allocating entry points (spf_dist_topk_bf16 +
+spf_rerank_fp32) give, on two calls in a row with different frames, without
+taking device memory after its first call, and must reject sizes beyond its
+static scratch.  This file is collected last on purpose."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _allocating(lib_mod, fr, rs):
+    L = lib_mod
+    tiles = int(L.lib().spf_dist_topk_bf16_tiles(rs.n_ref))
+    dev = fr.f32.device
+    cd = torch.empty(tiles * fr.n * 8, dtype=torch.float32, device=dev)
+    ci = torch.empty(tiles * fr.n * 8, dtype=torch.int32, device=dev)
+    work = torch.empty(fr.n, dtype=torch.float32, device=dev)
+    idx = torch.empty(fr.n, dtype=torch.int32, device=dev)
+    dist = torch.empty(fr.n, dtype=torch.float32, device=dev)
+    unc = torch.empty(fr.n, dtype=torch.int32, device=dev)
+    sh = L.stream_handle()
+    L.call("spf_dist_topk_bf16", L.ptr(fr.bf16), fr.n, L.ptr(rs.bf16), rs.n_ref, rs.n_pix, rs.ld,
+           L.ptr(rs.sq), L.ptr(cd), L.ptr(ci), sh)
+    L.call("spf_rerank_fp32", L.ptr(cd), L.ptr(ci), tiles, L.ptr(fr.f32), L.ptr(fr.sq), fr.n,
+           L.ptr(rs.f32), L.ptr(rs.sq), L.ptr(rs.m2), float(rs.sq_max), rs.n_ref, rs.n_pix, 0,
+           L.ptr(work), L.ptr(idx), L.ptr(dist), L.ptr(unc), None, sh)
+    torch.cuda.synchronize()
+    return idx, dist, unc
+
+
+def _static(lib_mod, fr, rs, idx, dist, unc):
+    L = lib_mod
+    L.call("spf_match_bf16_static", L.ptr(fr.bf16), L.ptr(fr.f32), L.ptr(fr.sq), fr.n,
+           L.ptr(rs.bf16), L.ptr(rs.f32), L.ptr(rs.sq), L.ptr(rs.m2), float(rs.sq_max), rs.n_ref,
+           rs.n_pix, rs.ld, L.ptr(idx), L.ptr(dist), L.ptr(unc), L.stream_handle())
+    torch.cuda.synchronize()
+
+
+def test_static_scratch_entry_point_matches_allocating_path(lib):
+    from spinifel_gb300 import _lib, matching
+
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(90)
+    n_ref, n_pix = 3000, 2048
+    refs = rng.gamma(0.5, 1.0, (n_ref, n_pix)).astype(np.float32)
+    rs = matching.ReferenceSet(torch.as_tensor(refs, device=dev))
+    frames = []
+    for n in (300, 77):  # two calls in a row, different frames and sizes
+        pick = rng.integers(0, n_ref, n)
+        x = torch.as_tensor(rng.poisson(refs[pick]).astype(np.float32), device=dev)
+        frames.append(matching.FrameSet(x))
+    outs = [(torch.empty(f.n, dtype=torch.int32, device=dev),
+             torch.empty(f.n, dtype=torch.float32, device=dev),
+             torch.empty(f.n, dtype=torch.int32, device=dev)) for f in frames]
+    torch.cuda.synchronize()
+    free_before = None
+    for k, (fr, out) in enumerate(zip(frames, outs)):
+        _static(_lib, fr, rs, *out)
+        if k == 0:
+            free_before = torch.cuda.mem_get_info(dev)[0]
+    free_after = torch.cuda.mem_get_info(dev)[0]
+    assert free_after == free_before  # no device memory taken by the second call
+    for fr, (idx, dist, unc) in zip(frames, outs):
+        ridx, rdist, runc = _allocating(_lib, fr, rs)
+        assert torch.equal(idx, ridx)
+        assert torch.equal(dist, rdist)
+        assert torch.equal(unc, runc)
+
+
+def test_static_scratch_entry_point_rejects_oversize(lib):
+    from spinifel_gb300 import _lib
+
+    L = _lib.lib()
+    # 4097 frames: more than the scratch holds; rejected before any device work
+    st = L.spf_match_bf16_static(ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16),
+                                 4097, ctypes.c_void_p(16), ctypes.c_void_p(16),
+                                 ctypes.c_void_p(16), ctypes.c_void_p(16), 1.0, 1000, 64, 64,
+                                 ctypes.c_void_p(16), None, None, None)
+    assert st == _lib.SPF_ERR_ARG
+    assert b"static scratch limit" in L.spf_last_error()
+    # 2000 frames x 200,000 references: 782 tiles * 2000 > 262,144
+    st = L.spf_match_bf16_static(ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16),
+                                 2000, ctypes.c_void_p(16), ctypes.c_void_p(16),
+                                 ctypes.c_void_p(16), ctypes.c_void_p(16), 1.0, 200_000, 64, 64,
+                                 ctypes.c_void_p(16), None, None, None)
+    assert st == _lib.SPF_ERR_ARG
+    assert b"static scratch limit" in L.spf_last_error()
