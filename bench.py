@@ -203,6 +203,7 @@ def main():
     ppr, pdr = geom.flat_detector(W["panels"], W["nx"], W["ny"])
     mult = float(np.pi / pdr.max())
     ppr_t = torch.as_tensor(ppr.reshape(3, -1), dtype=torch.float32, device=dev)
+    det = (W["panels"], W["nx"], W["ny"])
     ref_q = torch.as_tensor(geom.uniform_quaternions(W["n_ref"], rng), dtype=torch.float32,
                             device=dev)
     img_rng = np.random.default_rng(W["seed"] + 1 + rank)
@@ -219,7 +220,7 @@ def main():
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for st in range(0, W["n_ref"], B):
-        plan.slice(ref_q[st:st + B], ppr_t, mult, out=refs[st:st + B])
+        plan.slice(ref_q[st:st + B], ppr_t, mult, out=refs[st:st + B], det_shape=det)
     e1.record()
     barrier()
     slice_ms = e0.elapsed_time(e1)
@@ -227,7 +228,7 @@ def main():
     # --- frames: Poisson counts of slices at other orientations -------------
     imgs_f = torch.empty(W["n_img"], n_pix, dtype=torch.float32, device=dev)
     for st in range(0, W["n_img"], B):
-        plan.slice(img_q[st:st + B], ppr_t, mult, out=imgs_f[st:st + B])
+        plan.slice(img_q[st:st + B], ppr_t, mult, out=imgs_f[st:st + B], det_shape=det)
     lam = imgs_f.clamp_min_(0)
     lam *= W["photons"] / lam.mean()
     gen = torch.Generator(device=dev)
@@ -257,11 +258,13 @@ def main():
     l0 = _lib.launch_count()
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
+        torch.cuda.nvtx.range_push("timed")
         t0.record()
         for _ in range(args.steps):
             idx_bf, _ = step_bf16(frames)
         t1.record()
         barrier()
+        torch.cuda.nvtx.range_pop()
     launches = (_lib.launch_count() - l0) // max(args.steps, 1) * args.steps
     ms = t0.elapsed_time(t1) / args.steps
     ms_t = torch.tensor([ms], device=dev)

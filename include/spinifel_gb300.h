@@ -84,6 +84,13 @@ int spf_slice_t2(spf_nufft_plan plan, const float *d_quats, int64_t n_orient,
                  const float *d_ppr, int64_t n_pix, double scale, float *d_out,
                  void *d_out_bf16, void *stream);
 
+/* spf_slice_t2 for a detector of n_panels x nx x ny pixels (d_ppr is
+ * 3 x n_panels x nx x ny, C order): 16 x 16 pixel patches are sliced from a
+ * shared-memory copy of their grid footprint.  Same values as spf_slice_t2. */
+int spf_slice_t2_det(spf_nufft_plan plan, const float *d_quats, int64_t n_orient,
+                     const float *d_ppr, int n_panels, int nx, int ny, double scale,
+                     float *d_out, void *d_out_bf16, void *stream);
+
 /* Type 1: zero the plan's fine grid, spread real strengths, then FFT and
  * deconvolve onto the (m1, m2, m3) modes.  isign as in the caller
  * (+1 in spinifel/autocorrelation.py:118, -1 in nufft_ext.py:316).

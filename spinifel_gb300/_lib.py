@@ -53,6 +53,8 @@ SIGNATURES = {
                             _c_void_p, _c_void_p],
     "spf_slice_t2": [_c_void_p, _c_void_p, _i64, _c_void_p, _i64, _dbl, _c_void_p, _c_void_p,
                      _c_void_p],
+    "spf_slice_t2_det": [_c_void_p, _c_void_p, _i64, _c_void_p, _int, _int, _int, _dbl, _c_void_p,
+                         _c_void_p, _c_void_p],
     "spf_nufft_t1_zero": [_c_void_p, _c_void_p],
     "spf_nufft_t1_spread": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _i64,
                             _c_void_p],

@@ -296,6 +296,109 @@ __global__ void k_slice_t2(const float *__restrict__ re_pad, GridGeom g,
   if (out_bf16) out_bf16[idx] = __float2bfloat16_rn(v);
 }
 
+// Slicing on a multi-panel detector [n_panels][nx][ny]: a CTA of 256 threads
+// takes a 16 x 16 pixel patch of one panel at one orientation, so its points
+// are neighbours on the Ewald sphere.  It finds the bounding box of their
+// kernel footprints in the padded fine grid, stages that box in shared memory
+// (coalesced along the fastest axis) and interpolates from there; a box too
+// large for shared memory (a patch seen edge-on) reads the grid directly.
+// The arithmetic per point is that of k_slice_t2, so the values are identical.
+constexpr int SLICE_PATCH = 16;
+constexpr int SLICE_SMEM_FLOATS = 11264;  // 44 KB
+
+template <int W>
+__global__ void __launch_bounds__(256)
+    k_slice_t2_det(const float *__restrict__ re_pad, GridGeom g, const float *__restrict__ quats,
+                   const float *__restrict__ ppr, int n_panels, int nx, int ny, float scale1,
+                   float scale2, float scale3, float *__restrict__ out,
+                   __nv_bfloat16 *__restrict__ out_bf16) {
+  __shared__ float box[SLICE_SMEM_FLOATS];
+  __shared__ int bb[6];
+  const int64_t o = blockIdx.x;
+  const int patches_y = (ny + SLICE_PATCH - 1) / SLICE_PATCH;
+  const int patches_x = (nx + SLICE_PATCH - 1) / SLICE_PATCH;
+  const int pid = blockIdx.y;
+  const int panel = pid / (patches_x * patches_y);
+  const int rem = pid % (patches_x * patches_y);
+  const int px = (rem / patches_y) * SLICE_PATCH + (int)(threadIdx.x / SLICE_PATCH);
+  const int py = (rem % patches_y) * SLICE_PATCH + (int)(threadIdx.x % SLICE_PATCH);
+  const bool valid = px < nx && py < ny && panel < n_panels;
+  const int64_t n_pix = (int64_t)n_panels * nx * ny;
+  const int64_t p = ((int64_t)panel * nx + (valid ? px : 0)) * ny + (valid ? py : 0);
+  if (threadIdx.x < 6) bb[threadIdx.x] = (threadIdx.x < 3) ? INT32_MAX : INT32_MIN;
+  __syncthreads();
+  float h, k, l;
+  rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
+  float w1[W], w2[W], w3[W];
+  int i0 = axis_setup<W>(h * scale1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
+  int j0 = axis_setup<W>(k * scale2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
+  int k0 = axis_setup<W>(l * scale3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
+  {
+    int mi = valid ? i0 : INT32_MAX, mj = valid ? j0 : INT32_MAX, mk = valid ? k0 : INT32_MAX;
+    int xi = valid ? i0 : INT32_MIN, xj = valid ? j0 : INT32_MIN, xk = valid ? k0 : INT32_MIN;
+    mi = __reduce_min_sync(0xffffffffu, mi);
+    mj = __reduce_min_sync(0xffffffffu, mj);
+    mk = __reduce_min_sync(0xffffffffu, mk);
+    xi = __reduce_max_sync(0xffffffffu, xi);
+    xj = __reduce_max_sync(0xffffffffu, xj);
+    xk = __reduce_max_sync(0xffffffffu, xk);
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&bb[0], mi);
+      atomicMin(&bb[1], mj);
+      atomicMin(&bb[2], mk);
+      atomicMax(&bb[3], xi);
+      atomicMax(&bb[4], xj);
+      atomicMax(&bb[5], xk);
+    }
+  }
+  __syncthreads();
+  const int imin = bb[0], jmin = bb[1], kmin = bb[2];
+  const int di = bb[3] - imin + W, dj = bb[4] - jmin + W, dk = bb[5] - kmin + W;
+  const int64_t vol = (int64_t)di * dj * dk;
+  float acc = 0.0f;
+  if (bb[3] >= imin && vol <= SLICE_SMEM_FLOATS) {
+    for (int idx = threadIdx.x; idx < (int)vol; idx += blockDim.x) {
+      int kk = idx % dk;
+      int jj = (idx / dk) % dj;
+      int ii = idx / (dk * dj);
+      box[idx] = __ldg(re_pad + ((size_t)(imin + ii) * g.p2 + (jmin + jj)) * g.p3 + kmin + kk);
+    }
+    __syncthreads();
+    const int li = i0 - imin, lj = j0 - jmin, lk = k0 - kmin;
+#pragma unroll
+    for (int a = 0; a < W; ++a) {
+      float acc_a = 0.0f;
+#pragma unroll
+      for (int b = 0; b < W; ++b) {
+        const float *row = box + ((li + a) * dj + (lj + b)) * dk + lk;
+        float r = 0.0f;
+#pragma unroll
+        for (int c = 0; c < W; ++c) r = fmaf(w3[c], row[c], r);
+        acc_a = fmaf(w2[b], r, acc_a);
+      }
+      acc = fmaf(w1[a], acc_a, acc);
+    }
+  } else {
+#pragma unroll
+    for (int a = 0; a < W; ++a) {
+      float acc_a = 0.0f;
+#pragma unroll
+      for (int b = 0; b < W; ++b) {
+        const float *row = re_pad + ((size_t)(i0 + a) * g.p2 + (j0 + b)) * g.p3 + k0;
+        float r = 0.0f;
+#pragma unroll
+        for (int c = 0; c < W; ++c) r = fmaf(w3[c], __ldg(row + c), r);
+        acc_a = fmaf(w2[b], r, acc_a);
+      }
+      acc = fmaf(w1[a], acc_a, acc);
+    }
+  }
+  if (!valid) return;
+  int64_t idx = o * n_pix + p;
+  out[idx] = acc;
+  if (out_bf16) out_bf16[idx] = __float2bfloat16_rn(acc);
+}
+
 template <int W>
 __global__ void k_t1_spread(float *__restrict__ acc_pad, GridGeom g, const float *__restrict__ x,
                             const float *__restrict__ y, const float *__restrict__ z,
@@ -612,6 +715,30 @@ int spf_slice_t2(spf_nufft_plan P, const float *d_quats, int64_t n_orient, const
   SPF_W_DISPATCH(P->w, (k_slice_t2<W><<<grid, 256, 0, s>>>(P->re_pad, g, d_quats, d_ppr, n_pix,
                                                               s1, s2, s3, d_out, bf)));
   return check_launch("k_slice_t2");
+}
+
+int spf_slice_t2_det(spf_nufft_plan P, const float *d_quats, int64_t n_orient, const float *d_ppr,
+                     int n_panels, int nx, int ny, double scale, float *d_out, void *d_out_bf16,
+                     void *stream) {
+  SPF_TRY(check_plan(P, "spf_slice_t2_det"));
+  SPF_REQUIRE(n_orient >= 0 && n_panels >= 0 && nx >= 0 && ny >= 0,
+              "spf_slice_t2_det: negative size");
+  if (n_orient == 0 || n_panels == 0 || nx == 0 || ny == 0) return SPF_OK;
+  SPF_REQUIRE(d_quats && d_ppr && d_out, "spf_slice_t2_det: NULL pointer");
+  int64_t patches = (int64_t)n_panels * ((nx + SLICE_PATCH - 1) / SLICE_PATCH) *
+                    ((ny + SLICE_PATCH - 1) / SLICE_PATCH);
+  SPF_REQUIRE(n_orient < (1LL << 31) && patches <= 65535, "spf_slice_t2_det: size too large");
+  cudaStream_t s = as_stream(stream);
+  GridGeom g = geom_of(P);
+  float s1 = (float)(scale * P->n[0] / (2.0 * M_PI));
+  float s2 = (float)(scale * P->n[1] / (2.0 * M_PI));
+  float s3 = (float)(scale * P->n[2] / (2.0 * M_PI));
+  dim3 grid((unsigned)n_orient, (unsigned)patches);
+  auto *bf = reinterpret_cast<__nv_bfloat16 *>(d_out_bf16);
+  SPF_W_DISPATCH(P->w, (k_slice_t2_det<W><<<grid, 256, 0, s>>>(P->re_pad, g, d_quats, d_ppr,
+                                                                  n_panels, nx, ny, s1, s2, s3,
+                                                                  d_out, bf)));
+  return check_launch("k_slice_t2_det");
 }
 
 int spf_nufft_t1_zero(spf_nufft_plan P, void *stream) {

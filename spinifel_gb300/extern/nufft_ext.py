@@ -77,7 +77,9 @@ class NUFFT:
 
     def slice_real(self, P: NufftPlan, st: int, en: int, out=None, out_bf16=None):
         """Real part of the type 2 at reference orientations st:en, [en-st, N_pixels]."""
-        return P.slice(self._quats[st:en], self._ppr, self.mult, out=out, out_bf16=out_bf16)
+        det = self.reduced_det_shape if len(self.reduced_det_shape) == 3 else None
+        return P.slice(self._quats[st:en], self._ppr, self.mult, out=out, out_bf16=out_bf16,
+                       det_shape=det)
 
     def forward(self, ugrid, st, en, support, use_recip_sym, N):
         if use_recip_sym:

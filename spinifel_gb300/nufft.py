@@ -8,6 +8,8 @@ from __future__ import annotations
 import ctypes
 import math
 
+import numpy as np
+
 import torch
 
 from . import _lib
@@ -81,9 +83,13 @@ class NufftPlan:
         return re, im
 
     def slice(self, quats: torch.Tensor, ppr: torch.Tensor, scale: float,
-              out: torch.Tensor | None = None, out_bf16: torch.Tensor | None = None):
-        """Slices [n_orient, n_pix] (real part) at the given orientations."""
+              out: torch.Tensor | None = None, out_bf16: torch.Tensor | None = None,
+              det_shape: tuple | None = None):
+        """Slices [n_orient, n_pix] (real part) at the given orientations.
+        With det_shape = (n_panels, nx, ny) the patch-staged kernel is used."""
         quats = quats.to(device=self.device, dtype=torch.float32).contiguous()
+        if det_shape is None and ppr.dim() == 4:
+            det_shape = tuple(ppr.shape[1:])
         ppr = ppr.to(device=self.device, dtype=torch.float32).contiguous().reshape(3, -1)
         n_o, n_p = quats.shape[0], ppr.shape[1]
         if out is None:
@@ -93,8 +99,13 @@ class NufftPlan:
             raise ValueError("out has the wrong size")
         if out_bf16 is not None:
             _lib.require_cuda(out_bf16, "out_bf16", torch.bfloat16)
-        _lib.call("spf_slice_t2", self._h, _lib.ptr(quats), n_o, _lib.ptr(ppr), n_p,
-                  float(scale), _lib.ptr(out), _lib.ptr(out_bf16), _lib.stream_handle())
+        if det_shape is not None and len(det_shape) == 3 and int(np.prod(det_shape)) == n_p:
+            _lib.call("spf_slice_t2_det", self._h, _lib.ptr(quats), n_o, _lib.ptr(ppr),
+                      int(det_shape[0]), int(det_shape[1]), int(det_shape[2]), float(scale),
+                      _lib.ptr(out), _lib.ptr(out_bf16), _lib.stream_handle())
+        else:
+            _lib.call("spf_slice_t2", self._h, _lib.ptr(quats), n_o, _lib.ptr(ppr), n_p,
+                      float(scale), _lib.ptr(out), _lib.ptr(out_bf16), _lib.stream_handle())
         return out
 
     # ---- type 1 ---------------------------------------------------------

@@ -151,6 +151,21 @@ def test_slice_full_size_subset_and_linearity(dev):
     assert float((comb.double() - lin).norm() / lin.norm()) < 1e-6
 
 
+@pytest.mark.parametrize("det", [(4, 32, 32), (4, 128, 128), (2, 20, 37)])
+def test_patch_slicing_identical_to_point_slicing(dev, det):
+    """spf_slice_t2_det (shared-memory patches) gives the same bits as
+    spf_slice_t2 (thread per point), ragged patches included."""
+    from spinifel_gb300.nufft import NufftPlan
+
+    model, ppr, pdr, quats = _slice_case(81, det, 64, 25)
+    ppr_t = t(ppr.reshape(3, -1), dev)
+    P = NufftPlan(81, 1e-6)
+    P.set_modes(t(model, dev))
+    a = P.slice(t(quats, dev), ppr_t, np.pi / pdr.max())
+    b = P.slice(t(quats, dev), ppr_t, np.pi / pdr.max(), det_shape=det)
+    assert torch.equal(a, b)
+
+
 def test_spread_orient_equals_spread_points(dev):
     from spinifel_gb300 import geom
     from spinifel_gb300.nufft import NufftPlan
