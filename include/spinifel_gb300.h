@@ -104,6 +104,17 @@ int spf_nufft_t1_spread_orient(spf_nufft_plan plan, const float *d_quats,
                                double scale, const float *d_c, void *stream);
 int spf_nufft_t1_finish(spf_nufft_plan plan, int isign, float *d_out_re,
                         float *d_out_im, void *stream);
+/* spf_nufft_t1_spread_orient / spf_nufft_interp_spread_orient for a detector
+ * of n_panels x nx x ny pixels: 16 x 16 pixel patches spread into a
+ * shared-memory box of their footprints, added to the accumulator once per
+ * cell. */
+int spf_nufft_t1_spread_det(spf_nufft_plan plan, const float *d_quats, int64_t n_orient,
+                            const float *d_ppr, int n_panels, int nx, int ny, double scale,
+                            const float *d_c, void *stream);
+int spf_nufft_interp_spread_det(spf_nufft_plan plan, const float *d_quats, int64_t n_orient,
+                                const float *d_ppr, int n_panels, int nx, int ny,
+                                double scale, const float *d_weights, void *stream);
+
 /* Fused type 2 -> type 1 at orientation points (the direct A^H D A product):
  * every point interpolates Re of the type-2 fine grid set by
  * spf_nufft_t2_set_modes, multiplies by d_weights[o*n_pix+p] (NULL = 1) and
@@ -179,9 +190,11 @@ int spf_merge_destroy(spf_merge merge);
 int spf_merge_info(spf_merge merge, int *fft_size);
 int spf_merge_set_kernel(spf_merge merge, const float *d_ugrid_conv, int M_ups,
                          void *stream);
+/* det_panels/det_nx/det_ny > 0 select the patch kernels for a multi-panel
+ * detector (n_pix = their product); 0 treats the pixels as an unordered list. */
 int spf_merge_set_direct(spf_merge merge, spf_nufft_plan plan, const float *d_quats,
-                         int64_t n_orient, const float *d_ppr, int64_t n_pix,
-                         double coord_scale, const float *d_weights);
+                         int64_t n_orient, const float *d_ppr, int64_t n_pix, int det_panels,
+                         int det_nx, int det_ny, double coord_scale, const float *d_weights);
 /* d_y = W d_x (M^3 doubles); form 0 = Toeplitz, 1 = direct. */
 int spf_merge_apply(spf_merge merge, int form, const double *d_x, double *d_y,
                     void *stream);

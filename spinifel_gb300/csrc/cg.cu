@@ -56,6 +56,7 @@ struct spf_merge_s {
   spf_nufft_plan_s *nufft = nullptr;
   const float *quats = nullptr, *ppr = nullptr, *weights = nullptr;
   int64_t n_orient = 0, n_pix = 0;
+  int det[3] = {0, 0, 0};
   double coord_scale = 0;
 };
 
@@ -69,6 +70,9 @@ extern "C" int spf_nufft_t1_finish(spf_nufft_plan_s *, int, float *, float *, vo
 extern "C" int spf_nufft_interp_spread_orient(spf_nufft_plan_s *, const float *, int64_t,
                                               const float *, int64_t, double, const float *,
                                               void *);
+extern "C" int spf_nufft_interp_spread_det(spf_nufft_plan_s *, const float *, int64_t,
+                                           const float *, int, int, int, double, const float *,
+                                           void *);
 
 namespace spf {
 namespace cg {
@@ -337,8 +341,12 @@ static int apply_operator_core(spf_merge_s *G, bool direct, cudaStream_t s) {
   } else {
     SPF_TRY(spf_nufft_t2_set_modes(G->nufft, G->modes, nullptr, -1, 0, s));
     SPF_TRY(spf_nufft_t1_zero(G->nufft, s));
-    SPF_TRY(spf_nufft_interp_spread_orient(G->nufft, G->quats, G->n_orient, G->ppr, G->n_pix,
-                                           G->coord_scale, G->weights, s));
+    if (G->det[0] > 0)
+      SPF_TRY(spf_nufft_interp_spread_det(G->nufft, G->quats, G->n_orient, G->ppr, G->det[0],
+                                          G->det[1], G->det[2], G->coord_scale, G->weights, s));
+    else
+      SPF_TRY(spf_nufft_interp_spread_orient(G->nufft, G->quats, G->n_orient, G->ppr, G->n_pix,
+                                             G->coord_scale, G->weights, s));
     SPF_TRY(spf_nufft_t1_finish(G->nufft, +1, G->t1_out, nullptr, s));
   }
   SPF_TRY(cufft_ok(cufftExecD2Z(G->r2c_M, G->reg_in,
@@ -466,9 +474,14 @@ int spf_merge_set_kernel(spf_merge_s *G, const float *d_ugrid_conv, int M_ups, v
 }
 
 int spf_merge_set_direct(spf_merge_s *G, spf_nufft_plan_s *plan, const float *d_quats,
-                         int64_t n_orient, const float *d_ppr, int64_t n_pix, double coord_scale,
-                         const float *d_weights) {
+                         int64_t n_orient, const float *d_ppr, int64_t n_pix, int det_panels,
+                         int det_nx, int det_ny, double coord_scale, const float *d_weights) {
   SPF_REQUIRE(G && plan && d_quats && d_ppr, "spf_merge_set_direct: NULL pointer");
+  SPF_REQUIRE(det_panels <= 0 || (int64_t)det_panels * det_nx * det_ny == n_pix,
+              "spf_merge_set_direct: detector shape does not match n_pix");
+  G->det[0] = det_panels > 0 ? det_panels : 0;
+  G->det[1] = det_nx;
+  G->det[2] = det_ny;
   G->nufft = plan;
   G->quats = d_quats;
   G->ppr = d_ppr;

@@ -541,12 +541,22 @@ __global__ void __launch_bounds__(RR_THREADS)
   }
 }
 
-// 8 lanes per frame, one candidate each: the exact FP32 distance computed
-// with the arithmetic of the plain kernel (k_dist_argmin_f32): acc =
-// fma(x_p, s_p, acc) for p = 0 .. n_pix-1 in order, then (x2 + s2) - 2 acc,
-// so the re-ranked values are bit-identical to the plain path's.  Lane 0 of
-// the group keeps the lexicographic minimum and evaluates the certificate.
-__global__ void __launch_bounds__(RR_THREADS)
+// Exact FP32 distances of the 8 candidates of each frame, computed with the
+// arithmetic of the plain kernel (k_dist_argmin_f32): acc = fma(x_p, s_p, acc)
+// for p = 0 .. n_pix-1 in order, then (x2 + s2) - 2 acc, so the re-ranked
+// values are bit-identical to the plain path's.  A CTA takes 4 frames (32
+// (frame, candidate) chains, one per lane of warp 0); all its warps stream the
+// 4 frame rows and 32 candidate rows through shared memory in coalesced
+// 256-pixel chunks (double-buffered, rows padded to 257 floats so the 32
+// chains read 32 different banks).  Lane 0 of each group of 8 keeps the
+// lexicographic minimum and evaluates the certificate.
+constexpr int RX_FRAMES = 4;
+constexpr int RX_ROWS = RX_FRAMES * (TOPK + 1);  // 4 frame rows + 32 candidate rows
+constexpr int RX_CHUNK = 256;
+constexpr int RX_STRIDE = RX_CHUNK + 1;
+constexpr int RX_THREADS = 128;
+
+__global__ void __launch_bounds__(RX_THREADS)
     k_rerank_exact(const float *__restrict__ cand_d, const int32_t *__restrict__ cand_i,
                    const float *__restrict__ img, const float *__restrict__ img_sq,
                    int64_t n_img, const float *__restrict__ ref, const float *__restrict__ ref_sq,
@@ -554,35 +564,69 @@ __global__ void __launch_bounds__(RR_THREADS)
                    float *__restrict__ work, int32_t *__restrict__ out_idx,
                    float *__restrict__ out_dist, int32_t *__restrict__ uncertified,
                    int32_t *__restrict__ out_top) {
-  const int64_t gt = blockIdx.x * (int64_t)RR_THREADS + threadIdx.x;
-  const int64_t im = gt / TOPK;
-  const int c = (int)(gt % TOPK);
+  extern __shared__ float rx[];  // [2][RX_ROWS][RX_STRIDE]
+  __shared__ const float *rows[RX_ROWS];
+  const int tid = threadIdx.x;
+  const int64_t f0 = (int64_t)blockIdx.x * RX_FRAMES;
+  // row table: r < 4 -> frame rows, r >= 4 -> candidate rows (frame (r-4)/8)
+  if (tid < RX_ROWS) {
+    const float *ptr = nullptr;
+    if (tid < RX_FRAMES) {
+      int64_t im = f0 + tid;
+      if (im < n_img) ptr = img + im * n_pix;
+    } else {
+      int q = tid - RX_FRAMES;
+      int64_t im = f0 + q / TOPK;
+      if (im < n_img) {
+        int32_t j = cand_i[(size_t)im * TOPK + (q % TOPK)];
+        if (j != INT32_MAX) ptr = ref + (int64_t)j * n_pix;
+      }
+    }
+    rows[tid] = ptr;
+  }
+  __syncthreads();
+  const int64_t nchunks = (n_pix + RX_CHUNK - 1) / RX_CHUNK;
+  auto stage = [&](int buf, int64_t chunk) {
+    float *dst = rx + (size_t)buf * RX_ROWS * RX_STRIDE;
+    const int64_t base = chunk * RX_CHUNK;
+    for (int e = tid; e < RX_ROWS * RX_CHUNK; e += RX_THREADS) {
+      int r = e / RX_CHUNK, k = e % RX_CHUNK;
+      const float *src = rows[r];
+      int64_t p = base + k;
+      dst[r * RX_STRIDE + k] = (src && p < n_pix) ? __ldg(src + p) : 0.0f;
+    }
+  };
+  // chain of lane l of warp 0: frame l / 8, candidate l % 8
+  const int lane = tid & 31;
+  const int fr = lane / TOPK;
+  const int crow = RX_FRAMES + lane;
+  float acc = 0.0f;
+  stage(0, 0);
+  __syncthreads();
+  for (int64_t ch = 0; ch < nchunks; ++ch) {
+    int cur = (int)(ch & 1);
+    if (ch + 1 < nchunks) stage(cur ^ 1, ch + 1);
+    if (tid < 32) {
+      const float *xb = rx + (size_t)cur * RX_ROWS * RX_STRIDE + fr * RX_STRIDE;
+      const float *sb = rx + (size_t)cur * RX_ROWS * RX_STRIDE + crow * RX_STRIDE;
+      int64_t lim = n_pix - ch * RX_CHUNK;
+      int kmax = lim < RX_CHUNK ? (int)lim : RX_CHUNK;
+#pragma unroll 8
+      for (int k = 0; k < kmax; ++k) acc = fmaf(xb[k], sb[k], acc);
+    }
+    __syncthreads();
+  }
+  if (tid >= 32) return;
+  const int64_t im = f0 + fr;
+  const int c = lane % TOPK;
   const bool live = im < n_img;
   const int64_t imc = live ? im : 0;
   int32_t j = cand_i[(size_t)imc * TOPK + c];
   const bool valid = live && j != INT32_MAX;
-  float acc = 0.0f;
-  if (valid) {
-    const float *x = img + imc * n_pix;
-    const float *sr = ref + (int64_t)j * n_pix;
-    int64_t p = 0;
-    if ((n_pix & 3) == 0 && aligned(x, 16) && aligned(sr, 16)) {
-      for (; p < n_pix; p += 4) {
-        float4 a = *reinterpret_cast<const float4 *>(x + p);
-        float4 b = __ldg(reinterpret_cast<const float4 *>(sr + p));
-        acc = fmaf(a.x, b.x, acc);
-        acc = fmaf(a.y, b.y, acc);
-        acc = fmaf(a.z, b.z, acc);
-        acc = fmaf(a.w, b.w, acc);
-      }
-    }
-    for (; p < n_pix; ++p) acc = fmaf(x[p], __ldg(sr + p), acc);
-  }
   float x2 = live ? img_sq[imc] : 0.0f;
   float dist = valid ? __fsub_rn(__fadd_rn(x2, ref_sq[j]), __fmul_rn(2.0f, acc))
                      : __int_as_float(0x7f800000);
   int32_t jj = valid ? j : INT32_MAX;
-  // lexicographic minimum over the 8 lanes of this frame
 #pragma unroll
   for (int o = 4; o >= 1; o >>= 1) {
     float od = __shfl_xor_sync(0xffffffffu, dist, o, TOPK);
@@ -619,6 +663,8 @@ __global__ void __launch_bounds__(RR_THREADS)
   // of the re-ranked best
   work[im] = (dist - x2) + band;
 }
+
+constexpr size_t RX_SMEM = 2 * RX_ROWS * RX_STRIDE * sizeof(float);
 
 // Exact FP32 distances (plain-path arithmetic) for every listed candidate of
 // every frame; the per-frame lexicographic minimum is folded into best[]
@@ -700,6 +746,20 @@ __global__ void k_row_norms(const float *__restrict__ x, int64_t n_rows, int64_t
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// k_rerank_exact uses RX_SMEM (74 KB) of dynamic shared memory
+static int rerank_smem_attr() {
+  static bool done[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64 || done[dev]) return SPF_OK;
+  SPF_TRY(check_cuda(cudaFuncSetAttribute(k_rerank_exact,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)RX_SMEM),
+                     "k_rerank_exact"));
+  done[dev] = true;
+  return SPF_OK;
+}
+
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static bool tried = false;
@@ -857,8 +917,8 @@ int spf_rerank_fp32(float *d_cand_d, int32_t *d_cand_i, int64_t n_tiles, const f
   k_merge_top8<<<(unsigned)n_img, RR_THREADS, 0, s>>>(d_cand_d, d_cand_i, n_tiles, d_img, n_img,
                                                       d_ref_m2, n_pix, d_work);
   SPF_TRY(check_launch("k_merge_top8"));
-  int64_t threads = n_img * TOPK;
-  k_rerank_exact<<<(unsigned)((threads + RR_THREADS - 1) / RR_THREADS), RR_THREADS, 0, s>>>(
+  SPF_TRY(rerank_smem_attr());
+  k_rerank_exact<<<(unsigned)((n_img + RX_FRAMES - 1) / RX_FRAMES), RX_THREADS, RX_SMEM, s>>>(
       d_cand_d, d_cand_i, d_img, d_img_sq, n_img, d_ref, d_ref_sq, ref_sq_max, n_pix, ref_offset,
       d_work, d_idx, d_dist, d_uncertified, d_top8);
   return check_launch("k_rerank_exact");
@@ -1004,8 +1064,8 @@ extern "C" int spf_match_bf16_static(const void *d_img_bf16, const float *d_img,
   k_merge_top8<<<(unsigned)n_img, RR_THREADS, 0, s>>>(cand_d, cand_i, tiles, d_img, n_img,
                                                       d_ref_m2, n_pix, work);
   SPF_TRY(check_launch("k_merge_top8 (static scratch)"));
-  int64_t threads = n_img * TOPK;
-  k_rerank_exact<<<(unsigned)((threads + RR_THREADS - 1) / RR_THREADS), RR_THREADS, 0, s>>>(
+  SPF_TRY(rerank_smem_attr());
+  k_rerank_exact<<<(unsigned)((n_img + RX_FRAMES - 1) / RX_FRAMES), RX_THREADS, RX_SMEM, s>>>(
       cand_d, cand_i, d_img, d_img_sq, n_img, d_ref, d_ref_sq, ref_sq_max, n_pix, 0, work, d_idx,
       d_dist, d_uncertified, nullptr);
   return check_launch("k_rerank_exact (static scratch)");

@@ -364,6 +364,8 @@ __global__ void __launch_bounds__(256)
       box[idx] = __ldg(re_pad + ((size_t)(imin + ii) * g.p2 + (jmin + jj)) * g.p3 + kmin + kk);
     }
     __syncthreads();
+    // only valid points' footprints are inside the box
+    if (!valid) return;
     const int li = i0 - imin, lj = j0 - jmin, lk = k0 - kmin;
 #pragma unroll
     for (int a = 0; a < W; ++a) {
@@ -379,6 +381,7 @@ __global__ void __launch_bounds__(256)
       acc = fmaf(w1[a], acc_a, acc);
     }
   } else {
+    if (!valid) return;
 #pragma unroll
     for (int a = 0; a < W; ++a) {
       float acc_a = 0.0f;
@@ -397,6 +400,159 @@ __global__ void __launch_bounds__(256)
   int64_t idx = o * n_pix + p;
   out[idx] = acc;
   if (out_bf16) out_bf16[idx] = __float2bfloat16_rn(acc);
+}
+
+// Shared pieces of the patch kernels: pixel of this thread, its footprint and
+// the CTA's bounding box of footprints.
+struct PatchPoint {
+  bool valid;
+  int64_t p;
+  int i0, j0, k0;
+};
+
+template <int W>
+__device__ __forceinline__ PatchPoint patch_point(const GridGeom &g, const float *__restrict__ quat,
+                                                  const float *__restrict__ ppr, int n_panels,
+                                                  int nx, int ny, float s1, float s2, float s3,
+                                                  float *w1, float *w2, float *w3) {
+  const int patches_y = (ny + SLICE_PATCH - 1) / SLICE_PATCH;
+  const int patches_x = (nx + SLICE_PATCH - 1) / SLICE_PATCH;
+  const int pid = blockIdx.y;
+  const int panel = pid / (patches_x * patches_y);
+  const int rem = pid % (patches_x * patches_y);
+  const int px = (rem / patches_y) * SLICE_PATCH + (int)(threadIdx.x / SLICE_PATCH);
+  const int py = (rem % patches_y) * SLICE_PATCH + (int)(threadIdx.x % SLICE_PATCH);
+  PatchPoint pt;
+  pt.valid = px < nx && py < ny && panel < n_panels;
+  const int64_t n_pix = (int64_t)n_panels * nx * ny;
+  pt.p = ((int64_t)panel * nx + (pt.valid ? px : 0)) * ny + (pt.valid ? py : 0);
+  float h, k, l;
+  rotate_inv(quat, ppr[pt.p], ppr[n_pix + pt.p], ppr[2 * n_pix + pt.p], 1.0f, h, k, l);
+  pt.i0 = axis_setup<W>(h * s1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
+  pt.j0 = axis_setup<W>(k * s2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
+  pt.k0 = axis_setup<W>(l * s3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
+  return pt;
+}
+
+// bb must be shared int[6]; returns false when no thread of the CTA is valid
+__device__ __forceinline__ bool patch_box(const PatchPoint &pt, int *bb) {
+  if (threadIdx.x < 6) bb[threadIdx.x] = (threadIdx.x < 3) ? INT32_MAX : INT32_MIN;
+  __syncthreads();
+  int mi = pt.valid ? pt.i0 : INT32_MAX, mj = pt.valid ? pt.j0 : INT32_MAX;
+  int mk = pt.valid ? pt.k0 : INT32_MAX;
+  int xi = pt.valid ? pt.i0 : INT32_MIN, xj = pt.valid ? pt.j0 : INT32_MIN;
+  int xk = pt.valid ? pt.k0 : INT32_MIN;
+  mi = __reduce_min_sync(0xffffffffu, mi);
+  mj = __reduce_min_sync(0xffffffffu, mj);
+  mk = __reduce_min_sync(0xffffffffu, mk);
+  xi = __reduce_max_sync(0xffffffffu, xi);
+  xj = __reduce_max_sync(0xffffffffu, xj);
+  xk = __reduce_max_sync(0xffffffffu, xk);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&bb[0], mi);
+    atomicMin(&bb[1], mj);
+    atomicMin(&bb[2], mk);
+    atomicMax(&bb[3], xi);
+    atomicMax(&bb[4], xj);
+    atomicMax(&bb[5], xk);
+  }
+  __syncthreads();
+  return bb[3] >= bb[0];
+}
+
+// Type-1 spreading on a multi-panel detector: the CTA's 256 points spread
+// into a shared-memory copy of their footprint box (shared atomics), which is
+// then added to the padded accumulator once per cell (W^3 global atomics per
+// point become about (box volume / 256)).  Boxes too large for shared memory
+// spread straight to global memory.
+constexpr int SPREAD_SMEM_FLOATS = 11264;
+
+template <int W, bool INTERP>
+__global__ void __launch_bounds__(256)
+    k_spread_det(const float *__restrict__ re_pad, float *__restrict__ acc_pad, GridGeom g,
+                 const float *__restrict__ quats, const float *__restrict__ ppr, int n_panels,
+                 int nx, int ny, float s1, float s2, float s3, const float *__restrict__ vals) {
+  __shared__ float box[SPREAD_SMEM_FLOATS];
+  __shared__ int bb[6];
+  const int64_t o = blockIdx.x;
+  const int64_t n_pix = (int64_t)n_panels * nx * ny;
+  float w1[W], w2[W], w3[W];
+  PatchPoint pt = patch_point<W>(g, quats + 4 * o, ppr, n_panels, nx, ny, s1, s2, s3, w1, w2, w3);
+  if (!patch_box(pt, bb)) return;
+  const int imin = bb[0], jmin = bb[1], kmin = bb[2];
+  const int di = bb[3] - imin + W, dj = bb[4] - jmin + W, dk = bb[5] - kmin + W;
+  const int64_t vol = (int64_t)di * dj * dk;
+  const bool staged = vol <= SPREAD_SMEM_FLOATS;
+  float v = 0.0f;
+  if constexpr (INTERP) {
+    // interpolate from the type-2 grid first (staged through the same box)
+    if (staged) {
+      for (int idx = threadIdx.x; idx < (int)vol; idx += blockDim.x) {
+        int kk = idx % dk, jj = (idx / dk) % dj, ii = idx / (dk * dj);
+        box[idx] = __ldg(re_pad + ((size_t)(imin + ii) * g.p2 + (jmin + jj)) * g.p3 + kmin + kk);
+      }
+      __syncthreads();
+    }
+    const int li = pt.i0 - imin, lj = pt.j0 - jmin, lk = pt.k0 - kmin;
+    if (pt.valid) {  // only valid points' footprints are inside the box
+#pragma unroll
+      for (int a = 0; a < W; ++a) {
+        float acc_a = 0.0f;
+#pragma unroll
+        for (int b = 0; b < W; ++b) {
+          const float *row = staged ? box + ((li + a) * dj + (lj + b)) * dk + lk
+                                    : re_pad + ((size_t)(pt.i0 + a) * g.p2 + (pt.j0 + b)) * g.p3 +
+                                          pt.k0;
+          float r = 0.0f;
+#pragma unroll
+          for (int c = 0; c < W; ++c) r = fmaf(w3[c], row[c], r);
+          acc_a = fmaf(w2[b], r, acc_a);
+        }
+        v = fmaf(w1[a], acc_a, v);
+      }
+      if (vals) v *= vals[o * n_pix + pt.p];
+    }
+    if (staged) __syncthreads();  // everyone has read the box before it is reused
+  } else {
+    v = vals[o * n_pix + pt.p];
+  }
+  if (!pt.valid) v = 0.0f;
+  if (staged) {
+    for (int idx = threadIdx.x; idx < (int)vol; idx += blockDim.x) box[idx] = 0.0f;
+    __syncthreads();
+    if (v != 0.0f) {
+      const int li = pt.i0 - imin, lj = pt.j0 - jmin, lk = pt.k0 - kmin;
+#pragma unroll
+      for (int a = 0; a < W; ++a) {
+#pragma unroll
+        for (int b = 0; b < W; ++b) {
+          float wab = w1[a] * w2[b] * v;
+          float *row = box + ((li + a) * dj + (lj + b)) * dk + lk;
+#pragma unroll
+          for (int c = 0; c < W; ++c) atomicAdd(row + c, wab * w3[c]);
+        }
+      }
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < (int)vol; idx += blockDim.x) {
+      float bv = box[idx];
+      if (bv != 0.0f) {
+        int kk = idx % dk, jj = (idx / dk) % dj, ii = idx / (dk * dj);
+        atomicAdd(acc_pad + ((size_t)(imin + ii) * g.p2 + (jmin + jj)) * g.p3 + kmin + kk, bv);
+      }
+    }
+  } else if (v != 0.0f) {
+#pragma unroll
+    for (int a = 0; a < W; ++a) {
+#pragma unroll
+      for (int b = 0; b < W; ++b) {
+        float wab = w1[a] * w2[b] * v;
+        float *row = acc_pad + ((size_t)(pt.i0 + a) * g.p2 + (pt.j0 + b)) * g.p3 + pt.k0;
+#pragma unroll
+        for (int c = 0; c < W; ++c) atomicAdd(row + c, wab * w3[c]);
+      }
+    }
+  }
 }
 
 template <int W>
@@ -801,6 +957,48 @@ int spf_nufft_interp_spread_orient(spf_nufft_plan P, const float *d_quats, int64
                            P->re_pad, P->acc_pad, g, d_quats, d_ppr, n_pix, s1, s2, s3,
                            d_weights)));
   return check_launch("k_interp_spread_orient");
+}
+
+static int spread_det(spf_nufft_plan P, bool interp, const float *d_quats, int64_t n_orient,
+                      const float *d_ppr, int n_panels, int nx, int ny, double scale,
+                      const float *d_vals, void *stream, const char *name) {
+  SPF_TRY(check_plan(P, name));
+  SPF_REQUIRE(n_orient >= 0 && n_panels >= 0 && nx >= 0 && ny >= 0, "%s: negative size", name);
+  if (n_orient == 0 || n_panels == 0 || nx == 0 || ny == 0) return SPF_OK;
+  SPF_REQUIRE(d_quats && d_ppr && (interp || d_vals), "%s: NULL pointer", name);
+  int64_t patches = (int64_t)n_panels * ((nx + SLICE_PATCH - 1) / SLICE_PATCH) *
+                    ((ny + SLICE_PATCH - 1) / SLICE_PATCH);
+  SPF_REQUIRE(n_orient < (1LL << 31) && patches <= 65535, "%s: size too large", name);
+  cudaStream_t s = as_stream(stream);
+  GridGeom g = geom_of(P);
+  float s1 = (float)(scale * P->n[0] / (2.0 * M_PI));
+  float s2 = (float)(scale * P->n[1] / (2.0 * M_PI));
+  float s3 = (float)(scale * P->n[2] / (2.0 * M_PI));
+  dim3 grid((unsigned)n_orient, (unsigned)patches);
+  if (interp) {
+    SPF_W_DISPATCH(P->w, (k_spread_det<W, true><<<grid, 256, 0, s>>>(
+                             P->re_pad, P->acc_pad, g, d_quats, d_ppr, n_panels, nx, ny, s1, s2, s3,
+                             d_vals)));
+  } else {
+    SPF_W_DISPATCH(P->w, (k_spread_det<W, false><<<grid, 256, 0, s>>>(
+                             P->re_pad, P->acc_pad, g, d_quats, d_ppr, n_panels, nx, ny, s1, s2, s3,
+                             d_vals)));
+  }
+  return check_launch(name);
+}
+
+int spf_nufft_t1_spread_det(spf_nufft_plan P, const float *d_quats, int64_t n_orient,
+                            const float *d_ppr, int n_panels, int nx, int ny, double scale,
+                            const float *d_c, void *stream) {
+  return spread_det(P, false, d_quats, n_orient, d_ppr, n_panels, nx, ny, scale, d_c, stream,
+                    "spf_nufft_t1_spread_det");
+}
+
+int spf_nufft_interp_spread_det(spf_nufft_plan P, const float *d_quats, int64_t n_orient,
+                                const float *d_ppr, int n_panels, int nx, int ny, double scale,
+                                const float *d_weights, void *stream) {
+  return spread_det(P, true, d_quats, n_orient, d_ppr, n_panels, nx, ny, scale, d_weights, stream,
+                    "spf_nufft_interp_spread_det");
 }
 
 int spf_nufft_t1_finish(spf_nufft_plan P, int isign, float *d_out_re, float *d_out_im,

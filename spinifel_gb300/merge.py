@@ -58,13 +58,17 @@ class MergeOperator:
         torch.cuda.current_stream().synchronize()
 
     def set_direct(self, plan: NufftPlan, quats: torch.Tensor, ppr: torch.Tensor, scale: float,
-                   weights: torch.Tensor | None = None):
+                   weights: torch.Tensor | None = None, det_shape: tuple | None = None):
         quats = quats.to(device=self.device, dtype=torch.float32).contiguous()
+        if det_shape is None and ppr.dim() == 4:
+            det_shape = tuple(ppr.shape[1:])
         ppr = ppr.to(device=self.device, dtype=torch.float32).contiguous().reshape(3, -1)
         if weights is not None:
             weights = weights.to(device=self.device, dtype=torch.float32).contiguous()
+        d = tuple(det_shape) if det_shape is not None and len(det_shape) == 3 else (0, 0, 0)
         _lib.call("spf_merge_set_direct", self._h, plan.handle, _lib.ptr(quats), quats.shape[0],
-                  _lib.ptr(ppr), ppr.shape[1], float(scale), _lib.ptr(weights))
+                  _lib.ptr(ppr), ppr.shape[1], int(d[0]), int(d[1]), int(d[2]), float(scale),
+                  _lib.ptr(weights))
         self._keep = [plan, quats, ppr, weights]
         self.has_direct = True
 
@@ -74,6 +78,15 @@ class MergeOperator:
         _lib.call("spf_merge_apply", self._h, int(form), _lib.ptr(x), _lib.ptr(y),
                   _lib.stream_handle())
         return y
+
+    def cg_into(self, b: torch.Tensor, x: torch.Tensor, hist: torch.Tensor | None,
+                iters: torch.Tensor, maxiter: int, rtol: float = 1e-5, form: int = 0,
+                x0_is_zero: bool = False):
+        """CG into preallocated device tensors with no host synchronisation, so
+        the call can be captured in a CUDA graph (x holds x0 on entry)."""
+        _lib.call("spf_merge_cg", self._h, int(form), _lib.ptr(b), _lib.ptr(x), int(x0_is_zero),
+                  int(maxiter), float(rtol), _lib.ptr(hist), _lib.ptr(iters),
+                  _lib.stream_handle())
 
     def cg(self, b: torch.Tensor, x0: torch.Tensor, maxiter: int, rtol: float = 1e-5,
            form: int = 0, history: bool = True):

@@ -118,14 +118,23 @@ class NufftPlan:
         _lib.call("spf_nufft_t1_spread", self._h, _lib.ptr(x), _lib.ptr(y), _lib.ptr(z),
                   _lib.ptr(c), x.numel(), _lib.stream_handle())
 
-    def spread_orient(self, quats, ppr, scale, c):
+    def spread_orient(self, quats, ppr, scale, c, det_shape: tuple | None = None):
         quats = quats.to(device=self.device, dtype=torch.float32).contiguous()
+        if det_shape is None and ppr.dim() == 4:
+            det_shape = tuple(ppr.shape[1:])
         ppr = ppr.to(device=self.device, dtype=torch.float32).contiguous().reshape(3, -1)
         c = c.to(device=self.device, dtype=torch.float32).contiguous()
         if c.numel() != quats.shape[0] * ppr.shape[1]:
             raise ValueError("strengths must be n_orient * n_pix")
-        _lib.call("spf_nufft_t1_spread_orient", self._h, _lib.ptr(quats), quats.shape[0],
-                  _lib.ptr(ppr), ppr.shape[1], float(scale), _lib.ptr(c), _lib.stream_handle())
+        if det_shape is not None and len(det_shape) == 3 and \
+                int(np.prod(det_shape)) == ppr.shape[1]:
+            _lib.call("spf_nufft_t1_spread_det", self._h, _lib.ptr(quats), quats.shape[0],
+                      _lib.ptr(ppr), int(det_shape[0]), int(det_shape[1]), int(det_shape[2]),
+                      float(scale), _lib.ptr(c), _lib.stream_handle())
+        else:
+            _lib.call("spf_nufft_t1_spread_orient", self._h, _lib.ptr(quats), quats.shape[0],
+                      _lib.ptr(ppr), ppr.shape[1], float(scale), _lib.ptr(c),
+                      _lib.stream_handle())
 
     def finish(self, isign: int = 1, want_imag=False):
         re = torch.empty(self.m, device=self.device, dtype=torch.float32)

@@ -69,9 +69,11 @@ class Merge:
         if self.form == "direct":
             assert orientations is not None
             plan = self.nufft.plan(self.M)
+            det = tuple(self.pixel_position_reciprocal.shape[1:])
             op.set_direct(plan, torch.as_tensor(orientations, dtype=torch.float32, device=dev),
                           torch.as_tensor(self.pixel_position_reciprocal.reshape(3, -1),
-                                          dtype=torch.float32, device=dev), self.mult)
+                                          dtype=torch.float32, device=dev), self.mult,
+                          det_shape=det if len(det) == 3 else None)
         uvect_ADb = self.nufft.adjoint(self.data, H_, K_, L_, sup,
                                        self.use_reciprocal_symmetry, self.M).reshape(-1)
         d = uvect_ADb.double() + self.rlambda * x0

@@ -135,3 +135,35 @@ def test_cg_stops_on_rtol(setup):
     assert h[n] < 0.05 * float(b.norm()) <= h[n - 1]
     r = b - op.apply(x)
     assert float(r.norm() / b.norm()) < 0.06
+
+
+def test_cg_solve_captured_in_a_cuda_graph(setup):
+    """The whole CG solve (operator FFTs included) is one graph; replaying it
+    gives the eagerly computed solution bit for bit."""
+    M = setup["M"]
+    S = omerge.support_from_estimate(setup["ac_est"])
+    op, mo, _ = _operator(setup, S)
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(53)
+    xs = rng.standard_normal((M,) * 3)
+    xs = 0.5 * (xs + xs[::-1, ::-1, ::-1])
+    b = op.apply(torch.as_tensor(xs.reshape(-1).copy(), device=dev))
+    x = torch.zeros_like(b)
+    hist = torch.zeros(12, dtype=torch.float64, device=dev)
+    iters = torch.zeros(1, dtype=torch.int32, device=dev)
+    op.cg_into(b, x, hist, iters, 12, 1e-9, x0_is_zero=True)
+    torch.cuda.synchronize()
+    eager = x.clone()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        x.zero_()
+        with torch.cuda.graph(g, stream=s):
+            op.cg_into(b, x, hist, iters, 12, 1e-9, x0_is_zero=True)
+    torch.cuda.current_stream().wait_stream(s)
+    x.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    assert int(iters.item()) == 12
+    assert torch.equal(x, eager)

@@ -185,6 +185,40 @@ def test_spread_orient_equals_spread_points(dev):
     assert rel(a.cpu().numpy(), b.cpu().numpy()) < 1e-5
 
 
+@pytest.mark.parametrize("det", [(4, 16, 16), (4, 128, 128), (2, 20, 37)])
+def test_patch_spreading_equals_point_spreading(dev, det):
+    from spinifel_gb300.nufft import NufftPlan
+
+    model, ppr, pdr, quats = _slice_case(41, det, 24, 26)
+    mult = np.pi / pdr.max()
+    rng = np.random.default_rng(27)
+    c = t(rng.poisson(2.0, (24, ppr[0].size)).astype(np.float32), dev)
+    ppr_t = t(ppr.reshape(3, -1), dev)
+    P = NufftPlan(41, 1e-6)
+    out = []
+    for shape in (None, det):
+        P.spread_zero()
+        P.spread_orient(t(quats, dev), ppr_t, mult, c, det_shape=shape)
+        out.append(P.finish(+1)[0].cpu().numpy())
+    assert rel(out[1], out[0]) < 1e-6
+    # the fused interpolate-then-spread operator, point vs patch kernels
+    from spinifel_gb300 import _lib
+
+    P.set_modes(t(model, dev))
+    res = []
+    for patch in (False, True):
+        P.spread_zero()
+        if patch:
+            _lib.call("spf_nufft_interp_spread_det", P.handle, _lib.ptr(t(quats, dev)), 24,
+                      _lib.ptr(ppr_t), det[0], det[1], det[2], float(mult), None,
+                      _lib.stream_handle())
+        else:
+            _lib.call("spf_nufft_interp_spread_orient", P.handle, _lib.ptr(t(quats, dev)), 24,
+                      _lib.ptr(ppr_t), ppr_t.shape[1], float(mult), None, _lib.stream_handle())
+        res.append(P.finish(+1)[0].cpu().numpy())
+    assert rel(res[1], res[0]) < 1e-6
+
+
 def test_operator_glue_matches_reference_golden(dev):
     """autocorrelation.forward / adjoint against the reference's own glue
     (support, real part, / M^3) run on the FP64 oracle."""
