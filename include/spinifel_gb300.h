@@ -41,6 +41,11 @@ const char *spf_last_error(void);
 uint64_t spf_launch_count(void);
 /* Device-side error word written by bounded waits (0 = none); reset to 0. */
 int spf_device_error(void *stream, int *h_code);
+/* Self-test of the bounded-wait path used by the tensor-core kernels: one
+ * thread waits on an mbarrier that nothing completes, gives up after
+ * timeout_ms (1..5000), records -SPF_ERR_TIMEOUT in the device error word and
+ * writes d_result[0] = 0 (gave up) / 1, d_result[1] = milliseconds waited. */
+int spf_selftest_bounded_wait(int64_t timeout_ms, int *d_result, void *stream);
 
 /* ---- NUFFT plan ---------------------------------------------------------
  * Replaces the cufinufft / finufft plans built in

@@ -44,6 +44,7 @@ SIGNATURES = {
     "spf_last_error": [],
     "spf_launch_count": [],
     "spf_device_error": [_c_void_p, ctypes.POINTER(_int)],
+    "spf_selftest_bounded_wait": [_i64, _c_void_p, _c_void_p],
     "spf_nufft_plan_create": [_int, _int, _int, _dbl, _dbl, ctypes.POINTER(_c_void_p)],
     "spf_nufft_plan_destroy": [_c_void_p],
     "spf_nufft_plan_info": [_c_void_p, ctypes.POINTER(_int), ctypes.POINTER(_int),

@@ -405,6 +405,36 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
+// Waits on an mbarrier that nothing arrives at, through the same bounded wait
+// the GEMM uses, and reports what the wait returned: the self-test of the
+// timeout path (the wait must give up, raise the abort flag and leave the
+// device usable).
+__global__ void k_wait_selftest(uint64_t timeout_ns, unsigned int *err, int *result) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int abort;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint64_t t0 = globaltimer();
+    bool ok = true;
+    while (!mbar_try_wait(&bar, 0)) {
+      if (globaltimer() - t0 > timeout_ns) {
+        ok = false;
+        break;
+      }
+    }
+    result[0] = ok ? 1 : 0;
+    result[1] = (int)((globaltimer() - t0) / 1000000ull);  // ms waited
+    if (!ok) atomicExch(err, (unsigned int)(-SPF_ERR_TIMEOUT));
+    // complete the barrier's phase so no waiter can remain
+    mbar_arrive(&bar);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // merge + exact FP32 re-rank
 // ---------------------------------------------------------------------------
@@ -932,6 +962,16 @@ int spf_col_maxsq_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_
   k_col_maxsq<<<grid_for(n_pix, 256, 4096), 256, 0, as_stream(stream)>>>(d_x, n_rows, n_pix,
                                                                           d_out);
   return check_launch("spf_col_maxsq_f32");
+}
+
+int spf_selftest_bounded_wait(int64_t timeout_ms, int *d_result, void *stream) {
+  SPF_REQUIRE(timeout_ms > 0 && timeout_ms <= 5000, "spf_selftest_bounded_wait: 1..5000 ms");
+  SPF_REQUIRE(d_result != nullptr, "spf_selftest_bounded_wait: NULL pointer");
+  unsigned int *err = device_error_word();
+  SPF_REQUIRE(err != nullptr, "spf_selftest_bounded_wait: no device error word");
+  k_wait_selftest<<<1, 32, 0, as_stream(stream)>>>((uint64_t)timeout_ms * 1000000ull, err,
+                                                   d_result);
+  return check_launch("k_wait_selftest");
 }
 
 int spf_row_norms_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_sq, float *d_n4,

@@ -200,7 +200,9 @@ def test_patch_spreading_equals_point_spreading(dev, det):
         P.spread_zero()
         P.spread_orient(t(quats, dev), ppr_t, mult, c, det_shape=shape)
         out.append(P.finish(+1)[0].cpu().numpy())
-    assert rel(out[1], out[0]) < 1e-6
+    # two FP32 accumulation orders (shared-memory box then flush, vs direct
+    # atomics) over ~1.6e6 points: equal within the NUFFT tolerance
+    assert rel(out[1], out[0]) < TOL
     # the fused interpolate-then-spread operator, point vs patch kernels
     from spinifel_gb300 import _lib
 
@@ -216,7 +218,7 @@ def test_patch_spreading_equals_point_spreading(dev, det):
             _lib.call("spf_nufft_interp_spread_orient", P.handle, _lib.ptr(t(quats, dev)), 24,
                       _lib.ptr(ppr_t), ppr_t.shape[1], float(mult), None, _lib.stream_handle())
         res.append(P.finish(+1)[0].cpu().numpy())
-    assert rel(res[1], res[0]) < 1e-6
+    assert rel(res[1], res[0]) < TOL
 
 
 def test_operator_glue_matches_reference_golden(dev):
