@@ -167,7 +167,9 @@ def measure_serving(rset, frames_u16_host, rate_fps, total_frames, path, seed=7)
     return {"path": path, "offered_fps": rate_fps, "requests": len(sched), "frames": n,
             "frames_per_s": n / (t1 - t0), "p50_ms": float(np.percentile(lat, 50)),
             "p99_ms": float(np.percentile(lat, 99)), "launches": stats.get("launches", 0),
-            "uncertified": stats.get("uncertified", 0)}
+            "uncertified": stats.get("uncertified", 0),
+            "server_ms": {k: round(stats.get(k, 0.0), 1)
+                          for k in ("t_launch_ms", "t_gpu_ms", "t_complete_ms")}}
 
 
 def config_dict(W):
@@ -389,6 +391,14 @@ def main():
         print(json.dumps(out), flush=True)
         return
 
+    # --- launch parameters measured on these operands (outside the timing) -
+    from spinifel_gb300 import autotune
+
+    tuned = {"bf16": autotune.tune_bf16(frames, rset),
+             "fp32": autotune.tune_fp32(frames.f32, frames.sq, rset)}
+    for k in tuned:
+        tuned[k].pop("trials", None)
+
     # --- BF16 tensor cores + exact FP32 re-rank (the measured path) ---------
     st_bf = {}
 
@@ -517,7 +527,7 @@ def main():
                "argmin": {"differs_from_plain": n_diff, "non_tie_differences": n_nontie,
                           "identical": n_nontie == 0, "uncertified_frames":
                               st_bf.get("uncertified"), "e2e_equals_device": same_e2e},
-               "serving": serving,
+               "serving": serving, "autotune": tuned,
                "slicing": {"ms_all_refs": slice_ms,
                            "points_per_s": W["n_ref"] * n_pix / (slice_ms / 1e3)},
                "peaks_source": peak_src}

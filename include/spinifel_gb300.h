@@ -47,6 +47,19 @@ int spf_device_error(void *stream, int *h_code);
  * writes d_result[0] = 0 (gave up) / 1, d_result[1] = milliseconds waited. */
 int spf_selftest_bounded_wait(int64_t timeout_ms, int *d_result, void *stream);
 
+/* Runtime tunables, set by the autotuner (spinifel_gb300/autotune.py); 0
+ * restores the built-in default.
+ *   SPF_TUNE_BF16_GROUP_M : image tiles per rasterisation group of the
+ *                           tensor-core kernels (default 16)
+ *   SPF_TUNE_FP32_GROUP_M : the same for the plain FP32 kernels (default 8)
+ *   SPF_TUNE_BF16_GRID    : persistent CTAs of the tensor-core kernels
+ *                           (default: one per SM) */
+#define SPF_TUNE_BF16_GROUP_M 1
+#define SPF_TUNE_FP32_GROUP_M 2
+#define SPF_TUNE_BF16_GRID 3
+int spf_tune_set(int param, int64_t value);
+int spf_tune_get(int param, int64_t *value);
+
 /* ---- NUFFT plan ---------------------------------------------------------
  * Replaces the cufinufft / finufft plans built in
  * spinifel/extern/nufft_ext.py:271-280 (type 2) and :308-319 (type 1).

@@ -25,6 +25,10 @@ SPF_ERR_LAUNCH = -4
 SPF_ERR_CUDA = -5
 SPF_ERR_UNSUPPORTED = -6
 
+SPF_TUNE_BF16_GROUP_M = 1
+SPF_TUNE_FP32_GROUP_M = 2
+SPF_TUNE_BF16_GRID = 3
+
 
 class SpfError(RuntimeError):
     def __init__(self, status: int, where: str, msg: str):
@@ -45,6 +49,8 @@ SIGNATURES = {
     "spf_launch_count": [],
     "spf_device_error": [_c_void_p, ctypes.POINTER(_int)],
     "spf_selftest_bounded_wait": [_i64, _c_void_p, _c_void_p],
+    "spf_tune_set": [_int, _i64],
+    "spf_tune_get": [_int, ctypes.POINTER(_i64)],
     "spf_nufft_plan_create": [_int, _int, _int, _dbl, _dbl, ctypes.POINTER(_c_void_p)],
     "spf_nufft_plan_destroy": [_c_void_p],
     "spf_nufft_plan_info": [_c_void_p, ctypes.POINTER(_int), ctypes.POINTER(_int),

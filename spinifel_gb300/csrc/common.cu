@@ -37,6 +37,14 @@ unsigned int *device_error_word() {
   return g_err_words[dev];
 }
 
+static std::atomic<int64_t> g_tune[16];
+static std::atomic<bool> g_tune_set[16];
+
+int64_t tune_get(int param, int64_t dflt) {
+  if (param <= 0 || param >= 16 || !g_tune_set[param].load()) return dflt;
+  return g_tune[param].load();
+}
+
 int sm_count() {
   static int cached[64] = {0};
   int dev = 0;
@@ -72,6 +80,27 @@ const char *spf_status_string(int status) {
 const char *spf_last_error(void) { return spf::get_error(); }
 
 uint64_t spf_launch_count(void) { return spf::g_launches.load(); }
+
+int spf_tune_set(int param, int64_t value) {
+  SPF_REQUIRE(param >= 1 && param <= 3, "spf_tune_set: unknown parameter %d", param);
+  if (param == SPF_TUNE_BF16_GROUP_M || param == SPF_TUNE_FP32_GROUP_M)
+    SPF_REQUIRE(value >= 0 && value <= 1024, "spf_tune_set: group size out of range");
+  if (param == SPF_TUNE_BF16_GRID)
+    SPF_REQUIRE(value >= 0 && value <= 4096, "spf_tune_set: grid size out of range");
+  if (value == 0) {
+    spf::g_tune_set[param].store(false);
+  } else {
+    spf::g_tune[param].store(value);
+    spf::g_tune_set[param].store(true);
+  }
+  return SPF_OK;
+}
+
+int spf_tune_get(int param, int64_t *value) {
+  SPF_REQUIRE(param >= 1 && param <= 3 && value, "spf_tune_get: bad arguments");
+  *value = spf::tune_get(param, 0);
+  return SPF_OK;
+}
 
 int spf_device_error(void *stream, int *h_code) {
   SPF_REQUIRE(h_code != nullptr, "spf_device_error: h_code is NULL");

@@ -93,4 +93,7 @@ inline int grid_for(int64_t n, int block, int64_t cap = 1 << 30) {
 
 int sm_count();
 
+// Runtime tunables (set by the autotuner through spf_tune_set).
+int64_t tune_get(int param, int64_t dflt);
+
 }  // namespace spf

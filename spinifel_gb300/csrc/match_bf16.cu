@@ -193,12 +193,12 @@ struct TopK {
   }
 };
 
-__device__ __forceinline__ void tile_of(int64_t t, int64_t n_m, int64_t n_n, int64_t &m,
-                                        int64_t &n) {
-  int64_t per_group = (int64_t)GROUP_M * n_n;
+__device__ __forceinline__ void tile_of(int64_t t, int64_t n_m, int64_t n_n, int group_m,
+                                        int64_t &m, int64_t &n) {
+  int64_t per_group = (int64_t)group_m * n_n;
   int64_t g = t / per_group;
-  int64_t first_m = g * GROUP_M;
-  int64_t gm = n_m - first_m < GROUP_M ? n_m - first_m : GROUP_M;
+  int64_t first_m = g * group_m;
+  int64_t gm = n_m - first_m < group_m ? n_m - first_m : group_m;
   int64_t r = t % per_group;
   m = first_m + r % gm;
   n = r / gm;
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                      int64_t n_img, int64_t n_ref, int64_t n_pix, float *__restrict__ cand_d,
                      int32_t *__restrict__ cand_i, const float *__restrict__ thresh,
                      int32_t *__restrict__ list, int32_t *__restrict__ count, int cap,
-                     unsigned int *__restrict__ err) {
+                     int group_m, unsigned int *__restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       bool ok = true;
       for (int64_t t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
         int64_t m, n;
-        tile_of(t, n_m, n_n, m, n);
+        tile_of(t, n_m, n_n, group_m, m, n);
         for (int kb = 0; kb < nkb; ++kb, ++it) {
           int s = it % STAGES;
           uint32_t ph = (it / STAGES) & 1;
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     uint32_t tc = 0;
     for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x, ++tc) {
       int64_t m, n;
-      tile_of(t, n_m, n_n, m, n);
+      tile_of(t, n_m, n_n, group_m, m, n);
       uint32_t b = tc & 1, use = tc >> 1;
       // one lane waits, the warp follows (tcgen05.ld below is warp-collective)
       int ok = 1;
@@ -583,8 +583,13 @@ __global__ void __launch_bounds__(RR_THREADS)
 constexpr int RX_FRAMES = 4;
 constexpr int RX_ROWS = RX_FRAMES * (TOPK + 1);  // 4 frame rows + 32 candidate rows
 constexpr int RX_CHUNK = 256;
-constexpr int RX_STRIDE = RX_CHUNK + 1;
+constexpr int RX_STRIDE = RX_CHUNK + 4;          // 16-byte aligned rows, 4-way banks
 constexpr int RX_THREADS = 128;
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem)
+               : "memory");
+}
 
 __global__ void __launch_bounds__(RX_THREADS)
     k_rerank_exact(const float *__restrict__ cand_d, const int32_t *__restrict__ cand_i,
@@ -594,7 +599,7 @@ __global__ void __launch_bounds__(RX_THREADS)
                    float *__restrict__ work, int32_t *__restrict__ out_idx,
                    float *__restrict__ out_dist, int32_t *__restrict__ uncertified,
                    int32_t *__restrict__ out_top) {
-  extern __shared__ float rx[];  // [2][RX_ROWS][RX_STRIDE]
+  extern __shared__ __align__(16) float rx[];  // [2][RX_ROWS][RX_STRIDE]
   __shared__ const float *rows[RX_ROWS];
   const int tid = threadIdx.x;
   const int64_t f0 = (int64_t)blockIdx.x * RX_FRAMES;
@@ -616,15 +621,25 @@ __global__ void __launch_bounds__(RX_THREADS)
   }
   __syncthreads();
   const int64_t nchunks = (n_pix + RX_CHUNK - 1) / RX_CHUNK;
+  const bool vec = (n_pix % 4) == 0 && aligned(img, 16) && aligned(ref, 16);
+  // asynchronous 16-byte copies of one chunk of every row (ragged ends and
+  // missing rows filled with zeros by plain stores)
   auto stage = [&](int buf, int64_t chunk) {
     float *dst = rx + (size_t)buf * RX_ROWS * RX_STRIDE;
     const int64_t base = chunk * RX_CHUNK;
-    for (int e = tid; e < RX_ROWS * RX_CHUNK; e += RX_THREADS) {
-      int r = e / RX_CHUNK, k = e % RX_CHUNK;
+    for (int e = tid; e < RX_ROWS * (RX_CHUNK / 4); e += RX_THREADS) {
+      int r = e / (RX_CHUNK / 4), q4 = (e % (RX_CHUNK / 4)) * 4;
       const float *src = rows[r];
-      int64_t p = base + k;
-      dst[r * RX_STRIDE + k] = (src && p < n_pix) ? __ldg(src + p) : 0.0f;
+      int64_t p = base + q4;
+      float *d = dst + r * RX_STRIDE + q4;
+      if (src && vec && p + 3 < n_pix) {
+        cp_async16(d, src + p);
+      } else {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) d[u] = (src && p + u < n_pix) ? __ldg(src + p + u) : 0.0f;
+      }
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
   };
   // chain of lane l of warp 0: frame l / 8, candidate l % 8
   const int lane = tid & 31;
@@ -632,9 +647,11 @@ __global__ void __launch_bounds__(RX_THREADS)
   const int crow = RX_FRAMES + lane;
   float acc = 0.0f;
   stage(0, 0);
-  __syncthreads();
   for (int64_t ch = 0; ch < nchunks; ++ch) {
     int cur = (int)(ch & 1);
+    // chunk ch has landed (and is visible to every thread) before use
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
     if (ch + 1 < nchunks) stage(cur ^ 1, ch + 1);
     if (tid < 32) {
       const float *xb = rx + (size_t)cur * RX_ROWS * RX_STRIDE + fr * RX_STRIDE;
@@ -644,8 +661,8 @@ __global__ void __launch_bounds__(RX_THREADS)
 #pragma unroll 8
       for (int k = 0; k < kmax; ++k) acc = fmaf(xb[k], sb[k], acc);
     }
-    __syncthreads();
   }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
   if (tid >= 32) return;
   const int64_t im = f0 + fr;
   const int c = lane % TOPK;
@@ -875,15 +892,17 @@ static int launch_bf16(bool range, const void *d_img_bf16, int64_t n_img, const 
   unsigned int *err = device_error_word();
   SPF_REQUIRE(err != nullptr, "%s: no device error word", name);
   int64_t tiles = ((n_img + BM - 1) / BM) * ((n_ref + BN - 1) / BN);
-  int grid = (int)(tiles < sm_count() ? tiles : sm_count());
+  int64_t max_grid = tune_get(SPF_TUNE_BF16_GRID, sm_count());
+  int grid = (int)(tiles < max_grid ? tiles : max_grid);
+  int group_m = (int)tune_get(SPF_TUNE_BF16_GROUP_M, GROUP_M);
   if (range)
     k_dist_topk_bf16<true><<<grid, THREADS, SMEM_BYTES, as_stream(stream)>>>(
         ma, mb, d_ref_sq, n_img, n_ref, n_pix, nullptr, nullptr, d_thresh, d_list, d_count, cap,
-        err);
+        group_m, err);
   else
     k_dist_topk_bf16<false><<<grid, THREADS, SMEM_BYTES, as_stream(stream)>>>(
         ma, mb, d_ref_sq, n_img, n_ref, n_pix, d_cand_d, d_cand_i, nullptr, nullptr, nullptr, 0,
-        err);
+        group_m, err);
   return check_launch(name);
 }
 
@@ -1099,7 +1118,7 @@ extern "C" int spf_match_bf16_static(const void *d_img_bf16, const float *d_img,
   int grid = (int)(gemm_tiles < sm_count() ? gemm_tiles : sm_count());
   k_dist_topk_bf16<false><<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, d_ref_sq, n_img, n_ref,
                                                             n_pix, cand_d, cand_i, nullptr,
-                                                            nullptr, nullptr, 0, err);
+                                                            nullptr, nullptr, 0, GROUP_M, err);
   SPF_TRY(check_launch("k_dist_topk_bf16 (static scratch)"));
   k_merge_top8<<<(unsigned)n_img, RR_THREADS, 0, s>>>(cand_d, cand_i, tiles, d_img, n_img,
                                                       d_ref_m2, n_pix, work);

@@ -65,13 +65,13 @@ struct TileLoader {
 };
 
 __device__ __forceinline__ void tile_coords(int64_t n_img_tiles, int64_t n_ref_tiles,
-                                            int64_t &mt, int64_t &nt) {
+                                            int group_m, int64_t &mt, int64_t &nt) {
   int64_t bid = blockIdx.x;
-  int64_t per_group = (int64_t)GROUP_M * n_ref_tiles;
+  int64_t per_group = (int64_t)group_m * n_ref_tiles;
   int64_t group = bid / per_group;
-  int64_t first_m = group * GROUP_M;
+  int64_t first_m = group * group_m;
   int64_t gm = n_img_tiles - first_m;
-  if (gm > GROUP_M) gm = GROUP_M;
+  if (gm > group_m) gm = group_m;
   int64_t in = bid % per_group;
   mt = first_m + in % gm;
   nt = in / gm;
@@ -143,13 +143,13 @@ __global__ void __launch_bounds__(TB_THREADS) k_knn_eudist(const T *__restrict__
                                                            const T *__restrict__ data,
                                                            int64_t n_ref, int64_t n_data,
                                                            int64_t ld, int64_t K,
-                                                           T *__restrict__ out) {
+                                                           T *__restrict__ out, int group_m) {
   __shared__ __align__(16) T As[2][TB_K][TB_M + 4];
   __shared__ __align__(16) T Bs[2][TB_K][TB_N + 4];
   int64_t n_img_tiles = (n_data + TB_M - 1) / TB_M;
   int64_t n_ref_tiles = (n_ref + TB_N - 1) / TB_N;
   int64_t mt, nt;
-  tile_coords(n_img_tiles, n_ref_tiles, mt, nt);
+  tile_coords(n_img_tiles, n_ref_tiles, group_m, mt, nt);
   T acc[8][8];
   tile_mainloop<T, Mode::DIFF>(data, n_data, ref, n_ref, ld, K, mt * TB_M, nt * TB_N, acc, As,
                                Bs);
@@ -171,13 +171,13 @@ __global__ void __launch_bounds__(TB_THREADS) k_knn_eudist(const T *__restrict__
 __global__ void __launch_bounds__(TB_THREADS) k_dist_argmin_f32(
     const float *__restrict__ img, const float *__restrict__ img_sq, int64_t n_img,
     const float *__restrict__ ref, const float *__restrict__ ref_sq, int64_t n_ref, int64_t K,
-    int64_t ref_offset, unsigned long long *__restrict__ best) {
+    int64_t ref_offset, unsigned long long *__restrict__ best, int group_m) {
   __shared__ __align__(16) float As[2][TB_K][TB_M + 4];
   __shared__ __align__(16) float Bs[2][TB_K][TB_N + 4];
   int64_t n_img_tiles = (n_img + TB_M - 1) / TB_M;
   int64_t n_ref_tiles = (n_ref + TB_N - 1) / TB_N;
   int64_t mt, nt;
-  tile_coords(n_img_tiles, n_ref_tiles, mt, nt);
+  tile_coords(n_img_tiles, n_ref_tiles, group_m, mt, nt);
   float acc[8][8];
   tile_mainloop<float, Mode::DOT>(img, n_img, ref, n_ref, K, K, mt * TB_M, nt * TB_N, acc, As,
                                   Bs);
@@ -369,8 +369,9 @@ static int knn_eudist(const T *ref, const T *data, int64_t n_ref, int64_t n_data
   int64_t K = (n_pix / 16) * 16;  // the reference kernel drops the ragged tail
   int64_t tiles = ((n_data + TB_M - 1) / TB_M) * ((n_ref + TB_N - 1) / TB_N);
   SPF_REQUIRE(tiles < (1LL << 31), "%s: too many tiles", name);
+  int group_m = (int)tune_get(SPF_TUNE_FP32_GROUP_M, GROUP_M);
   k_knn_eudist<T><<<(unsigned)tiles, TB_THREADS, 0, as_stream(stream)>>>(ref, data, n_ref, n_data,
-                                                                          n_pix, K, out);
+                                                                          n_pix, K, out, group_m);
   return check_launch(name);
 }
 
@@ -466,7 +467,8 @@ int spf_dist_argmin_f32(const float *d_img, const float *d_img_sq, int64_t n_img
   SPF_REQUIRE(tiles < (1LL << 31), "spf_dist_argmin_f32: too many tiles");
   k_dist_argmin_f32<<<(unsigned)tiles, TB_THREADS, 0, as_stream(stream)>>>(
       d_img, d_img_sq, n_img, d_ref, d_ref_sq, n_ref, n_pix, ref_offset,
-      reinterpret_cast<unsigned long long *>(d_best));
+      reinterpret_cast<unsigned long long *>(d_best),
+      (int)tune_get(SPF_TUNE_FP32_GROUP_M, GROUP_M));
   return check_launch("spf_dist_argmin_f32");
 }
 

@@ -62,7 +62,8 @@ class _Slot:
         self.unc = torch.empty(cap, dtype=torch.int32, device=device)
         self.work = torch.empty(cap, dtype=torch.float32, device=device)
         self.host_out = torch.empty(2, cap, dtype=torch.int32).pin_memory()
-        self.event = torch.cuda.Event()
+        self.event = torch.cuda.Event(enable_timing=True)
+        self.t_start = torch.cuda.Event(enable_timing=True)
         self.requests: list[Request] = []
         self.n = 0
         self.bytes = 0
@@ -170,7 +171,9 @@ class OrientationServer:
         return launched
 
     def _launch(self, slot: _Slot):
+        t0 = time.perf_counter()
         with torch.cuda.stream(slot.stream):
+            slot.t_start.record(slot.stream)
             row = 0
             for r in slot.requests:
                 slot.u16[row:row + r.n].copy_(r.frames, non_blocking=True)
@@ -205,22 +208,23 @@ class OrientationServer:
             slot.event.record(slot.stream)
         self.stats["launches"] += 1
         self.stats["frames"] += slot.n
+        self.stats["t_launch_ms"] += (time.perf_counter() - t0) * 1e3
 
     def _complete(self, slot: _Slot):
+        t0 = time.perf_counter()
         n = slot.n
         idx = slot.host_out[0, :n].numpy().copy()
         unc = slot.host_out[1, :n].numpy()
         bad = np.flatnonzero(unc)
         if bad.size:
-            # exact re-match over all references for frames the certificate
-            # could not settle (rare)
+            # certified completion for the frames the top-8 certificate left
+            # open (range query on the tensor cores + exact re-rank of the list)
             with torch.cuda.stream(slot.stream):
-                sel = torch.as_tensor(bad, device=self.device)
-                sub = slot.f32[:n].index_select(0, sel).contiguous()
-                sq = slot.sq[:n].index_select(0, sel).contiguous()
-                tr = matching.BestTracker(int(bad.size), self.device)
-                tr.update_fp32(sub, sq, self.refs.f32, self.refs.sq, 0)
-                i2, _ = tr.result()
+                rows = torch.as_tensor(bad, device=self.device)
+                fs = slot.view(n)
+                thresh = slot.work[:n].index_select(0, rows).contiguous()
+                i2, _ = matching._complete_range(fs, self.refs, rows, thresh, None,
+                                                 _lib.stream_handle(slot.stream))
                 idx[bad] = i2.cpu().numpy()
             self.stats["uncertified"] += int(bad.size)
         now = time.perf_counter()
@@ -232,6 +236,7 @@ class OrientationServer:
             self.completed.append(r)
         self.in_use_bytes -= slot.bytes
         slot.requests, slot.n, slot.bytes = [], 0, 0
+        self.stats["t_complete_ms"] += (time.perf_counter() - t0) * 1e3
 
     def _loop(self):
         torch.cuda.set_device(self.device)
@@ -258,6 +263,7 @@ class OrientationServer:
             still = []
             for slot in self.busy:
                 if slot.event.query():
+                    self.stats["t_gpu_ms"] += slot.t_start.elapsed_time(slot.event)
                     self._complete(slot)
                     with self.lock:
                         self.free.append(slot)

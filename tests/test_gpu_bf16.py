@@ -140,3 +140,29 @@ def test_rerank_distances_bit_identical_to_plain(dev):
     idx, dist = matching.match_bf16(matching.FrameSet(x), matching.ReferenceSet(s))
     pidx, pdist = matching.argmin_fp32(x, s)
     assert torch.equal(idx, pidx) and torch.equal(dist, pdist)
+
+
+def test_autotuner_picks_a_candidate_and_never_changes_results(dev, tmp_path, monkeypatch):
+    from spinifel_gb300 import _lib, autotune, matching
+
+    monkeypatch.setenv("SPF_TUNE_CACHE", str(tmp_path / "tuned.json"))
+    rng = np.random.default_rng(45)
+    refs = rng.random((1500, 1024)).astype(np.float32)
+    imgs = (refs[rng.integers(0, 1500, 400)] + 0.3 * rng.random((400, 1024))).astype(np.float32)
+    fr = matching.FrameSet(torch.as_tensor(imgs, device=dev))
+    rs = matching.ReferenceSet(torch.as_tensor(refs, device=dev))
+    base, _ = matching.match_bf16(fr, rs)
+    try:
+        rec = autotune.tune_bf16(fr, rs, group_sizes=(1, 2, 16), grids=(0, 64))
+        assert rec["group_m"] in (1, 2, 16) and rec["grid"] in (0, 64) and not rec["cached"]
+        assert len(rec["trials"]) == 6
+        for gm, gr in ((1, 64), (2, 0), (16, 0)):
+            _lib.call("spf_tune_set", _lib.SPF_TUNE_BF16_GROUP_M, gm)
+            _lib.call("spf_tune_set", _lib.SPF_TUNE_BF16_GRID, gr)
+            idx, _ = matching.match_bf16(fr, rs)
+            assert torch.equal(idx, base)
+        rec2 = autotune.tune_bf16(fr, rs)
+        assert rec2["cached"] and rec2["group_m"] == rec["group_m"]
+    finally:
+        _lib.call("spf_tune_set", _lib.SPF_TUNE_BF16_GROUP_M, 0)
+        _lib.call("spf_tune_set", _lib.SPF_TUNE_BF16_GRID, 0)
