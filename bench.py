@@ -526,7 +526,9 @@ def main():
                "speedup_vs_plain_fp32": plain_ms / ms,
                "argmin": {"differs_from_plain": n_diff, "non_tie_differences": n_nontie,
                           "identical": n_nontie == 0, "uncertified_frames":
-                              st_bf.get("uncertified"), "e2e_equals_device": same_e2e},
+                              st_bf.get("uncertified"), "range_overflow":
+                              st_bf.get("range_overflow"), "range_max_list":
+                              st_bf.get("range_max_list"), "e2e_equals_device": same_e2e},
                "serving": serving, "autotune": tuned,
                "slicing": {"ms_all_refs": slice_ms,
                            "points_per_s": W["n_ref"] * n_pix / (slice_ms / 1e3)},

@@ -133,6 +133,18 @@ int spf_nufft_interp_spread_det(spf_nufft_plan plan, const float *d_quats, int64
                                 const float *d_ppr, int n_panels, int nx, int ny,
                                 double scale, const float *d_weights, void *stream);
 
+/* Bin-sorted points for repeated type 2 -> type 1 products over a fixed set
+ * of orientation points (the direct merge operator): spf_nufft_sort_orient
+ * places every point o*n_pix + p in its 8^3-cell bin of the padded fine grid
+ * (a counting sort on the device; large bins split into 2048-point work
+ * items) and keeps the order in the plan (allocates; synchronises the
+ * stream once).  spf_nufft_interp_spread_sorted then does the fused
+ * interpolate / weight / spread with each work item's grid box staged in
+ * shared memory.  The points' geometry pointers must stay valid. */
+int spf_nufft_sort_orient(spf_nufft_plan plan, const float *d_quats, int64_t n_orient,
+                          const float *d_ppr, int64_t n_pix, double scale, void *stream);
+int spf_nufft_interp_spread_sorted(spf_nufft_plan plan, const float *d_weights, void *stream);
+
 /* Fused type 2 -> type 1 at orientation points (the direct A^H D A product):
  * every point interpolates Re of the type-2 fine grid set by
  * spf_nufft_t2_set_modes, multiplies by d_weights[o*n_pix+p] (NULL = 1) and
@@ -208,8 +220,9 @@ int spf_merge_destroy(spf_merge merge);
 int spf_merge_info(spf_merge merge, int *fft_size);
 int spf_merge_set_kernel(spf_merge merge, const float *d_ugrid_conv, int M_ups,
                          void *stream);
-/* det_panels/det_nx/det_ny > 0 select the patch kernels for a multi-panel
- * detector (n_pix = their product); 0 treats the pixels as an unordered list. */
+/* The points are bin-sorted once here (spf_nufft_sort_orient) and every
+ * direct-form product uses the sorted kernel; det_panels/det_nx/det_ny
+ * describe a multi-panel detector (n_pix = their product, 0 = unordered). */
 int spf_merge_set_direct(spf_merge merge, spf_nufft_plan plan, const float *d_quats,
                          int64_t n_orient, const float *d_ppr, int64_t n_pix, int det_panels,
                          int det_nx, int det_ny, double coord_scale, const float *d_weights);

@@ -57,6 +57,7 @@ struct spf_merge_s {
   const float *quats = nullptr, *ppr = nullptr, *weights = nullptr;
   int64_t n_orient = 0, n_pix = 0;
   int det[3] = {0, 0, 0};
+  bool sorted = false;
   double coord_scale = 0;
 };
 
@@ -73,6 +74,9 @@ extern "C" int spf_nufft_interp_spread_orient(spf_nufft_plan_s *, const float *,
 extern "C" int spf_nufft_interp_spread_det(spf_nufft_plan_s *, const float *, int64_t,
                                            const float *, int, int, int, double, const float *,
                                            void *);
+extern "C" int spf_nufft_sort_orient(spf_nufft_plan_s *, const float *, int64_t, const float *,
+                                     int64_t, double, void *);
+extern "C" int spf_nufft_interp_spread_sorted(spf_nufft_plan_s *, const float *, void *);
 
 namespace spf {
 namespace cg {
@@ -341,7 +345,9 @@ static int apply_operator_core(spf_merge_s *G, bool direct, cudaStream_t s) {
   } else {
     SPF_TRY(spf_nufft_t2_set_modes(G->nufft, G->modes, nullptr, -1, 0, s));
     SPF_TRY(spf_nufft_t1_zero(G->nufft, s));
-    if (G->det[0] > 0)
+    if (G->sorted)
+      SPF_TRY(spf_nufft_interp_spread_sorted(G->nufft, G->weights, s));
+    else if (G->det[0] > 0)
       SPF_TRY(spf_nufft_interp_spread_det(G->nufft, G->quats, G->n_orient, G->ppr, G->det[0],
                                           G->det[1], G->det[2], G->coord_scale, G->weights, s));
     else
@@ -489,6 +495,10 @@ int spf_merge_set_direct(spf_merge_s *G, spf_nufft_plan_s *plan, const float *d_
   G->n_orient = n_orient;
   G->n_pix = n_pix;
   G->coord_scale = coord_scale;
+  // the points are fixed for the solve: sort them by fine-grid bin once
+  G->sorted = false;
+  SPF_TRY(spf_nufft_sort_orient(plan, d_quats, n_orient, d_ppr, n_pix, coord_scale, nullptr));
+  G->sorted = true;
   return SPF_OK;
 }
 

@@ -411,10 +411,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 // device usable).
 __global__ void k_wait_selftest(uint64_t timeout_ns, unsigned int *err, int *result) {
   __shared__ __align__(8) uint64_t bar;
-  __shared__ int abort;
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
-    abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -715,39 +713,93 @@ constexpr size_t RX_SMEM = 2 * RX_ROWS * RX_STRIDE * sizeof(float);
 
 // Exact FP32 distances (plain-path arithmetic) for every listed candidate of
 // every frame; the per-frame lexicographic minimum is folded into best[]
-// (packed order key << 32 | index, as spf_dist_argmin_f32 keeps it).
-__global__ void __launch_bounds__(RR_THREADS)
+// (packed order key << 32 | index, as spf_dist_argmin_f32 keeps it).  A CTA
+// takes one frame and walks its list 32 candidates at a time: all warps
+// stream the frame row and the 32 candidate rows through shared memory in
+// 256-pixel chunks (cp.async, double-buffered) while warp 0 runs the 32
+// sequential FMA chains.
+constexpr int RL_ROWS = 33;
+
+__global__ void __launch_bounds__(RX_THREADS)
     k_rerank_list(const int32_t *__restrict__ list, const int32_t *__restrict__ count, int cap,
                   const float *__restrict__ img, const float *__restrict__ img_sq, int64_t n_img,
                   const float *__restrict__ ref, const float *__restrict__ ref_sq, int64_t n_pix,
                   int64_t ref_offset, unsigned long long *__restrict__ best) {
-  const int64_t gt = blockIdx.x * (int64_t)RR_THREADS + threadIdx.x;
-  const int64_t im = gt / cap;
-  const int c = (int)(gt % cap);
+  extern __shared__ __align__(16) float rx[];  // [2][RL_ROWS][RX_STRIDE]
+  __shared__ const float *rows[RL_ROWS];
+  const int64_t im = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31;
   if (im >= n_img) return;
   int cnt = count[im];
-  if (c >= cnt || c >= cap) return;
-  int32_t j = list[im * cap + c];
-  const float *x = img + im * n_pix;
-  const float *sr = ref + (int64_t)j * n_pix;
-  float acc = 0.0f;
-  int64_t p = 0;
-  if ((n_pix & 3) == 0 && aligned(x, 16) && aligned(sr, 16)) {
-    for (; p < n_pix; p += 4) {
-      float4 a = *reinterpret_cast<const float4 *>(x + p);
-      float4 b = __ldg(reinterpret_cast<const float4 *>(sr + p));
-      acc = fmaf(a.x, b.x, acc);
-      acc = fmaf(a.y, b.y, acc);
-      acc = fmaf(a.z, b.z, acc);
-      acc = fmaf(a.w, b.w, acc);
+  if (cnt > cap) cnt = cap;
+  const int64_t nchunks = (n_pix + RX_CHUNK - 1) / RX_CHUNK;
+  const bool vec = (n_pix % 4) == 0 && aligned(img, 16) && aligned(ref, 16);
+  unsigned long long kbest = ~0ULL;
+  for (int g0 = 0; g0 < cnt; g0 += 32) {
+    __syncthreads();  // the previous group is done with rows[] and the buffers
+    if (tid < RL_ROWS) {
+      const float *ptr = nullptr;
+      if (tid == 0) {
+        ptr = img + im * n_pix;
+      } else if (g0 + tid - 1 < cnt) {
+        ptr = ref + (int64_t)list[im * cap + g0 + tid - 1] * n_pix;
+      }
+      rows[tid] = ptr;
+    }
+    __syncthreads();
+    auto stage = [&](int buf, int64_t chunk) {
+      float *dst = rx + (size_t)buf * RL_ROWS * RX_STRIDE;
+      const int64_t base = chunk * RX_CHUNK;
+      for (int e = tid; e < RL_ROWS * (RX_CHUNK / 4); e += RX_THREADS) {
+        int r = e / (RX_CHUNK / 4), q4 = (e % (RX_CHUNK / 4)) * 4;
+        const float *src = rows[r];
+        int64_t p = base + q4;
+        float *d = dst + r * RX_STRIDE + q4;
+        if (src && vec && p + 3 < n_pix) {
+          cp_async16(d, src + p);
+        } else {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) d[u] = (src && p + u < n_pix) ? __ldg(src + p + u) : 0.0f;
+        }
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    float acc = 0.0f;
+    stage(0, 0);
+    for (int64_t ch = 0; ch < nchunks; ++ch) {
+      int cur = (int)(ch & 1);
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      __syncthreads();
+      if (ch + 1 < nchunks) stage(cur ^ 1, ch + 1);
+      if (tid < 32) {
+        const float *xb = rx + (size_t)cur * RL_ROWS * RX_STRIDE;
+        const float *sb = xb + (1 + lane) * RX_STRIDE;
+        int64_t lim = n_pix - ch * RX_CHUNK;
+        int kmax = lim < RX_CHUNK ? (int)lim : RX_CHUNK;
+#pragma unroll 8
+        for (int k = 0; k < kmax; ++k) acc = fmaf(xb[k], sb[k], acc);
+      }
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    if (tid < 32 && g0 + lane < cnt) {
+      int32_t j = list[im * cap + g0 + lane];
+      float dist = __fsub_rn(__fadd_rn(img_sq[im], ref_sq[j]), __fmul_rn(2.0f, acc));
+      unsigned long long key =
+          ((unsigned long long)float_key(dist) << 32) | (unsigned long long)(j + ref_offset);
+      kbest = key < kbest ? key : kbest;
     }
   }
-  for (; p < n_pix; ++p) acc = fmaf(x[p], __ldg(sr + p), acc);
-  float dist = __fsub_rn(__fadd_rn(img_sq[im], ref_sq[j]), __fmul_rn(2.0f, acc));
-  unsigned long long key =
-      ((unsigned long long)float_key(dist) << 32) | (unsigned long long)(j + ref_offset);
-  atomicMin(best + im, key);
+  if (tid < 32) {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+      unsigned long long other = __shfl_xor_sync(0xffffffffu, kbest, o);
+      kbest = other < kbest ? other : kbest;
+    }
+    if (lane == 0 && kbest != ~0ULL) atomicMin(best + im, kbest);
+  }
 }
+
+constexpr size_t RL_SMEM = 2 * RL_ROWS * RX_STRIDE * sizeof(float);
 
 // column maxima of squares: out[p] = max_r x[r, p]^2
 __global__ void k_col_maxsq(const float *__restrict__ x, int64_t n_rows, int64_t n_pix,
@@ -939,12 +991,20 @@ int spf_rerank_list_fp32(const int32_t *d_list, const int32_t *d_count, int cap,
   if (n_img == 0) return SPF_OK;
   SPF_REQUIRE(d_list && d_count && d_img && d_img_sq && d_ref && d_ref_sq && d_best,
               "spf_rerank_list_fp32: NULL pointer");
-  int64_t threads = n_img * (int64_t)cap;
-  SPF_REQUIRE(threads / RR_THREADS < (1LL << 31), "spf_rerank_list_fp32: too large");
-  k_rerank_list<<<(unsigned)((threads + RR_THREADS - 1) / RR_THREADS), RR_THREADS, 0,
-                  as_stream(stream)>>>(d_list, d_count, cap, d_img, d_img_sq, n_img, d_ref,
-                                       d_ref_sq, n_pix, ref_offset,
-                                       reinterpret_cast<unsigned long long *>(d_best));
+  SPF_REQUIRE(n_img < (1LL << 31), "spf_rerank_list_fp32: too many frames");
+  static bool attr[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !attr[dev]) {
+    SPF_TRY(check_cuda(cudaFuncSetAttribute(k_rerank_list,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)RL_SMEM),
+                       "spf_rerank_list_fp32"));
+    attr[dev] = true;
+  }
+  k_rerank_list<<<(unsigned)n_img, RX_THREADS, RL_SMEM, as_stream(stream)>>>(
+      d_list, d_count, cap, d_img, d_img_sq, n_img, d_ref, d_ref_sq, n_pix, ref_offset,
+      reinterpret_cast<unsigned long long *>(d_best));
   return check_launch("k_rerank_list");
 }
 

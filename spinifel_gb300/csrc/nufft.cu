@@ -34,6 +34,14 @@ struct spf_nufft_plan_s {
   float *acc_pad = nullptr;
   cufftHandle fft = 0;
   bool fft_ok = false;
+  // bin-sorted orientation points (spf_nufft_sort_orient)
+  int32_t *sorted = nullptr;   // point indices o * n_pix + p, grouped by bin
+  int4 *items = nullptr;       // (bin, start, count, 0) work items
+  int64_t n_items = 0, n_sorted = 0, sorted_cap = 0, items_cap = 0;
+  int nb[3] = {0, 0, 0};
+  const float *s_quats = nullptr, *s_ppr = nullptr;
+  int64_t s_n_orient = 0, s_n_pix = 0;
+  double s_scale = 0;
 };
 
 namespace spf {
@@ -144,14 +152,18 @@ __device__ __forceinline__ float es_eval(float z, float beta) {
   return expf(beta * (sqrtf(s) - 1.0f));
 }
 
-// Padded first index and the W weights along one axis for fine-grid
-// coordinate t (already scaled to grid units).
+// Padded first index and the W weights along one axis for the point at
+// x (in units of the coordinate scale) with grid scale s: t = x s in grid
+// units, wrapped into [-n/2, n/2).  The index arithmetic uses explicitly
+// rounded operations (no contraction), so every kernel that places a point
+// computes the same cell for it.
 template <int W>
-__device__ __forceinline__ int axis_setup(float t, int n, int off, float beta, float inv_half_w,
-                                          float *wt) {
+__device__ __forceinline__ int axis_setup(float x, float s, int n, int off, float beta,
+                                          float inv_half_w, float *wt) {
   float fn = (float)n;
-  t = t - fn * floorf(t / fn + 0.5f);  // [-n/2, n/2)
-  float l0 = ceilf(t - 0.5f * W);
+  float t = __fmul_rn(x, s);
+  t = __fsub_rn(t, __fmul_rn(fn, floorf(__fadd_rn(__fdiv_rn(t, fn), 0.5f))));
+  float l0 = ceilf(__fsub_rn(t, 0.5f * W));
 #pragma unroll
   for (int a = 0; a < W; ++a) {
     float z = (l0 + (float)a - t) * inv_half_w;
@@ -162,11 +174,12 @@ __device__ __forceinline__ int axis_setup(float t, int n, int off, float beta, f
 
 template <int W>
 __device__ __forceinline__ float interp_point(const float *__restrict__ grid, const GridGeom &g,
-                                              float t1, float t2, float t3) {
+                                              float x1, float s1, float x2, float s2, float x3,
+                                              float s3) {
   float w1[W], w2[W], w3[W];
-  int i0 = axis_setup<W>(t1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
-  int j0 = axis_setup<W>(t2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
-  int k0 = axis_setup<W>(t3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
+  int i0 = axis_setup<W>(x1, s1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
+  int j0 = axis_setup<W>(x2, s2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
+  int k0 = axis_setup<W>(x3, s3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
   float acc = 0.0f;
 #pragma unroll
   for (int a = 0; a < W; ++a) {
@@ -185,12 +198,13 @@ __device__ __forceinline__ float interp_point(const float *__restrict__ grid, co
 }
 
 template <int W>
-__device__ __forceinline__ void spread_point(float *__restrict__ grid, const GridGeom &g, float t1,
-                                             float t2, float t3, float c) {
+__device__ __forceinline__ void spread_point(float *__restrict__ grid, const GridGeom &g, float x1,
+                                             float s1, float x2, float s2, float x3, float s3,
+                                             float c) {
   float w1[W], w2[W], w3[W];
-  int i0 = axis_setup<W>(t1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
-  int j0 = axis_setup<W>(t2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
-  int k0 = axis_setup<W>(t3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
+  int i0 = axis_setup<W>(x1, s1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
+  int j0 = axis_setup<W>(x2, s2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
+  int k0 = axis_setup<W>(x3, s3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
 #pragma unroll
   for (int c3 = 0; c3 < W; ++c3) w3[c3] *= c;
 #pragma unroll
@@ -216,10 +230,10 @@ __device__ __forceinline__ void rotate_inv(const float *__restrict__ quat, float
         r12 = 2.f * (q2 * q3 - q0 * q1);
   float r20 = 2.f * (q1 * q3 - q0 * q2), r21 = 2.f * (q2 * q3 + q0 * q1),
         r22 = 1.f - 2.f * (q1 * q1 + q2 * q2);
-  // R^-1 = R^T for a unit quaternion
-  h = s * (r00 * qx + r10 * qy + r20 * qz);
-  k = s * (r01 * qx + r11 * qy + r21 * qz);
-  l = s * (r02 * qx + r12 * qy + r22 * qz);
+  // R^-1 = R^T for a unit quaternion (explicitly rounded: no contraction)
+  h = __fmul_rn(s, __fadd_rn(__fadd_rn(__fmul_rn(r00, qx), __fmul_rn(r10, qy)), __fmul_rn(r20, qz)));
+  k = __fmul_rn(s, __fadd_rn(__fadd_rn(__fmul_rn(r01, qx), __fmul_rn(r11, qy)), __fmul_rn(r21, qz)));
+  l = __fmul_rn(s, __fadd_rn(__fadd_rn(__fmul_rn(r02, qx), __fmul_rn(r12, qy)), __fmul_rn(r22, qz)));
 }
 
 // ---------------------------------------------------------------------------
@@ -274,9 +288,8 @@ __global__ void k_t2_interp(const float *__restrict__ re_pad, const float *__res
               sc3 = g.n3 * (float)(0.5 / M_PI);
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < npts;
        j += (int64_t)gridDim.x * blockDim.x) {
-    float t1 = x[j] * sc1, t2 = y[j] * sc2, t3 = z[j] * sc3;
-    out_re[j] = interp_point<W>(re_pad, g, t1, t2, t3);
-    if (out_im) out_im[j] = interp_point<W>(im_pad, g, t1, t2, t3);
+    out_re[j] = interp_point<W>(re_pad, g, x[j], sc1, y[j], sc2, z[j], sc3);
+    if (out_im) out_im[j] = interp_point<W>(im_pad, g, x[j], sc1, y[j], sc2, z[j], sc3);
   }
 }
 
@@ -290,7 +303,7 @@ __global__ void k_slice_t2(const float *__restrict__ re_pad, GridGeom g,
   if (p >= n_pix) return;
   float h, k, l;
   rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
-  float v = interp_point<W>(re_pad, g, h * scale1, k * scale2, l * scale3);
+  float v = interp_point<W>(re_pad, g, h, scale1, k, scale2, l, scale3);
   int64_t idx = o * n_pix + p;
   out[idx] = v;
   if (out_bf16) out_bf16[idx] = __float2bfloat16_rn(v);
@@ -330,9 +343,9 @@ __global__ void __launch_bounds__(256)
   float h, k, l;
   rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
   float w1[W], w2[W], w3[W];
-  int i0 = axis_setup<W>(h * scale1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
-  int j0 = axis_setup<W>(k * scale2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
-  int k0 = axis_setup<W>(l * scale3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
+  int i0 = axis_setup<W>(h, scale1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
+  int j0 = axis_setup<W>(k, scale2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
+  int k0 = axis_setup<W>(l, scale3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
   {
     int mi = valid ? i0 : INT32_MAX, mj = valid ? j0 : INT32_MAX, mk = valid ? k0 : INT32_MAX;
     int xi = valid ? i0 : INT32_MIN, xj = valid ? j0 : INT32_MIN, xk = valid ? k0 : INT32_MIN;
@@ -428,9 +441,9 @@ __device__ __forceinline__ PatchPoint patch_point(const GridGeom &g, const float
   pt.p = ((int64_t)panel * nx + (pt.valid ? px : 0)) * ny + (pt.valid ? py : 0);
   float h, k, l;
   rotate_inv(quat, ppr[pt.p], ppr[n_pix + pt.p], ppr[2 * n_pix + pt.p], 1.0f, h, k, l);
-  pt.i0 = axis_setup<W>(h * s1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
-  pt.j0 = axis_setup<W>(k * s2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
-  pt.k0 = axis_setup<W>(l * s3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
+  pt.i0 = axis_setup<W>(h, s1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
+  pt.j0 = axis_setup<W>(k, s2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
+  pt.k0 = axis_setup<W>(l, s3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
   return pt;
 }
 
@@ -565,7 +578,7 @@ __global__ void k_t1_spread(float *__restrict__ acc_pad, GridGeom g, const float
        j += (int64_t)gridDim.x * blockDim.x) {
     float cj = c[j];
     if (cj == 0.0f) continue;
-    spread_point<W>(acc_pad, g, x[j] * sc1, y[j] * sc2, z[j] * sc3, cj);
+    spread_point<W>(acc_pad, g, x[j], sc1, y[j], sc2, z[j], sc3, cj);
   }
 }
 
@@ -581,7 +594,7 @@ __global__ void k_t1_spread_orient(float *__restrict__ acc_pad, GridGeom g,
   if (cj == 0.0f) return;
   float h, k, l;
   rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
-  spread_point<W>(acc_pad, g, h * scale1, k * scale2, l * scale3, cj);
+  spread_point<W>(acc_pad, g, h, scale1, k, scale2, l, scale3, cj);
 }
 
 // Fused type 2 -> type 1 at the same points (the direct A^H D A operator):
@@ -600,9 +613,9 @@ __global__ void k_interp_spread_orient(const float *__restrict__ re_pad,
   float h, k, l;
   rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
   float w1[W], w2[W], w3[W];
-  int i0 = axis_setup<W>(h * scale1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
-  int j0 = axis_setup<W>(k * scale2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
-  int k0 = axis_setup<W>(l * scale3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
+  int i0 = axis_setup<W>(h, scale1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
+  int j0 = axis_setup<W>(k, scale2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
+  int k0 = axis_setup<W>(l, scale3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
   float acc = 0.0f;
 #pragma unroll
   for (int a = 0; a < W; ++a) {
@@ -629,6 +642,156 @@ __global__ void k_interp_spread_orient(const float *__restrict__ re_pad,
       float *row = acc_pad + ((size_t)(i0 + a) * g.p2 + (j0 + b)) * g.p3 + k0;
 #pragma unroll
       for (int c = 0; c < W; ++c) atomicAdd(row + c, wab * w3[c]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// bin-sorted points: 8^3-cell bins of the padded grid
+// ---------------------------------------------------------------------------
+constexpr int BIN = 8;
+constexpr int BIN_CHUNK = 2048;  // points per work item (big bins are split)
+
+template <int W>
+__device__ __forceinline__ int point_bin(const GridGeom &g, const int *nb, float h, float k, float l,
+                                         float s1, float s2, float s3) {
+  float w[W];
+  int i0 = axis_setup<W>(h, s1, g.n1, g.off1, g.beta, g.inv_half_w, w);
+  int j0 = axis_setup<W>(k, s2, g.n2, g.off2, g.beta, g.inv_half_w, w);
+  int k0 = axis_setup<W>(l, s3, g.n3, g.off3, g.beta, g.inv_half_w, w);
+  return ((i0 / BIN) * nb[1] + (j0 / BIN)) * nb[2] + (k0 / BIN);
+}
+
+struct BinDims {
+  int nb[3];
+};
+
+template <int W>
+__global__ void k_bin_count(GridGeom g, BinDims bd, const float *__restrict__ quats,
+                            const float *__restrict__ ppr, int64_t n_orient, int64_t n_pix,
+                            float s1, float s2, float s3, int32_t *__restrict__ bin_of,
+                            int32_t *__restrict__ counts) {
+  const int64_t n = n_orient * n_pix;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t o = i / n_pix, p = i % n_pix;
+    float h, k, l;
+    rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
+    int b = point_bin<W>(g, bd.nb, h, k, l, s1, s2, s3);
+    bin_of[i] = b;
+    atomicAdd(counts + b, 1);
+  }
+}
+
+// exclusive prefix sum of n ints, one block of 1024 threads
+__global__ void __launch_bounds__(1024) k_scan(const int32_t *__restrict__ in, int64_t n,
+                                               int32_t *__restrict__ out) {
+  __shared__ int32_t part[1024];
+  const int t = threadIdx.x;
+  const int64_t per = (n + 1023) / 1024;
+  const int64_t lo = t * per, hi = lo + per < n ? lo + per : n;
+  int32_t s = 0;
+  for (int64_t i = lo; i < hi; ++i) s += in[i];
+  part[t] = s;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    int32_t v = t >= off ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  int32_t run = t > 0 ? part[t - 1] : 0;
+  for (int64_t i = lo; i < hi; ++i) {
+    out[i] = run;
+    run += in[i];
+  }
+}
+
+__global__ void k_bin_scatter(const int32_t *__restrict__ bin_of, int64_t n,
+                              const int32_t *__restrict__ offsets, int32_t *__restrict__ cursor,
+                              int32_t *__restrict__ sorted) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int b = bin_of[i];
+    int pos = atomicAdd(cursor + b, 1);
+    sorted[offsets[b] + pos] = (int32_t)i;
+  }
+}
+
+// One work item (a bin, or a chunk of a big bin): stage the bin's box of the
+// type-2 grid, interpolate every point, weight it, spread it into a shared
+// box, and add the box to the type-1 accumulator.
+template <int W>
+__global__ void __launch_bounds__(256)
+    k_interp_spread_sorted(const float *__restrict__ re_pad, float *__restrict__ acc_pad,
+                           GridGeom g, BinDims bd, const int4 *__restrict__ items,
+                           const int32_t *__restrict__ sorted, const float *__restrict__ quats,
+                           const float *__restrict__ ppr, int64_t n_pix, float s1, float s2,
+                           float s3, const float *__restrict__ weights,
+                           unsigned int *__restrict__ err) {
+  constexpr int D = BIN + W - 1;
+  __shared__ float tbox[D * D * D];
+  __shared__ float abox[D * D * D];
+  const int4 it = items[blockIdx.x];
+  const int b = it.x;
+  const int bi = b / (bd.nb[1] * bd.nb[2]), bj = (b / bd.nb[2]) % bd.nb[1], bk = b % bd.nb[2];
+  const int i0b = bi * BIN, j0b = bj * BIN, k0b = bk * BIN;
+  const int di = min(D, g.p1 - i0b), dj = min(D, g.p2 - j0b), dk = min(D, g.p3 - k0b);
+  const int vol = di * dj * dk;
+  for (int idx = threadIdx.x; idx < vol; idx += blockDim.x) {
+    int kk = idx % dk, jj = (idx / dk) % dj, ii = idx / (dk * dj);
+    tbox[idx] = __ldg(re_pad + ((size_t)(i0b + ii) * g.p2 + (j0b + jj)) * g.p3 + k0b + kk);
+    abox[idx] = 0.0f;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < it.z; q += blockDim.x) {
+    const int32_t pi = sorted[it.y + q];
+    const int64_t o = pi / n_pix, p = pi % n_pix;
+    float h, k, l;
+    rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
+    float w1[W], w2[W], w3[W];
+    const int li = axis_setup<W>(h, s1, g.n1, g.off1, g.beta, g.inv_half_w, w1) - i0b;
+    const int lj = axis_setup<W>(k, s2, g.n2, g.off2, g.beta, g.inv_half_w, w2) - j0b;
+    const int lk = axis_setup<W>(l, s3, g.n3, g.off3, g.beta, g.inv_half_w, w3) - k0b;
+    // the sort placed this point in this bin with the same arithmetic; a
+    // point outside the box would be a defect: record it and skip the point
+    if (li < 0 || lj < 0 || lk < 0 || li + W > di || lj + W > dj || lk + W > dk) {
+      if (err) atomicExch(err, (unsigned int)(-SPF_ERR_CUDA));
+      continue;
+    }
+    float v = 0.0f;
+#pragma unroll
+    for (int a = 0; a < W; ++a) {
+      float acc_a = 0.0f;
+#pragma unroll
+      for (int c2 = 0; c2 < W; ++c2) {
+        const float *row = tbox + ((li + a) * dj + (lj + c2)) * dk + lk;
+        float r = 0.0f;
+#pragma unroll
+        for (int c = 0; c < W; ++c) r = fmaf(w3[c], row[c], r);
+        acc_a = fmaf(w2[c2], r, acc_a);
+      }
+      v = fmaf(w1[a], acc_a, v);
+    }
+    if (weights) v *= weights[pi];
+    if (v == 0.0f) continue;
+#pragma unroll
+    for (int a = 0; a < W; ++a) {
+#pragma unroll
+      for (int c2 = 0; c2 < W; ++c2) {
+        float wab = w1[a] * w2[c2] * v;
+        float *row = abox + ((li + a) * dj + (lj + c2)) * dk + lk;
+#pragma unroll
+        for (int c = 0; c < W; ++c) atomicAdd(row + c, wab * w3[c]);
+      }
+    }
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < vol; idx += blockDim.x) {
+    float bv = abox[idx];
+    if (bv != 0.0f) {
+      int kk = idx % dk, jj = (idx / dk) % dj, ii = idx / (dk * dj);
+      atomicAdd(acc_pad + ((size_t)(i0b + ii) * g.p2 + (j0b + jj)) * g.p3 + k0b + kk, bv);
     }
   }
 }
@@ -798,6 +961,8 @@ int spf_nufft_plan_destroy(spf_nufft_plan P) {
   cudaFree(P->re_pad);
   cudaFree(P->im_pad);
   cudaFree(P->acc_pad);
+  cudaFree(P->sorted);
+  cudaFree(P->items);
   if (P->fft_ok) cufftDestroy(P->fft);
   if (prev != P->dev && prev >= 0) cudaSetDevice(prev);
   delete P;
@@ -999,6 +1164,108 @@ int spf_nufft_interp_spread_det(spf_nufft_plan P, const float *d_quats, int64_t 
                                 const float *d_weights, void *stream) {
   return spread_det(P, true, d_quats, n_orient, d_ppr, n_panels, nx, ny, scale, d_weights, stream,
                     "spf_nufft_interp_spread_det");
+}
+
+int spf_nufft_sort_orient(spf_nufft_plan P, const float *d_quats, int64_t n_orient,
+                          const float *d_ppr, int64_t n_pix, double scale, void *stream) {
+  SPF_TRY(check_plan(P, "spf_nufft_sort_orient"));
+  SPF_REQUIRE(n_orient >= 0 && n_pix >= 0, "spf_nufft_sort_orient: negative size");
+  SPF_REQUIRE(d_quats && d_ppr, "spf_nufft_sort_orient: NULL pointer");
+  const int64_t n = n_orient * n_pix;
+  SPF_REQUIRE(n < (1LL << 31), "spf_nufft_sort_orient: more than 2^31 points");
+  cudaStream_t s = as_stream(stream);
+  GridGeom g = geom_of(P);
+  BinDims bd;
+  for (int d = 0; d < 3; ++d) bd.nb[d] = P->nb[d] = (P->np[d] + BIN - 1) / BIN;
+  const int64_t n_bins = (int64_t)bd.nb[0] * bd.nb[1] * bd.nb[2];
+  float s1 = (float)(scale * P->n[0] / (2.0 * M_PI));
+  float s2 = (float)(scale * P->n[1] / (2.0 * M_PI));
+  float s3 = (float)(scale * P->n[2] / (2.0 * M_PI));
+  // temporaries
+  int32_t *bin_of = nullptr, *counts = nullptr, *offsets = nullptr, *cursor = nullptr;
+  int st = check_cuda(cudaMalloc(&bin_of, (n > 0 ? n : 1) * sizeof(int32_t)), "sort_orient");
+  if (st == SPF_OK) st = check_cuda(cudaMalloc(&counts, n_bins * 3 * sizeof(int32_t)), "sort_orient");
+  if (st == SPF_OK && n > P->sorted_cap) {
+    cudaFree(P->sorted);
+    P->sorted = nullptr;
+    st = check_cuda(cudaMalloc(&P->sorted, n * sizeof(int32_t)), "sort_orient");
+    if (st == SPF_OK) P->sorted_cap = n;
+  }
+  if (st == SPF_OK) {
+    offsets = counts + n_bins;
+    cursor = counts + 2 * n_bins;
+    cudaMemsetAsync(counts, 0, n_bins * 3 * sizeof(int32_t), s);
+    int grid = grid_for(n, 256, (int64_t)sm_count() * 16);
+    SPF_W_DISPATCH(P->w, (k_bin_count<W><<<grid, 256, 0, s>>>(g, bd, d_quats, d_ppr, n_orient,
+                                                                 n_pix, s1, s2, s3, bin_of,
+                                                                 counts)));
+    st = check_launch("k_bin_count");
+  }
+  if (st == SPF_OK) {
+    k_scan<<<1, 1024, 0, s>>>(counts, n_bins, offsets);
+    st = check_launch("k_scan");
+  }
+  if (st == SPF_OK) {
+    k_bin_scatter<<<grid_for(n, 256, (int64_t)sm_count() * 16), 256, 0, s>>>(bin_of, n, offsets,
+                                                                            cursor, P->sorted);
+    st = check_launch("k_bin_scatter");
+  }
+  // work items: every non-empty bin, big bins split into BIN_CHUNK points
+  std::vector<int32_t> h_counts, h_offsets;
+  if (st == SPF_OK) {
+    h_counts.resize(n_bins);
+    h_offsets.resize(n_bins);
+    st = check_cuda(cudaMemcpyAsync(h_counts.data(), counts, n_bins * sizeof(int32_t),
+                                    cudaMemcpyDeviceToHost, s), "sort_orient");
+    if (st == SPF_OK)
+      st = check_cuda(cudaMemcpyAsync(h_offsets.data(), offsets, n_bins * sizeof(int32_t),
+                                      cudaMemcpyDeviceToHost, s), "sort_orient");
+    if (st == SPF_OK) st = check_cuda(cudaStreamSynchronize(s), "sort_orient");
+  }
+  cudaFree(bin_of);
+  cudaFree(counts);
+  if (st != SPF_OK) return st;
+  std::vector<int4> h_items;
+  for (int64_t b = 0; b < n_bins; ++b)
+    for (int32_t c = 0; c < h_counts[b]; c += BIN_CHUNK)
+      h_items.push_back(make_int4((int)b, h_offsets[b] + c,
+                                  h_counts[b] - c < BIN_CHUNK ? h_counts[b] - c : BIN_CHUNK, 0));
+  if ((int64_t)h_items.size() > P->items_cap) {
+    cudaFree(P->items);
+    P->items = nullptr;
+    SPF_TRY(check_cuda(cudaMalloc(&P->items, (h_items.size() + 1) * sizeof(int4)), "sort_orient"));
+    P->items_cap = (int64_t)h_items.size();
+  }
+  if (!h_items.empty())
+    SPF_TRY(check_cuda(cudaMemcpy(P->items, h_items.data(), h_items.size() * sizeof(int4),
+                                  cudaMemcpyHostToDevice), "sort_orient"));
+  P->n_items = (int64_t)h_items.size();
+  P->n_sorted = n;
+  P->s_quats = d_quats;
+  P->s_ppr = d_ppr;
+  P->s_n_orient = n_orient;
+  P->s_n_pix = n_pix;
+  P->s_scale = scale;
+  return SPF_OK;
+}
+
+int spf_nufft_interp_spread_sorted(spf_nufft_plan P, const float *d_weights, void *stream) {
+  SPF_TRY(check_plan(P, "spf_nufft_interp_spread_sorted"));
+  SPF_REQUIRE(P->sorted != nullptr && P->n_sorted > 0 || P->n_items == 0,
+              "spf_nufft_interp_spread_sorted: call spf_nufft_sort_orient first");
+  if (P->n_items == 0) return SPF_OK;
+  cudaStream_t s = as_stream(stream);
+  GridGeom g = geom_of(P);
+  BinDims bd;
+  for (int d = 0; d < 3; ++d) bd.nb[d] = P->nb[d];
+  float s1 = (float)(P->s_scale * P->n[0] / (2.0 * M_PI));
+  float s2 = (float)(P->s_scale * P->n[1] / (2.0 * M_PI));
+  float s3 = (float)(P->s_scale * P->n[2] / (2.0 * M_PI));
+  SPF_REQUIRE(P->n_items < (1LL << 31), "spf_nufft_interp_spread_sorted: too many items");
+  SPF_W_DISPATCH(P->w, (k_interp_spread_sorted<W><<<(unsigned)P->n_items, 256, 0, s>>>(
+                           P->re_pad, P->acc_pad, g, bd, P->items, P->sorted, P->s_quats,
+                           P->s_ppr, P->s_n_pix, s1, s2, s3, d_weights, device_error_word())));
+  return check_launch("k_interp_spread_sorted");
 }
 
 int spf_nufft_t1_finish(spf_nufft_plan P, int isign, float *d_out_re, float *d_out_im,

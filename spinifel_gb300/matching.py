@@ -247,7 +247,7 @@ def match_bf16(frames: FrameSet, refs: ReferenceSet, exact_fallback: bool = True
     return idx, dist
 
 
-RANGE_CAP = 64
+RANGE_CAP = 512
 
 
 def _complete_range(frames: FrameSet, refs: ReferenceSet, rows: torch.Tensor,

@@ -67,6 +67,11 @@ class _Slot:
         self.requests: list[Request] = []
         self.n = 0
         self.bytes = 0
+        self.stage = 0       # 0 free, 1 matching, 2 completing uncertified frames
+        self.result = None
+        self.bad = None
+        self.host_bad = None
+        self.keep = None
 
     def view(self, n):
         fs = self.frames
@@ -210,33 +215,79 @@ class OrientationServer:
         self.stats["frames"] += slot.n
         self.stats["t_launch_ms"] += (time.perf_counter() - t0) * 1e3
 
-    def _complete(self, slot: _Slot):
-        t0 = time.perf_counter()
+    def _finish_stage1(self, slot: _Slot) -> bool:
+        """Called when a slot's match has landed on the host.  Frames the
+        top-8 certificate left open get the certified completion (range query
+        on the tensor cores + exact re-rank of the list), enqueued on the
+        slot's stream without waiting; returns True when the slot is done."""
         n = slot.n
-        idx = slot.host_out[0, :n].numpy().copy()
+        slot.result = slot.host_out[0, :n].numpy().copy()
         unc = slot.host_out[1, :n].numpy()
         bad = np.flatnonzero(unc)
-        if bad.size:
-            # certified completion for the frames the top-8 certificate left
-            # open (range query on the tensor cores + exact re-rank of the list)
+        slot.bad = bad
+        if not bad.size:
+            return True
+        t0 = time.perf_counter()
+        with torch.cuda.stream(slot.stream):
+            rows = torch.as_tensor(bad, dtype=torch.int64).to(self.device, non_blocking=False)
+            fs = slot.view(n)
+            nb = int(bad.size)
+            bf = fs.bf16.index_select(0, rows).contiguous()
+            f32 = fs.f32.index_select(0, rows).contiguous()
+            sq = fs.sq.index_select(0, rows).contiguous()
+            thresh = slot.work[:n].index_select(0, rows).contiguous()
+            cap = matching.RANGE_CAP
+            lst = torch.empty(nb * cap, dtype=torch.int32, device=self.device)
+            cnt = torch.empty(nb, dtype=torch.int32, device=self.device)
+            sh = _lib.stream_handle(slot.stream)
+            _lib.call("spf_dist_range_bf16", _lib.ptr(bf), nb, _lib.ptr(self.refs.bf16),
+                      self.refs.n_ref, self.n_pix, self.ld, _lib.ptr(self.refs.sq),
+                      _lib.ptr(thresh), _lib.ptr(lst), _lib.ptr(cnt), cap, sh)
+            tr = matching.BestTracker(nb, self.device)
+            _lib.call("spf_rerank_list_fp32", _lib.ptr(lst), _lib.ptr(cnt), cap, _lib.ptr(f32),
+                      _lib.ptr(sq), nb, _lib.ptr(self.refs.f32), _lib.ptr(self.refs.sq),
+                      self.n_pix, 0, _lib.ptr(tr.best), sh)
+            i2, _ = tr.result()
+            slot.host_bad = torch.empty(2, nb, dtype=torch.int32).pin_memory()
+            slot.host_bad[0].copy_(i2, non_blocking=True)
+            slot.host_bad[1].copy_(cnt, non_blocking=True)
+            slot.keep = (f32, sq)
+            slot.event.record(slot.stream)
+        self.stats["uncertified"] += int(bad.size)
+        self.stats["t_complete_ms"] += (time.perf_counter() - t0) * 1e3
+        return False
+
+    def _finish_stage2(self, slot: _Slot):
+        idx2 = slot.host_bad[0].numpy()
+        cnt = slot.host_bad[1].numpy()
+        over = np.flatnonzero(cnt > matching.RANGE_CAP)
+        if over.size:
+            # a list longer than the cap: exact pass over all references (rare)
+            f32, sq = slot.keep
             with torch.cuda.stream(slot.stream):
-                rows = torch.as_tensor(bad, device=self.device)
-                fs = slot.view(n)
-                thresh = slot.work[:n].index_select(0, rows).contiguous()
-                i2, _ = matching._complete_range(fs, self.refs, rows, thresh, None,
-                                                 _lib.stream_handle(slot.stream))
-                idx[bad] = i2.cpu().numpy()
-            self.stats["uncertified"] += int(bad.size)
+                sel = torch.as_tensor(over, device=self.device)
+                tr = matching.BestTracker(int(over.size), self.device)
+                tr.update_fp32(f32.index_select(0, sel).contiguous(),
+                               sq.index_select(0, sel).contiguous(), self.refs.f32,
+                               self.refs.sq, 0)
+                i3, _ = tr.result()
+                idx2 = idx2.copy()
+                idx2[over] = i3.cpu().numpy()
+            self.stats["range_overflow"] += int(over.size)
+        slot.result[slot.bad] = idx2
+        slot.keep = None
+
+    def _deliver(self, slot: _Slot):
         now = time.perf_counter()
         row = 0
         for r in slot.requests:
             r.done_at = now
-            r.future.set_result(idx[row:row + r.n].astype(np.int64))
+            r.future.set_result(slot.result[row:row + r.n].astype(np.int64))
             row += r.n
             self.completed.append(r)
         self.in_use_bytes -= slot.bytes
         slot.requests, slot.n, slot.bytes = [], 0, 0
-        self.stats["t_complete_ms"] += (time.perf_counter() - t0) * 1e3
+        slot.stage = 0
 
     def _loop(self):
         torch.cuda.set_device(self.device)
@@ -251,6 +302,7 @@ class OrientationServer:
             for slot in launched:
                 try:
                     self._launch(slot)
+                    slot.stage = 1
                 except Exception as e:  # surface the failure to the requests
                     for r in slot.requests:
                         r.future.set_exception(e)
@@ -262,13 +314,20 @@ class OrientationServer:
                 self.busy.append(slot)
             still = []
             for slot in self.busy:
-                if slot.event.query():
-                    self.stats["t_gpu_ms"] += slot.t_start.elapsed_time(slot.event)
-                    self._complete(slot)
-                    with self.lock:
-                        self.free.append(slot)
-                else:
+                if not slot.event.query():
                     still.append(slot)
+                    continue
+                if slot.stage == 1:
+                    self.stats["t_gpu_ms"] += slot.t_start.elapsed_time(slot.event)
+                    if not self._finish_stage1(slot):
+                        slot.stage = 2  # completion enqueued; its event re-recorded
+                        still.append(slot)
+                        continue
+                else:
+                    self._finish_stage2(slot)
+                self._deliver(slot)
+                with self.lock:
+                    self.free.append(slot)
             self.busy = still
             if self.busy and not launched:
                 time.sleep(0.0001)

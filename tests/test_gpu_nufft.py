@@ -221,6 +221,33 @@ def test_patch_spreading_equals_point_spreading(dev, det):
     assert rel(res[1], res[0]) < TOL
 
 
+def test_sorted_interp_spread_equals_unsorted(dev):
+    from spinifel_gb300 import _lib
+    from spinifel_gb300.nufft import NufftPlan
+
+    det = (4, 64, 64)
+    model, ppr, pdr, quats = _slice_case(41, det, 40, 28)
+    mult = float(np.pi / pdr.max())
+    ppr_t = t(ppr.reshape(3, -1), dev)
+    q_t = t(quats, dev)
+    w = t(np.random.default_rng(29).random((40, ppr[0].size)).astype(np.float32), dev)
+    P = NufftPlan(41, 1e-6)
+    P.set_modes(t(model, dev))
+    P.spread_zero()
+    _lib.call("spf_nufft_interp_spread_orient", P.handle, _lib.ptr(q_t), 40, _lib.ptr(ppr_t),
+              ppr_t.shape[1], mult, _lib.ptr(w), _lib.stream_handle())
+    a = P.finish(+1)[0].cpu().numpy()
+    _lib.call("spf_nufft_sort_orient", P.handle, _lib.ptr(q_t), 40, _lib.ptr(ppr_t), ppr_t.shape[1],
+              mult, _lib.stream_handle())
+    P.spread_zero()
+    _lib.call("spf_nufft_interp_spread_sorted", P.handle, _lib.ptr(w), _lib.stream_handle())
+    b = P.finish(+1)[0].cpu().numpy()
+    from spinifel_gb300 import matching
+
+    matching.check_device_error()  # no point fell outside its bin's box
+    assert rel(b, a) < TOL
+
+
 def test_operator_glue_matches_reference_golden(dev):
     """autocorrelation.forward / adjoint against the reference's own glue
     (support, real part, / M^3) run on the FP64 oracle."""
