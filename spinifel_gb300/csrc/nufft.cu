@@ -720,7 +720,12 @@ __global__ void k_bin_scatter(const int32_t *__restrict__ bin_of, int64_t n,
 
 // One work item (a bin, or a chunk of a big bin): stage the bin's box of the
 // type-2 grid, interpolate every point, weight it, spread it into a shared
-// box, and add the box to the type-1 accumulator.
+// box, and add the box to the type-1 accumulator.  Eight lanes serve one
+// point (four points per warp): lane c owns offset c along the fastest axis,
+// evaluates the c-th kernel weight of each axis and shares them by
+// shuffles; the interpolation is a sum over (a, b) per lane followed by an
+// 8-lane shuffle reduction, and each spreading instruction writes 8
+// consecutive cells of one row per point, so lanes rarely collide on a cell.
 template <int W>
 __global__ void __launch_bounds__(256)
     k_interp_spread_sorted(const float *__restrict__ re_pad, float *__restrict__ acc_pad,
@@ -729,6 +734,7 @@ __global__ void __launch_bounds__(256)
                            const float *__restrict__ ppr, int64_t n_pix, float s1, float s2,
                            float s3, const float *__restrict__ weights,
                            unsigned int *__restrict__ err) {
+  static_assert(W <= 8, "eight lanes per point");
   constexpr int D = BIN + W - 1;
   __shared__ float tbox[D * D * D];
   __shared__ float abox[D * D * D];
@@ -744,45 +750,65 @@ __global__ void __launch_bounds__(256)
     abox[idx] = 0.0f;
   }
   __syncthreads();
-  for (int q = threadIdx.x; q < it.z; q += blockDim.x) {
-    const int32_t pi = sorted[it.y + q];
+  const int lane = threadIdx.x & 31;
+  const int grp = lane >> 3;   // point slot in the warp
+  const int c = lane & 7;      // offset along the fastest axis
+  const int warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  const float fn1 = (float)g.n1, fn2 = (float)g.n2, fn3 = (float)g.n3;
+  for (int base = warp * 4; base < it.z; base += nwarps * 4) {
+    const int q = base + grp;
+    const bool live = q < it.z;
+    const int32_t pi = live ? sorted[it.y + q] : sorted[it.y];
     const int64_t o = pi / n_pix, p = pi % n_pix;
     float h, k, l;
     rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
-    float w1[W], w2[W], w3[W];
-    const int li = axis_setup<W>(h, s1, g.n1, g.off1, g.beta, g.inv_half_w, w1) - i0b;
-    const int lj = axis_setup<W>(k, s2, g.n2, g.off2, g.beta, g.inv_half_w, w2) - j0b;
-    const int lk = axis_setup<W>(l, s3, g.n3, g.off3, g.beta, g.inv_half_w, w3) - k0b;
-    // the sort placed this point in this bin with the same arithmetic; a
-    // point outside the box would be a defect: record it and skip the point
-    if (li < 0 || lj < 0 || lk < 0 || li + W > di || lj + W > dj || lk + W > dk) {
-      if (err) atomicExch(err, (unsigned int)(-SPF_ERR_CUDA));
-      continue;
-    }
-    float v = 0.0f;
+    // per-axis first index (same arithmetic as axis_setup) and this lane's weight
+    float t1 = __fmul_rn(h, s1), t2 = __fmul_rn(k, s2), t3 = __fmul_rn(l, s3);
+    t1 = __fsub_rn(t1, __fmul_rn(fn1, floorf(__fadd_rn(__fdiv_rn(t1, fn1), 0.5f))));
+    t2 = __fsub_rn(t2, __fmul_rn(fn2, floorf(__fadd_rn(__fdiv_rn(t2, fn2), 0.5f))));
+    t3 = __fsub_rn(t3, __fmul_rn(fn3, floorf(__fadd_rn(__fdiv_rn(t3, fn3), 0.5f))));
+    const float l1 = ceilf(__fsub_rn(t1, 0.5f * W)), l2 = ceilf(__fsub_rn(t2, 0.5f * W)),
+                l3 = ceilf(__fsub_rn(t3, 0.5f * W));
+    const float cf = (float)c;
+    float my1 = c < W ? es_eval((l1 + cf - t1) * g.inv_half_w, g.beta) : 0.0f;
+    float my2 = c < W ? es_eval((l2 + cf - t2) * g.inv_half_w, g.beta) : 0.0f;
+    float my3 = c < W ? es_eval((l3 + cf - t3) * g.inv_half_w, g.beta) : 0.0f;
+    float w1[W], w2[W];
 #pragma unroll
     for (int a = 0; a < W; ++a) {
-      float acc_a = 0.0f;
+      w1[a] = __shfl_sync(0xffffffffu, my1, a, 8);
+      w2[a] = __shfl_sync(0xffffffffu, my2, a, 8);
+    }
+    const int li = (int)l1 + g.off1 - i0b, lj = (int)l2 + g.off2 - j0b, lk = (int)l3 + g.off3 - k0b;
+    bool inside = li >= 0 && lj >= 0 && lk >= 0 && li + W <= di && lj + W <= dj && lk + W <= dk;
+    if (live && !inside && c == 0 && err) atomicExch(err, (unsigned int)(-SPF_ERR_CUDA));
+    const bool act = live && inside && c < W;
+    // interpolate: lane c sums over (a, b), then the 8 lanes are reduced
+    float part = 0.0f;
+    if (act) {
 #pragma unroll
-      for (int c2 = 0; c2 < W; ++c2) {
-        const float *row = tbox + ((li + a) * dj + (lj + c2)) * dk + lk;
-        float r = 0.0f;
+      for (int a = 0; a < W; ++a) {
+        float pa = 0.0f;
 #pragma unroll
-        for (int c = 0; c < W; ++c) r = fmaf(w3[c], row[c], r);
-        acc_a = fmaf(w2[c2], r, acc_a);
+        for (int bb = 0; bb < W; ++bb)
+          pa = fmaf(w2[bb], tbox[((li + a) * dj + (lj + bb)) * dk + lk + c], pa);
+        part = fmaf(w1[a], pa, part);
       }
-      v = fmaf(w1[a], acc_a, v);
+      part *= my3;
     }
-    if (weights) v *= weights[pi];
-    if (v == 0.0f) continue;
+    part += __shfl_xor_sync(0xffffffffu, part, 4, 8);
+    part += __shfl_xor_sync(0xffffffffu, part, 2, 8);
+    part += __shfl_xor_sync(0xffffffffu, part, 1, 8);
+    float v = part;
+    if (weights && live) v *= weights[pi];
+    if (act && v != 0.0f) {
+      const float wv = my3 * v;
 #pragma unroll
-    for (int a = 0; a < W; ++a) {
+      for (int a = 0; a < W; ++a) {
 #pragma unroll
-      for (int c2 = 0; c2 < W; ++c2) {
-        float wab = w1[a] * w2[c2] * v;
-        float *row = abox + ((li + a) * dj + (lj + c2)) * dk + lk;
-#pragma unroll
-        for (int c = 0; c < W; ++c) atomicAdd(row + c, wab * w3[c]);
+        for (int bb = 0; bb < W; ++bb)
+          atomicAdd(&abox[((li + a) * dj + (lj + bb)) * dk + lk + c], w1[a] * w2[bb] * wv);
       }
     }
   }

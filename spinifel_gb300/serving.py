@@ -62,6 +62,10 @@ class _Slot:
         self.unc = torch.empty(cap, dtype=torch.int32, device=device)
         self.work = torch.empty(cap, dtype=torch.float32, device=device)
         self.host_out = torch.empty(2, cap, dtype=torch.int32).pin_memory()
+        # completion buffers, allocated once: pinning memory while other work
+        # runs on the device can wait for that work
+        self.host_rows = torch.empty(cap, dtype=torch.int64).pin_memory()
+        self.host_bad = torch.empty(2, cap, dtype=torch.int32).pin_memory()
         self.event = torch.cuda.Event(enable_timing=True)
         self.t_start = torch.cuda.Event(enable_timing=True)
         self.requests: list[Request] = []
@@ -70,7 +74,6 @@ class _Slot:
         self.stage = 0       # 0 free, 1 matching, 2 completing uncertified frames
         self.result = None
         self.bad = None
-        self.host_bad = None
         self.keep = None
 
     def view(self, n):
@@ -229,9 +232,10 @@ class OrientationServer:
             return True
         t0 = time.perf_counter()
         with torch.cuda.stream(slot.stream):
-            rows = torch.as_tensor(bad, dtype=torch.int64).to(self.device, non_blocking=False)
-            fs = slot.view(n)
             nb = int(bad.size)
+            slot.host_rows[:nb].copy_(torch.from_numpy(bad.astype(np.int64)))
+            rows = slot.host_rows[:nb].to(self.device, non_blocking=True)
+            fs = slot.view(n)
             bf = fs.bf16.index_select(0, rows).contiguous()
             f32 = fs.f32.index_select(0, rows).contiguous()
             sq = fs.sq.index_select(0, rows).contiguous()
@@ -248,9 +252,8 @@ class OrientationServer:
                       _lib.ptr(sq), nb, _lib.ptr(self.refs.f32), _lib.ptr(self.refs.sq),
                       self.n_pix, 0, _lib.ptr(tr.best), sh)
             i2, _ = tr.result()
-            slot.host_bad = torch.empty(2, nb, dtype=torch.int32).pin_memory()
-            slot.host_bad[0].copy_(i2, non_blocking=True)
-            slot.host_bad[1].copy_(cnt, non_blocking=True)
+            slot.host_bad[0, :nb].copy_(i2, non_blocking=True)
+            slot.host_bad[1, :nb].copy_(cnt, non_blocking=True)
             slot.keep = (f32, sq)
             slot.event.record(slot.stream)
         self.stats["uncertified"] += int(bad.size)
@@ -258,8 +261,9 @@ class OrientationServer:
         return False
 
     def _finish_stage2(self, slot: _Slot):
-        idx2 = slot.host_bad[0].numpy()
-        cnt = slot.host_bad[1].numpy()
+        nb = int(slot.bad.size)
+        idx2 = slot.host_bad[0, :nb].numpy().copy()
+        cnt = slot.host_bad[1, :nb].numpy()
         over = np.flatnonzero(cnt > matching.RANGE_CAP)
         if over.size:
             # a list longer than the cap: exact pass over all references (rare)
