@@ -169,7 +169,59 @@ def measure_serving(rset, frames_u16_host, rate_fps, total_frames, path, seed=7)
             "p99_ms": float(np.percentile(lat, 99)), "launches": stats.get("launches", 0),
             "uncertified": stats.get("uncertified", 0),
             "server_ms": {k: round(stats.get(k, 0.0), 1)
-                          for k in ("t_launch_ms", "t_gpu_ms", "t_complete_ms")}}
+                          for k in ("t_launch_ms", "t_gpu_ms", "t_complete_ms", "t_c_rows_ms",
+                                    "t_c_gather_ms", "t_c_range_ms")}}
+
+
+def measure_accuracy(plan, model, ref_q, ppr, ppr_t, mult, det, frames, rset, W, n_slices=3,
+                     n_frames=64):
+    """Relative L2 of GPU slices against the FP64 oracle NUFFT (a few
+    orientations), and relative errors of the bf16 tensor-core and re-ranked
+    FP32 distances against FP64 for the candidates of a few frames."""
+    import torch
+
+    from oracle import nufft as onufft
+    from spinifel_gb300 import _lib, geom
+
+    q = ref_q[:n_slices].double().cpu().numpy()
+    gpu = plan.slice(ref_q[:n_slices], ppr_t, mult, det_shape=det).double().cpu().numpy()
+    H, K, L = geom.hkl(q.astype(np.float32).astype(np.float64), ppr)
+    exact = onufft.nufft3d2(H.reshape(-1) * mult, K.reshape(-1) * mult, L.reshape(-1) * mult,
+                            model.astype(np.float64), -1, 1e-9).real.reshape(n_slices, -1)
+    slice_rel = float(np.linalg.norm(gpu - exact) / np.linalg.norm(exact))
+    # distances: top-8 candidates of the first frames
+    n = min(n_frames, frames.n)
+    tiles = int(_lib.lib().spf_dist_topk_bf16_tiles(rset.n_ref))
+    dev = frames.f32.device
+    sub_bf = frames.bf16[:n].contiguous()
+    cd = torch.empty(tiles * n * 8, dtype=torch.float32, device=dev)
+    ci = torch.empty(tiles * n * 8, dtype=torch.int32, device=dev)
+    _lib.call("spf_dist_topk_bf16", _lib.ptr(sub_bf), n, _lib.ptr(rset.bf16), rset.n_ref,
+              rset.n_pix, rset.ld, _lib.ptr(rset.sq), _lib.ptr(cd), _lib.ptr(ci),
+              _lib.stream_handle())
+    work = torch.empty(n, dtype=torch.float32, device=dev)
+    idx = torch.empty(n, dtype=torch.int32, device=dev)
+    dist = torch.empty(n, dtype=torch.float32, device=dev)
+    top = torch.empty(n * 8, dtype=torch.int32, device=dev)
+    _lib.call("spf_rerank_fp32", _lib.ptr(cd), _lib.ptr(ci), tiles,
+              _lib.ptr(frames.f32[:n].contiguous()), _lib.ptr(frames.sq[:n].contiguous()), n,
+              _lib.ptr(rset.f32), _lib.ptr(rset.sq), _lib.ptr(rset.m2), float(rset.sq_max),
+              rset.n_ref, rset.n_pix, 0, _lib.ptr(work), _lib.ptr(idx), _lib.ptr(dist), None,
+              _lib.ptr(top), _lib.stream_handle())
+    torch.cuda.synchronize()
+    approx = cd[:n * 8].view(n, 8).double() + frames.sq[:n].double()[:, None]
+    cand = ci[:n * 8].view(n, 8).long()
+    x = frames.f32[:n].double()
+    ex = torch.stack([((x - rset.f32[cand[:, k]].double()) ** 2).sum(1) for k in range(8)], 1)
+    rel_bf16 = ((approx - ex).abs() / ex).flatten()
+    ex_best = ((x - rset.f32[idx.long()].double()) ** 2).sum(1)
+    rel_fp32 = (dist.double() - ex_best).abs() / ex_best
+    return {"slice_rel_l2_vs_fp64": slice_rel, "slices_checked": n_slices,
+            "distance_rel_err_bf16": {"median": float(rel_bf16.median()),
+                                      "max": float(rel_bf16.max())},
+            "distance_rel_err_fp32_rerank_best": {"median": float(rel_fp32.median()),
+                                                  "max": float(rel_fp32.max())},
+            "frames_checked": n}
 
 
 def config_dict(W):
@@ -256,9 +308,25 @@ def run_merge(args):
         res[name] = {"ms_total": ms, "ms_per_iter": ms / W["iters"],
                      "iterations": int(iters.item()), "launches": _lib.launch_count() - l0,
                      "residual_first": float(hist[0]), "residual_last": float(hist[-1]),
+                     "residual_history": [round(float(h), 4) for h in hist.cpu()],
                      "x": x}
     xt, xd = res["toeplitz"].pop("x"), res["direct"].pop("x")
     rel_td = float((xd - xt).norm() / xt.norm())
+    # one application of each form to the same centrosymmetric vector
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    v = torch.randn((M,) * 3, dtype=torch.float64, device=dev, generator=g)
+    v = 0.5 * (v + torch.flip(v, dims=(0, 1, 2)))
+    wt_ = op.apply(v.reshape(-1), form=0)
+    wd_ = op.apply(v.reshape(-1), form=1)
+    op_rel = float((wd_ - wt_).norm() / wt_.norm())
+    # the data term alone (the regulariser, common to both forms, dominates W)
+    op0 = MergeOperator(M, Mu, rl, 0.0, S, antisupport(M, 1))
+    op0.set_kernel(ugrid_conv)
+    op0.set_direct(P, q, ppr_t, mult, det_shape=det)
+    ct = op0.apply(v.reshape(-1), form=0) - rl * v.reshape(-1)
+    cdir = op0.apply(v.reshape(-1), form=1) - rl * v.reshape(-1)
+    conv_rel = float((cdir - ct).norm() / ct.norm())
     # the direct operator alone: one interpolate+spread pass over all points,
     # with the bin-sorted kernel (used by the CG) and with the patch kernel
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -284,7 +352,9 @@ def run_merge(args):
            "config": {"workload": W["name"], "M": M, "n_points": npts, "iterations": W["iters"],
                       "eps": W["eps"]},
            "toeplitz": res["toeplitz"], "direct": res["direct"],
-           "direct_vs_toeplitz_rel_l2": rel_td,
+           "solution_direct_vs_toeplitz_rel_l2": rel_td,
+           "operator_direct_vs_toeplitz_rel_l2": op_rel,
+           "data_term_direct_vs_toeplitz_rel_l2": conv_rel,
            "setup_type1_spread_ms": spread_ms,
            "interp_spread_pass": {"ms": isp_ms, "patch_kernel_ms": passes["patch"],
                                   "points_per_s": npts / (isp_ms / 1e3),
@@ -517,6 +587,11 @@ def main():
         serving = {"bf16": measure_serving(rset, imgs_u16_host, 2000.0, 10_000, "bf16"),
                    "plain_fp32": measure_serving(rset, imgs_u16_host, 2000.0, 4_000, "fp32")}
 
+    # --- accuracy against FP64 ---------------------------------------------
+    accuracy = None
+    if rank == 0:
+        accuracy = measure_accuracy(plan, model, ref_q, ppr, ppr_t, mult, det, frames, rset, W)
+
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(n_pix, W["n_ref"])
@@ -538,7 +613,7 @@ def main():
                               st_bf.get("uncertified"), "range_overflow":
                               st_bf.get("range_overflow"), "range_max_list":
                               st_bf.get("range_max_list"), "e2e_equals_device": same_e2e},
-               "serving": serving, "autotune": tuned,
+               "serving": serving, "autotune": tuned, "accuracy": accuracy,
                "slicing": {"ms_all_refs": slice_ms,
                            "points_per_s": W["n_ref"] * n_pix / (slice_ms / 1e3)},
                "peaks_source": peak_src}

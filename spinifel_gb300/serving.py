@@ -235,6 +235,7 @@ class OrientationServer:
             nb = int(bad.size)
             slot.host_rows[:nb].copy_(torch.from_numpy(bad.astype(np.int64)))
             rows = slot.host_rows[:nb].to(self.device, non_blocking=True)
+            self.stats["t_c_rows_ms"] += (time.perf_counter() - t0) * 1e3
             fs = slot.view(n)
             bf = fs.bf16.index_select(0, rows).contiguous()
             f32 = fs.f32.index_select(0, rows).contiguous()
@@ -244,9 +245,11 @@ class OrientationServer:
             lst = torch.empty(nb * cap, dtype=torch.int32, device=self.device)
             cnt = torch.empty(nb, dtype=torch.int32, device=self.device)
             sh = _lib.stream_handle(slot.stream)
+            self.stats["t_c_gather_ms"] += (time.perf_counter() - t0) * 1e3
             _lib.call("spf_dist_range_bf16", _lib.ptr(bf), nb, _lib.ptr(self.refs.bf16),
                       self.refs.n_ref, self.n_pix, self.ld, _lib.ptr(self.refs.sq),
                       _lib.ptr(thresh), _lib.ptr(lst), _lib.ptr(cnt), cap, sh)
+            self.stats["t_c_range_ms"] += (time.perf_counter() - t0) * 1e3
             tr = matching.BestTracker(nb, self.device)
             _lib.call("spf_rerank_list_fp32", _lib.ptr(lst), _lib.ptr(cnt), cap, _lib.ptr(f32),
                       _lib.ptr(sq), nb, _lib.ptr(self.refs.f32), _lib.ptr(self.refs.sq),
