@@ -235,6 +235,77 @@ MERGE = dict(name="merge-cg-151", M=151, panels=4, nx=128, ny=128, n_frames=2000
              iters=30, eps=1e-6, seed=20261204)
 
 
+def run_nufft(args):
+    """The NUFFT kernels alone on the 151^3 merge grid: patch slicing of
+    n orientations (type 2), bin sort, the fused interpolate/spread pass and
+    the patch spreading pass (type 1); n = --n-img (default 2,000)."""
+    import torch
+
+    from spinifel_gb300 import _lib, geom, synth
+    from spinifel_gb300.nufft import NufftPlan
+
+    W = MERGE
+    n_or = args.n_img or W["n_frames"]
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(W["seed"])
+    M = W["M"]
+    det = (W["panels"], W["nx"], W["ny"])
+    n_pix = W["panels"] * W["nx"] * W["ny"]
+    model = synth.intensity_model(M, seed=W["seed"], dtype=np.float32)
+    ppr, pdr = geom.flat_detector(*det)
+    mult = float(np.pi / pdr.max())
+    ppr_t = torch.as_tensor(ppr.reshape(3, -1), dtype=torch.float32, device=dev)
+    q = torch.as_tensor(geom.uniform_quaternions(n_or, rng), dtype=torch.float32, device=dev)
+    P = NufftPlan(M, W["eps"])
+    P.set_modes(torch.as_tensor(model, device=dev))
+    out = torch.empty(n_or, n_pix, dtype=torch.float32, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    npts = n_or * n_pix
+    t_slice = timed(lambda: P.slice(q, ppr_t, mult, out=out, det_shape=det))
+    _lib.call("spf_nufft_sort_orient", P.handle, _lib.ptr(q), n_or, _lib.ptr(ppr_t), n_pix, mult,
+              _lib.stream_handle())
+
+    def isp():
+        P.spread_zero()
+        _lib.call("spf_nufft_interp_spread_sorted", P.handle, None, _lib.stream_handle())
+
+    t_isp = timed(isp)
+    c = out.clamp_min(0).contiguous()
+
+    def spr():
+        P.spread_zero()
+        P.spread_orient(q, ppr_t, mult, c, det_shape=det)
+
+    t_spr = timed(spr)
+    w = P.width
+    peaks, src = load_peaks()
+    fp32_peak = 152 * 128 * 2 * 2070.0 * 1e6 / 1e12
+    rec = {"metric": "NUFFT kernels on the 151^3 grid (points/s)", "config": {
+        "workload": "nufft-151", "M": M, "n_orient": n_or, "n_points": npts, "width": w,
+        "fine_grid": list(P.n_fine)},
+        "slice_t2": {"ms": t_slice, "points_per_s": npts / (t_slice / 1e3),
+                     "tflops": npts * (2 * w ** 3 + 3 * w) / (t_slice / 1e3) / 1e12,
+                     "fp32_peak_tflops_nominal": fp32_peak,
+                     "out_gbs": npts * 4 / (t_slice / 1e3) / 1e9},
+        "interp_spread_sorted": {"ms": t_isp, "points_per_s": npts / (t_isp / 1e3)},
+        "spread_t1_patch": {"ms": t_spr, "points_per_s": npts / (t_spr / 1e3),
+                            "gbs_points": npts * 16 / (t_spr / 1e3) / 1e9,
+                            "hbm_peak_gbs": float(peaks.get("hbm_gbs", 6800.0))}}
+    print(json.dumps(rec), flush=True)
+
+
 def run_merge(args):
     """Autocorrelation merge at 151^3 with 2,000 frames x 65,536 pixels
     (1.31e8 points): setup (two type-1 NUFFTs), then 30 CG iterations in the
@@ -375,10 +446,14 @@ def main():
     ap.add_argument("--n-img", type=int, default=None, help="override (testing only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--workload", default="match", choices=["match", "merge", "serving"])
+    ap.add_argument("--workload", default="match",
+                    choices=["match", "merge", "serving", "nufft"])
     args = ap.parse_args()
     if args.workload == "merge":
         run_merge(args)
+        return
+    if args.workload == "nufft":
+        run_nufft(args)
         return
     if args.workload == "serving":
         WORKLOAD.update(name="om-serving-200k", n_ref=200_000, n_img=20_000)

@@ -320,6 +320,12 @@ int spf_col_maxsq_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_
 int spf_row_norms_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_sq,
                       float *d_n4, void *stream);
 
+/* Row gather: d_dst[i] = d_src[d_rows[i]] for rows of row_bytes bytes
+ * (indices are not checked against n_src_rows on the device; the caller
+ * guarantees 0 <= d_rows[i] < n_src_rows). */
+int spf_gather_rows(const void *d_src, int64_t n_src_rows, int64_t row_bytes,
+                    const int64_t *d_rows, int64_t n, void *d_dst, void *stream);
+
 /* FP32 -> bf16 with a padded row stride: dst[r*ld + p] = bf16(src[r*n_pix+p])
  * for p < n_pix, 0 for n_pix <= p < ld. */
 int spf_f32_to_bf16(const float *d_src, int64_t n_rows, int64_t n_pix, void *d_dst,

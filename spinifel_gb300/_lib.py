@@ -112,6 +112,7 @@ SIGNATURES = {
                              _c_void_p, _i64, _i64, _c_void_p, _c_void_p],
     "spf_row_norms_f32": [_c_void_p, _i64, _i64, _c_void_p, _c_void_p, _c_void_p],
     "spf_f32_to_bf16": [_c_void_p, _i64, _i64, _c_void_p, _i64, _c_void_p],
+    "spf_gather_rows": [_c_void_p, _i64, _i64, _c_void_p, _i64, _c_void_p, _c_void_p],
 }
 
 _RESTYPES = {

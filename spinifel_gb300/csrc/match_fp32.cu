@@ -281,6 +281,29 @@ __global__ void k_ingest_u16(const uint16_t *__restrict__ in, int64_t n_img, int
   }
 }
 
+// dst[i] = src[rows[i]] for rows of row_bytes bytes (16-byte chunks when aligned)
+__global__ void k_gather_rows16(const uint4 *__restrict__ src, int64_t row_chunks,
+                                const int64_t *__restrict__ rows, int64_t n,
+                                uint4 *__restrict__ dst) {
+  int64_t total = n * row_chunks;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e / row_chunks, c = e % row_chunks;
+    dst[e] = src[rows[i] * row_chunks + c];
+  }
+}
+
+__global__ void k_gather_rows1(const unsigned char *__restrict__ src, int64_t row_bytes,
+                               const int64_t *__restrict__ rows, int64_t n,
+                               unsigned char *__restrict__ dst) {
+  int64_t total = n * row_bytes;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e / row_bytes, c = e % row_bytes;
+    dst[e] = src[rows[i] * row_bytes + c];
+  }
+}
+
 __global__ void k_f32_to_bf16(const float *__restrict__ src, int64_t n_rows, int64_t n_pix,
                               __nv_bfloat16 *__restrict__ dst, int64_t ld) {
   int64_t total = n_rows * ld;
@@ -432,6 +455,25 @@ int spf_frames_ingest_u16(const uint16_t *d_counts, int64_t n_img, int64_t n_pix
   k_ingest_u16<<<blocks, 256, 0, as_stream(stream)>>>(
       d_counts, n_img, n_pix, d_f32, reinterpret_cast<__nv_bfloat16 *>(d_bf16), ld, d_sq, d_n4);
   return check_launch("spf_frames_ingest_u16");
+}
+
+int spf_gather_rows(const void *d_src, int64_t n_src_rows, int64_t row_bytes,
+                    const int64_t *d_rows, int64_t n, void *d_dst, void *stream) {
+  SPF_REQUIRE(n >= 0 && row_bytes >= 0 && n_src_rows >= 0, "spf_gather_rows: negative size");
+  if (n == 0 || row_bytes == 0) return SPF_OK;
+  SPF_REQUIRE(d_src && d_rows && d_dst, "spf_gather_rows: NULL pointer");
+  cudaStream_t s = as_stream(stream);
+  if (row_bytes % 16 == 0 && aligned(d_src, 16) && aligned(d_dst, 16)) {
+    int64_t chunks = row_bytes / 16;
+    k_gather_rows16<<<grid_for(n * chunks, 256, (int64_t)sm_count() * 16), 256, 0, s>>>(
+        reinterpret_cast<const uint4 *>(d_src), chunks, d_rows, n,
+        reinterpret_cast<uint4 *>(d_dst));
+  } else {
+    k_gather_rows1<<<grid_for(n * row_bytes, 256, (int64_t)sm_count() * 16), 256, 0, s>>>(
+        reinterpret_cast<const unsigned char *>(d_src), row_bytes, d_rows, n,
+        reinterpret_cast<unsigned char *>(d_dst));
+  }
+  return check_launch("spf_gather_rows");
 }
 
 int spf_f32_to_bf16(const float *d_src, int64_t n_rows, int64_t n_pix, void *d_dst, int64_t ld,

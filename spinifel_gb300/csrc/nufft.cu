@@ -367,14 +367,18 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   const int imin = bb[0], jmin = bb[1], kmin = bb[2];
   const int di = bb[3] - imin + W, dj = bb[4] - jmin + W, dk = bb[5] - kmin + W;
+  // odd row strides spread neighbouring points' rows over the banks
+  const int sj = dj | 1, sk = dk | 1;
   const int64_t vol = (int64_t)di * dj * dk;
+  const int64_t svol = (int64_t)di * sj * sk;
   float acc = 0.0f;
-  if (bb[3] >= imin && vol <= SLICE_SMEM_FLOATS) {
+  if (bb[3] >= imin && svol <= SLICE_SMEM_FLOATS) {
     for (int idx = threadIdx.x; idx < (int)vol; idx += blockDim.x) {
       int kk = idx % dk;
       int jj = (idx / dk) % dj;
       int ii = idx / (dk * dj);
-      box[idx] = __ldg(re_pad + ((size_t)(imin + ii) * g.p2 + (jmin + jj)) * g.p3 + kmin + kk);
+      box[(ii * sj + jj) * sk + kk] =
+          __ldg(re_pad + ((size_t)(imin + ii) * g.p2 + (jmin + jj)) * g.p3 + kmin + kk);
     }
     __syncthreads();
     // only valid points' footprints are inside the box
@@ -385,7 +389,7 @@ __global__ void __launch_bounds__(256)
       float acc_a = 0.0f;
 #pragma unroll
       for (int b = 0; b < W; ++b) {
-        const float *row = box + ((li + a) * dj + (lj + b)) * dk + lk;
+        const float *row = box + ((li + a) * sj + (lj + b)) * sk + lk;
         float r = 0.0f;
 #pragma unroll
         for (int c = 0; c < W; ++c) r = fmaf(w3[c], row[c], r);
@@ -736,8 +740,9 @@ __global__ void __launch_bounds__(256)
                            unsigned int *__restrict__ err) {
   static_assert(W <= 8, "eight lanes per point");
   constexpr int D = BIN + W - 1;
-  __shared__ float tbox[D * D * D];
-  __shared__ float abox[D * D * D];
+  constexpr int S = D | 1;  // odd row stride
+  __shared__ float tbox[D * S * S];
+  __shared__ float abox[D * S * S];
   const int4 it = items[blockIdx.x];
   const int b = it.x;
   const int bi = b / (bd.nb[1] * bd.nb[2]), bj = (b / bd.nb[2]) % bd.nb[1], bk = b % bd.nb[2];
@@ -746,8 +751,9 @@ __global__ void __launch_bounds__(256)
   const int vol = di * dj * dk;
   for (int idx = threadIdx.x; idx < vol; idx += blockDim.x) {
     int kk = idx % dk, jj = (idx / dk) % dj, ii = idx / (dk * dj);
-    tbox[idx] = __ldg(re_pad + ((size_t)(i0b + ii) * g.p2 + (j0b + jj)) * g.p3 + k0b + kk);
-    abox[idx] = 0.0f;
+    int sidx = (ii * S + jj) * S + kk;
+    tbox[sidx] = __ldg(re_pad + ((size_t)(i0b + ii) * g.p2 + (j0b + jj)) * g.p3 + k0b + kk);
+    abox[sidx] = 0.0f;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
@@ -792,7 +798,7 @@ __global__ void __launch_bounds__(256)
         float pa = 0.0f;
 #pragma unroll
         for (int bb = 0; bb < W; ++bb)
-          pa = fmaf(w2[bb], tbox[((li + a) * dj + (lj + bb)) * dk + lk + c], pa);
+          pa = fmaf(w2[bb], tbox[((li + a) * S + (lj + bb)) * S + lk + c], pa);
         part = fmaf(w1[a], pa, part);
       }
       part *= my3;
@@ -808,17 +814,16 @@ __global__ void __launch_bounds__(256)
       for (int a = 0; a < W; ++a) {
 #pragma unroll
         for (int bb = 0; bb < W; ++bb)
-          atomicAdd(&abox[((li + a) * dj + (lj + bb)) * dk + lk + c], w1[a] * w2[bb] * wv);
+          atomicAdd(&abox[((li + a) * S + (lj + bb)) * S + lk + c], w1[a] * w2[bb] * wv);
       }
     }
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < vol; idx += blockDim.x) {
-    float bv = abox[idx];
-    if (bv != 0.0f) {
-      int kk = idx % dk, jj = (idx / dk) % dj, ii = idx / (dk * dj);
+    int kk = idx % dk, jj = (idx / dk) % dj, ii = idx / (dk * dj);
+    float bv = abox[(ii * S + jj) * S + kk];
+    if (bv != 0.0f)
       atomicAdd(acc_pad + ((size_t)(i0b + ii) * g.p2 + (j0b + jj)) * g.p3 + k0b + kk, bv);
-    }
   }
 }
 

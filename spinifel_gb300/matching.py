@@ -102,6 +102,22 @@ def knn_topk(dist: torch.Tensor, k: int) -> torch.Tensor:
 # BF16 tensor-core path with exact FP32 re-rank
 # ---------------------------------------------------------------------------
 
+def gather_rows(src: torch.Tensor, rows: torch.Tensor, out: torch.Tensor | None = None,
+                stream=None) -> torch.Tensor:
+    """out[i] = src[rows[i]] along the first axis, with the library's gather
+    kernel (rows: int64 device tensor)."""
+    _lib.require_cuda(src, "src")
+    rows = rows.to(torch.int64)
+    _lib.require_cuda(rows, "rows")
+    n = rows.numel()
+    if out is None:
+        out = torch.empty((n,) + tuple(src.shape[1:]), dtype=src.dtype, device=src.device)
+    row_bytes = src[0].numel() * src.element_size() if src.shape[0] else 0
+    _lib.call("spf_gather_rows", _lib.ptr(src), src.shape[0], row_bytes, _lib.ptr(rows), n,
+              _lib.ptr(out), _lib.stream_handle(stream))
+    return out
+
+
 def row_norms(x: torch.Tensor):
     """(sum x^2, sqrt(sum x^4)) per row, FP32 results."""
     _lib.require_cuda(x, "x", torch.float32)
@@ -240,8 +256,8 @@ def match_bf16(frames: FrameSet, refs: ReferenceSet, exact_fallback: bool = True
         if stats is not None:
             stats["uncertified"] = nbad
         if exact_fallback and nbad:
-            i2, d2 = _complete_range(frames, refs, bad, work.index_select(0, bad).contiguous(),
-                                     stats, sh)
+            i2, d2 = _complete_range(frames, refs, bad,
+                                     gather_rows(work.view(-1, 1), bad).view(-1), stats, sh)
             idx.index_copy_(0, bad, i2)
             dist.index_copy_(0, bad, d2)
     return idx, dist
@@ -258,9 +274,9 @@ def _complete_range(frames: FrameSet, refs: ReferenceSet, rows: torch.Tensor,
     back to the plain FP32 pass over all references."""
     dev = frames.f32.device
     n = int(rows.numel())
-    bf = frames.bf16.index_select(0, rows).contiguous()
-    f32 = frames.f32.index_select(0, rows).contiguous()
-    sq = frames.sq.index_select(0, rows).contiguous()
+    bf = gather_rows(frames.bf16, rows)
+    f32 = gather_rows(frames.f32, rows)
+    sq = gather_rows(frames.sq.view(-1, 1), rows).view(-1)
     lst = _ws.get("range_list", n * RANGE_CAP, torch.int32, dev)
     cnt = _ws.get("range_count", n, torch.int32, dev)
     _lib.call("spf_dist_range_bf16", _lib.ptr(bf), n, _lib.ptr(refs.bf16), refs.n_ref, refs.n_pix,
@@ -278,7 +294,7 @@ def _complete_range(frames: FrameSet, refs: ReferenceSet, rows: torch.Tensor,
         stats["range_max_list"] = int(cnt.max().item()) if n else 0
     if n_over:
         t2 = BestTracker(n_over, dev)
-        t2.update_fp32(f32.index_select(0, over).contiguous(), sq.index_select(0, over).contiguous(),
+        t2.update_fp32(gather_rows(f32, over), gather_rows(sq.view(-1, 1), over).view(-1),
                        refs.f32, refs.sq, 0)
         i3, d3 = t2.result()
         i2.index_copy_(0, over, i3)

@@ -237,10 +237,11 @@ class OrientationServer:
             rows = slot.host_rows[:nb].to(self.device, non_blocking=True)
             self.stats["t_c_rows_ms"] += (time.perf_counter() - t0) * 1e3
             fs = slot.view(n)
-            bf = fs.bf16.index_select(0, rows).contiguous()
-            f32 = fs.f32.index_select(0, rows).contiguous()
-            sq = fs.sq.index_select(0, rows).contiguous()
-            thresh = slot.work[:n].index_select(0, rows).contiguous()
+            sh0 = slot.stream
+            bf = matching.gather_rows(fs.bf16, rows, stream=sh0)
+            f32 = matching.gather_rows(fs.f32, rows, stream=sh0)
+            sq = matching.gather_rows(fs.sq.view(-1, 1), rows, stream=sh0).view(-1)
+            thresh = matching.gather_rows(slot.work[:n].view(-1, 1), rows, stream=sh0).view(-1)
             cap = matching.RANGE_CAP
             lst = torch.empty(nb * cap, dtype=torch.int32, device=self.device)
             cnt = torch.empty(nb, dtype=torch.int32, device=self.device)
@@ -272,11 +273,11 @@ class OrientationServer:
             # a list longer than the cap: exact pass over all references (rare)
             f32, sq = slot.keep
             with torch.cuda.stream(slot.stream):
-                sel = torch.as_tensor(over, device=self.device)
+                sel = torch.as_tensor(over, dtype=torch.int64, device=self.device)
                 tr = matching.BestTracker(int(over.size), self.device)
-                tr.update_fp32(f32.index_select(0, sel).contiguous(),
-                               sq.index_select(0, sel).contiguous(), self.refs.f32,
-                               self.refs.sq, 0)
+                tr.update_fp32(matching.gather_rows(f32, sel),
+                               matching.gather_rows(sq.view(-1, 1), sel).view(-1),
+                               self.refs.f32, self.refs.sq, 0)
                 i3, _ = tr.result()
                 idx2 = idx2.copy()
                 idx2[over] = i3.cpu().numpy()

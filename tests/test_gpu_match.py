@@ -160,3 +160,15 @@ def test_empty_inputs(dev):
     idx, d = matching.argmin_fp32(e, r)
     assert idx.numel() == 0
     assert matching.knn_eudist(r, e).shape == (0, 10)
+
+
+@pytest.mark.parametrize("dtype,shape", [(torch.bfloat16, (50, 64)), (torch.float32, (50, 7)),
+                                         (torch.float32, (9, 1)), (torch.int16, (30, 3))])
+def test_gather_rows_matches_indexing(dev, dtype, shape):
+    from spinifel_gb300 import matching
+
+    g = torch.Generator(device="cpu").manual_seed(3)
+    src = (torch.rand(shape, generator=g) * 100).to(dtype).to(dev)
+    rows = torch.tensor([3, 0, 49 % shape[0], 3, shape[0] - 1], dtype=torch.int64, device=dev)
+    out = matching.gather_rows(src, rows)
+    assert torch.equal(out, src[rows])
