@@ -41,6 +41,19 @@ METRIC = "frames oriented/s: BF16-TC+rerank vs plain FP32 @ same argmin; p50/p99
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
 
 
+def profiled_traffic(kernel: str, profile: str):
+    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu
+    summary `profiles/<profile>` (its `traffic_bytes_per_launch` line), or
+    None when the summary is absent."""
+    p = os.path.join(ROOT, "profiles", profile)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith(f"traffic_bytes_per_launch {kernel}:"):
+            return float(line.split(":")[1])
+    return None
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -151,26 +164,31 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
-def measure_serving(rset, frames_u16_host, rate_fps, total_frames, path, seed=7):
+def measure_serving(rset, frames_u16_host, rate_fps, total_frames, path, seed=7, native=False):
     """Replay a Poisson schedule (sizes log-uniform in [1, 512]) against the
-    continuous-batching server; p50/p99 request latency and frames/s."""
-    from spinifel_gb300.serving import OrientationServer, poisson_schedule, run_schedule
+    continuous-batching server (the Python scheduler, or the library's native
+    one); p50/p99 request latency and frames/s."""
+    from spinifel_gb300.serving import (NativeOrientationServer, OrientationServer,
+                                        poisson_schedule, run_schedule)
 
     sched = poisson_schedule(total_frames, rate_fps, np.random.default_rng(seed), max_batch=512)
-    with OrientationServer(rset, slot_frames=512, n_slots=3, path=path) as srv:
+    cls = NativeOrientationServer if native else OrientationServer
+    with cls(rset, slot_frames=512, n_slots=3, path=path) as srv:
         t0 = time.perf_counter()
         res = run_schedule(srv, frames_u16_host, sched)
         t1 = time.perf_counter()
         lat = srv.latency_ms()
         stats = dict(srv.stats)
     n = int(sum(r.size for r in res))
-    return {"path": path, "offered_fps": rate_fps, "requests": len(sched), "frames": n,
+    keys = (("t_gpu_ms",) if native else
+            ("t_launch_ms", "t_gpu_ms", "t_complete_ms", "t_c_rows_ms", "t_c_gather_ms",
+             "t_c_range_ms"))
+    return {"path": path, "scheduler": "native" if native else "python",
+            "offered_fps": rate_fps, "requests": len(sched), "frames": n,
             "frames_per_s": n / (t1 - t0), "p50_ms": float(np.percentile(lat, 50)),
-            "p99_ms": float(np.percentile(lat, 99)), "launches": stats.get("launches", 0),
-            "uncertified": stats.get("uncertified", 0),
-            "server_ms": {k: round(stats.get(k, 0.0), 1)
-                          for k in ("t_launch_ms", "t_gpu_ms", "t_complete_ms", "t_c_rows_ms",
-                                    "t_c_gather_ms", "t_c_range_ms")}}
+            "p99_ms": float(np.percentile(lat, 99)), "launches": int(stats.get("launches", 0)),
+            "uncertified": int(stats.get("uncertified", 0)),
+            "server_ms": {k: round(stats.get(k, 0.0), 1) for k in keys}}
 
 
 def measure_accuracy(plan, model, ref_q, ppr, ppr_t, mult, det, frames, rset, W, n_slices=3,
@@ -539,7 +557,11 @@ def main():
     if getattr(args, "serving_only", False):
         out = {"metric": "serving latency p50/p99 (ms) and frames/s, 200,000 resident references",
                "config": config_dict(W), "data": "synthetic",
+               "bf16_native": measure_serving(rset, imgs_u16_host, 2000.0, W["n_img"], "bf16",
+                                              native=True),
                "bf16": measure_serving(rset, imgs_u16_host, 2000.0, W["n_img"], "bf16"),
+               "plain_fp32_native": measure_serving(rset, imgs_u16_host, 2000.0, 4000, "fp32",
+                                                    native=True),
                "plain_fp32": measure_serving(rset, imgs_u16_host, 2000.0, 4000, "fp32"),
                "slicing": {"ms_all_refs": slice_ms}}
         print(json.dumps(out), flush=True)
@@ -601,8 +623,18 @@ def main():
     peaks, peak_src = load_peaks()
     peak = float(peaks.get("bf16_tflops", 1900.0))
     achieved = flops / (k_ms / 1e3) / 1e12
+    # DRAM traffic of one launch, captured by ncu on this exact workload
+    # (10,000 frames x 100,000 references); other sizes report none
+    traffic = None
+    if (W["n_img"], W["n_ref"], n_pix) == (10_000, 100_000, 65_536):
+        traffic = profiled_traffic("k_dist_topk_bf16", "launch_list_om_plain_fp32_at_scale.md")
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None, "kernel": "k_dist_topk_bf16",
+                "frac": achieved / peak, "traffic": traffic,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
+                                  "(profiles/launch_list_om_plain_fp32_at_scale.md)"
+                                  if traffic else None,
+                "algorithmic_operand_bytes": 2.0 * (W["n_img"] + W["n_ref"]) * n_pix,
+                "kernel": "k_dist_topk_bf16",
                 "kernel_ms": k_ms, "peak_source": f"bf16_tflops ({peak_src}, burst)"}
 
     # --- the plain FP32 path on the same GPU, same frames -------------------
@@ -659,7 +691,11 @@ def main():
     # --- serving: Poisson arrivals at 2,000 frames/s against the resident set
     serving = None
     if not args.no_serving:
-        serving = {"bf16": measure_serving(rset, imgs_u16_host, 2000.0, 10_000, "bf16"),
+        serving = {"bf16_native": measure_serving(rset, imgs_u16_host, 2000.0, 10_000, "bf16",
+                                                  native=True),
+                   "bf16": measure_serving(rset, imgs_u16_host, 2000.0, 10_000, "bf16"),
+                   "plain_fp32_native": measure_serving(rset, imgs_u16_host, 2000.0, 4_000,
+                                                        "fp32", native=True),
                    "plain_fp32": measure_serving(rset, imgs_u16_host, 2000.0, 4_000, "fp32")}
 
     # --- accuracy against FP64 ---------------------------------------------

@@ -31,6 +31,8 @@ extern "C" {
 #define SPF_ERR_UNSUPPORTED (-6) /* device or shape not supported            */
 
 typedef struct spf_nufft_plan_s *spf_nufft_plan;
+typedef struct spf_merge_s *spf_merge;
+typedef struct spf_server_s *spf_server;
 
 /* ---- library ---------------------------------------------------------- */
 const char *spf_version(void);
@@ -156,6 +158,27 @@ int spf_nufft_interp_spread_orient(spf_nufft_plan plan, const float *d_quats,
                                    int64_t n_orient, const float *d_ppr, int64_t n_pix,
                                    double scale, const float *d_weights, void *stream);
 
+/* Type 1 in one call at explicit points (radians, |x| < 3 pi): zero the
+ * accumulator, spread the real strengths d_c, fold, FFT and deconvolve onto
+ * the modes (spf_nufft_t1_zero + _spread + _finish).  Replaces nufft_3d_t1 /
+ * NUFFT.adjoint before the support multiply and the 1/M^3
+ * (spinifel/autocorrelation.py:97-128, spinifel/extern/nufft_ext.py:287-327). */
+int spf_spread_t1(spf_nufft_plan plan, const float *d_x, const float *d_y, const float *d_z,
+                  const float *d_c, int64_t npts, int isign, float *d_out_re, float *d_out_im,
+                  void *stream);
+
+/* The FFT + deconvolution stage of either transform.  type 2: d_modes_in
+ * (times d_support when not NULL) is deconvolved, zero-padded and
+ * transformed onto the plan's fine grid (Re kept; spf_nufft_t2_set_modes
+ * with want_imag 0), d_modes_out_* must be NULL.  type 1: the plan's spread
+ * accumulator is folded, transformed and deconvolved into d_modes_out_re
+ * (and _im when not NULL) (spf_nufft_t1_finish), d_modes_in and d_support
+ * must be NULL.  The reference runs this stage inside cufinufft / finufft
+ * (spinifel/extern/nufft_ext.py:271-282, :310-321). */
+int spf_fft_deconv(spf_nufft_plan plan, int type, int isign, const float *d_modes_in,
+                   const float *d_support, float *d_modes_out_re, float *d_modes_out_im,
+                   void *stream);
+
 /* ---- orientation matching --------------------------------------------- */
 
 /* pyCudaKNearestNeighbors.cudaEuclideanDistance
@@ -204,6 +227,16 @@ int spf_dist_argmin_f32(const float *d_img, const float *d_img_sq, int64_t n_img
 int spf_best_unpack(const uint64_t *d_best, int64_t n_img, int32_t *d_idx,
                     float *d_dist, void *stream);
 
+/* The whole plain FP32 match in one call (spf_best_init +
+ * spf_dist_argmin_f32 + spf_best_unpack): best reference index and its
+ * FP32 distance for every image; d_best (n_img uint64) is caller scratch.
+ * Replaces SNM.euclidean_dist + argmin over all references
+ * (spinifel/sequential/orientation_matching.py:98-109,179). */
+int spf_dist_argmin_fp32(const float *d_img, const float *d_img_sq, int64_t n_img,
+                         const float *d_ref, const float *d_ref_sq, int64_t n_ref,
+                         int64_t n_pix, uint64_t *d_best, int32_t *d_idx, float *d_dist,
+                         void *stream);
+
 /* ---- autocorrelation merge: operator and device-resident CG -----------
  * Replaces Merge.setup_linops / W_matvec / cg
  * (spinifel/sequential/autocorrelation.py:152-225):
@@ -213,7 +246,6 @@ int spf_best_unpack(const uint64_t *d_best, int64_t n_img, int32_t *d_idx,
  * the direct Re T1(D T2(.)) / (M_ups^3 M^3) through an attached NUFFT plan;
  * reg the size-M circular filter by ifftshift(F_antisupport) (:116-128).
  * d_support and d_antisupport are M^3 floats (C order, centred). */
-typedef struct spf_merge_s *spf_merge;
 int spf_merge_create(int M, int M_ups, double rlambda, double flambda,
                      const float *d_support, const float *d_antisupport, spf_merge *out);
 int spf_merge_destroy(spf_merge merge);
@@ -236,6 +268,10 @@ int spf_merge_apply(spf_merge merge, int form, const double *d_x, double *d_y,
  * d_iters (device int, may be NULL) the iteration count.  No host
  * synchronisation: the launch sequence can be captured in a CUDA graph. */
 int spf_merge_cg(spf_merge merge, int form, const double *d_b, double *d_x, int x0_is_zero,
+                 int maxiter, double rtol, double *d_hist, int *d_iters, void *stream);
+/* The same solve under the name of the reference's step: Merge.solve_ac's
+ * cg(W, d, maxiter=...) (spinifel/sequential/autocorrelation.py:198-225). */
+int spf_cg_solve(spf_merge merge, int form, const double *d_b, double *d_x, int x0_is_zero,
                  int maxiter, double rtol, double *d_hist, int *d_iters, void *stream);
 
 /* ---- BF16 tensor-core matching with exact FP32 re-rank ----------------
@@ -310,6 +346,45 @@ int spf_match_bf16_static(const void *d_img_bf16, const float *d_img, const floa
                           const float *d_ref_sq, const float *d_ref_m2, float ref_sq_max,
                           int64_t n_ref, int64_t n_pix, int64_t ld, int32_t *d_idx,
                           float *d_dist, int32_t *d_uncertified, void *stream);
+
+/* ---- continuous-batching server ----------------------------------------
+ * Streaming form of SNM.slicing_and_match's matching step
+ * (spinifel/sequential/orientation_matching.py:113-186) against references
+ * kept resident: requests of 1..slot_frames uint16 frames are queued, a
+ * server thread packs whatever has arrived into a free slot (one CUDA stream
+ * each; n_slots in flight) while the in-flight frames stay within
+ * hbm_budget bytes (<= 0: slot_frames * n_slots frames' worth), and runs
+ * copy-in, ingest, the bf16 tcgen05 top-8 + exact FP32 re-rank (path 0) or
+ * the plain FP32 pass (path 1), and the certified completion of open frames.
+ * Results equal spf_dist_argmin_fp32's on the same frames.  The reference
+ * buffers (as for spf_rerank_fp32; d_ref_bf16/d_ref_m2 may be NULL for
+ * path 1) must outlive the server.  spf_serve_create allocates every buffer
+ * up front and starts the thread on `device`.
+ * spf_serve_submit queues h_counts [n_frames][n_pix] (read when the request
+ * is launched; keep it valid until the request completes; pinned memory is
+ * copied directly, pageable memory through pinned staging) and returns a
+ * ticket; h_idx / h_dist (n_frames each, h_dist may be NULL) receive the
+ * answer before the request is marked done.  arrival: the request's arrival
+ * time on spf_serve_clock() (< 0 = now), the start of its latency.
+ * spf_serve_wait blocks up to timeout_ms (< 0 = until done); *done = 1 once
+ * the request completed, and its status is returned (the ticket is then
+ * released).  A bounded device wait that gave up fails the slot's requests
+ * with SPF_ERR_TIMEOUT while the device error word stays set.
+ * spf_serve_stats: h_out[0..8] = requests, frames, launches, uncertified
+ * frames, range-list overflows, summed GPU ms of the matching stage, budget
+ * waits, p50 and p99 latency in ms.  spf_serve_destroy completes queued
+ * requests, stops the thread and frees the buffers. */
+double spf_serve_clock(void);
+int spf_serve_create(int device, const void *d_ref_bf16, const float *d_ref,
+                     const float *d_ref_sq, const float *d_ref_m2, float ref_sq_max,
+                     int64_t n_ref, int64_t n_pix, int64_t ld, int path, int64_t slot_frames,
+                     int n_slots, int64_t hbm_budget, spf_server *out);
+int spf_serve_submit(spf_server server, const uint16_t *h_counts, int64_t n_frames,
+                     int32_t *h_idx, float *h_dist, double arrival, int64_t *ticket);
+int spf_serve_wait(spf_server server, int64_t ticket, int64_t timeout_ms, int *done);
+int spf_serve_stats(spf_server server, double *h_out, int n_out);
+int spf_serve_latencies(spf_server server, double *h_ms, int64_t cap, int64_t *n);
+int spf_serve_destroy(spf_server server);
 
 /* d_out[p] = max over rows r of x[r, p]^2 (n_pix floats). */
 int spf_col_maxsq_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_out,

@@ -113,6 +113,23 @@ SIGNATURES = {
     "spf_row_norms_f32": [_c_void_p, _i64, _i64, _c_void_p, _c_void_p, _c_void_p],
     "spf_f32_to_bf16": [_c_void_p, _i64, _i64, _c_void_p, _i64, _c_void_p],
     "spf_gather_rows": [_c_void_p, _i64, _i64, _c_void_p, _i64, _c_void_p, _c_void_p],
+    "spf_spread_t1": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _i64, _int,
+                      _c_void_p, _c_void_p, _c_void_p],
+    "spf_fft_deconv": [_c_void_p, _int, _int, _c_void_p, _c_void_p, _c_void_p, _c_void_p,
+                       _c_void_p],
+    "spf_dist_argmin_fp32": [_c_void_p, _c_void_p, _i64, _c_void_p, _c_void_p, _i64, _i64,
+                             _c_void_p, _c_void_p, _c_void_p, _c_void_p],
+    "spf_cg_solve": [_c_void_p, _int, _c_void_p, _c_void_p, _int, _int, _dbl, _c_void_p,
+                     _c_void_p, _c_void_p],
+    "spf_serve_clock": [],
+    "spf_serve_create": [_int, _c_void_p, _c_void_p, _c_void_p, _c_void_p, ctypes.c_float, _i64,
+                         _i64, _i64, _int, _i64, _int, _i64, ctypes.POINTER(_c_void_p)],
+    "spf_serve_submit": [_c_void_p, _c_void_p, _i64, _c_void_p, _c_void_p, _dbl,
+                         ctypes.POINTER(_i64)],
+    "spf_serve_wait": [_c_void_p, _i64, _i64, ctypes.POINTER(_int)],
+    "spf_serve_stats": [_c_void_p, ctypes.POINTER(_dbl), _int],
+    "spf_serve_latencies": [_c_void_p, ctypes.POINTER(_dbl), _i64, ctypes.POINTER(_i64)],
+    "spf_serve_destroy": [_c_void_p],
 }
 
 _RESTYPES = {
@@ -121,6 +138,7 @@ _RESTYPES = {
     "spf_last_error": ctypes.c_char_p,
     "spf_launch_count": ctypes.c_uint64,
     "spf_dist_topk_bf16_tiles": ctypes.c_int64,
+    "spf_serve_clock": ctypes.c_double,
 }
 
 _lock = threading.Lock()

@@ -77,7 +77,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_v: bool = False) -> 
     libdir = _cuda_lib_dir(nvcc)
     tmp = LIB + f".tmp{os.getpid()}"
     cmd = [nvcc, *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", tmp,
-           *[o for o, _ in results], "-L", libdir, "-lcufft",
+           *[o for o, _ in results], "-L", libdir, "-lcufft", "-lpthread",
            f"-Xlinker=-rpath={libdir}"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -570,4 +570,9 @@ int spf_merge_cg(spf_merge_s *G, int form, const double *d_b, double *d_x, int x
   return SPF_OK;
 }
 
+int spf_cg_solve(spf_merge_s *G, int form, const double *d_b, double *d_x, int x0_is_zero,
+                 int maxiter, double rtol, double *d_hist, int *d_iters, void *stream) {
+  return spf_merge_cg(G, form, d_b, d_x, x0_is_zero, maxiter, rtol, d_hist, d_iters, stream);
+}
+
 }  // extern "C"

@@ -524,4 +524,14 @@ int spf_best_unpack(const uint64_t *d_best, int64_t n_img, int32_t *d_idx, float
   return check_launch("spf_best_unpack");
 }
 
+int spf_dist_argmin_fp32(const float *d_img, const float *d_img_sq, int64_t n_img,
+                         const float *d_ref, const float *d_ref_sq, int64_t n_ref, int64_t n_pix,
+                         uint64_t *d_best, int32_t *d_idx, float *d_dist, void *stream) {
+  SPF_REQUIRE(n_img == 0 || (d_idx && d_dist), "spf_dist_argmin_fp32: NULL output");
+  SPF_TRY(spf_best_init(d_best, n_img, stream));
+  SPF_TRY(spf_dist_argmin_f32(d_img, d_img_sq, n_img, d_ref, d_ref_sq, n_ref, n_pix, 0, d_best,
+                              stream));
+  return spf_best_unpack(d_best, n_img, d_idx, d_dist, stream);
+}
+
 }  // extern "C"

@@ -1317,4 +1317,26 @@ int spf_nufft_t1_finish(spf_nufft_plan P, int isign, float *d_out_re, float *d_o
   return check_launch("k_t1_extract");
 }
 
+int spf_spread_t1(spf_nufft_plan P, const float *d_x, const float *d_y, const float *d_z,
+                  const float *d_c, int64_t npts, int isign, float *d_out_re, float *d_out_im,
+                  void *stream) {
+  SPF_TRY(spf_nufft_t1_zero(P, stream));
+  SPF_TRY(spf_nufft_t1_spread(P, d_x, d_y, d_z, d_c, npts, stream));
+  return spf_nufft_t1_finish(P, isign, d_out_re, d_out_im, stream);
+}
+
+int spf_fft_deconv(spf_nufft_plan P, int type, int isign, const float *d_modes_in,
+                   const float *d_support, float *d_modes_out_re, float *d_modes_out_im,
+                   void *stream) {
+  if (type == 2) {
+    SPF_REQUIRE(!d_modes_out_re && !d_modes_out_im,
+                "spf_fft_deconv: type 2 keeps its result in the plan (outputs must be NULL)");
+    return spf_nufft_t2_set_modes(P, d_modes_in, d_support, isign, 0, stream);
+  }
+  SPF_REQUIRE(type == 1, "spf_fft_deconv: type must be 1 or 2");
+  SPF_REQUIRE(!d_modes_in && !d_support,
+              "spf_fft_deconv: type 1 reads the plan's accumulator (inputs must be NULL)");
+  return spf_nufft_t1_finish(P, isign, d_modes_out_re, d_modes_out_im, stream);
+}
+
 }  // extern "C"

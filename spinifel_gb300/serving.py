@@ -24,6 +24,7 @@ result is on the host.
 from __future__ import annotations
 
 import collections
+import ctypes
 import threading
 import time
 from concurrent.futures import Future
@@ -344,6 +345,126 @@ class OrientationServer:
     def latency_ms(self):
         lat = np.array([(r.done_at - r.arrival) * 1e3 for r in self.completed])
         return lat
+
+
+class _NativeFuture:
+    """Result of one request to the native server (the Future API subset
+    run_schedule uses)."""
+
+    def __init__(self, server: "NativeOrientationServer", ticket: int, n: int, keep):
+        self._srv, self._ticket, self._keep = server, ticket, keep
+        self._idx = np.empty(n, dtype=np.int32)
+        self._dist = np.empty(n, dtype=np.float32)
+        self._done = False
+
+    def _ptrs(self):
+        return (ctypes.c_void_p(self._idx.ctypes.data), ctypes.c_void_p(self._dist.ctypes.data))
+
+    def done(self) -> bool:
+        if not self._done:
+            self._wait(0)
+        return self._done
+
+    def _wait(self, timeout_ms: int):
+        flag = ctypes.c_int(0)
+        _lib.call("spf_serve_wait", self._srv._h, self._ticket, int(timeout_ms),
+                  ctypes.byref(flag))
+        if flag.value:
+            self._done = True
+            self._keep = None
+            self._srv._inflight.pop(self._ticket, None)
+
+    def result(self, timeout: float | None = None) -> np.ndarray:
+        if not self._done:
+            self._wait(-1 if timeout is None else int(timeout * 1e3))
+            if not self._done:
+                raise TimeoutError("request not complete")
+        return self._idx.astype(np.int64)
+
+    @property
+    def distances(self) -> np.ndarray:
+        self.result()
+        return self._dist
+
+
+class NativeOrientationServer:
+    """The continuous-batching server of the C ABI (spf_serve_*): admission,
+    launches and completion run on a native thread of the library, so no
+    Python code sits between a request's arrival and its result.  Same
+    constructor arguments and submit / close / latency_ms as
+    OrientationServer; stats are read from the library."""
+
+    def __init__(self, refs: "matching.ReferenceSet", slot_frames: int = 512, n_slots: int = 3,
+                 hbm_budget: int | None = None, path: str = "bf16"):
+        if path not in ("bf16", "fp32"):
+            raise ValueError("path is 'bf16' or 'fp32'")
+        self.refs = refs
+        self.n_pix = refs.n_pix
+        self.slot_frames = slot_frames
+        self.device = refs.f32.device
+        h = ctypes.c_void_p()
+        _lib.call("spf_serve_create", self.device.index or 0, _lib.ptr(refs.bf16),
+                  _lib.ptr(refs.f32), _lib.ptr(refs.sq), _lib.ptr(refs.m2),
+                  float(refs.sq_max), refs.n_ref, refs.n_pix, refs.ld,
+                  0 if path == "bf16" else 1, slot_frames, n_slots, int(hbm_budget or 0),
+                  ctypes.byref(h))
+        self._h = h
+        self._inflight = {}  # ticket -> future: its buffers stay alive until the library is done
+
+    def submit(self, frames_u16: torch.Tensor, arrival: float | None = None) -> _NativeFuture:
+        if frames_u16.dim() != 2 or frames_u16.shape[1] != self.n_pix:
+            raise ValueError(f"frames must be [n, {self.n_pix}]")
+        if frames_u16.dtype not in (torch.int16, torch.uint16) or frames_u16.is_cuda:
+            raise TypeError("frames must be 16-bit photon counts in host memory")
+        if not frames_u16.is_contiguous():
+            frames_u16 = frames_u16.contiguous()
+        n = int(frames_u16.shape[0])
+        # arrival is on time.perf_counter(); the library measures on its own clock
+        t_lib = -1.0
+        if arrival is not None:
+            t_lib = float(_lib.lib().spf_serve_clock()) - (time.perf_counter() - arrival)
+        fut = _NativeFuture(self, 0, n, frames_u16)
+        ticket = ctypes.c_int64(0)
+        pi, pd = fut._ptrs()
+        _lib.call("spf_serve_submit", self._h, ctypes.c_void_p(frames_u16.data_ptr()), n, pi, pd,
+                  t_lib, ctypes.byref(ticket))
+        fut._ticket = ticket.value
+        self._inflight[ticket.value] = fut
+        return fut
+
+    @property
+    def stats(self) -> dict:
+        v = (ctypes.c_double * 9)()
+        _lib.call("spf_serve_stats", self._h, v, 9)
+        keys = ("requests", "frames", "launches", "uncertified", "range_overflow", "t_gpu_ms",
+                "budget_waits", "p50_ms", "p99_ms")
+        return dict(zip(keys, list(v)))
+
+    def latency_ms(self) -> np.ndarray:
+        n = ctypes.c_int64(0)
+        _lib.call("spf_serve_latencies", self._h, None, 0, ctypes.byref(n))
+        out = np.empty(n.value, dtype=np.float64)
+        _lib.call("spf_serve_latencies", self._h,
+                  out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n.value, ctypes.byref(n))
+        return out
+
+    def close(self):
+        if self._h:
+            _lib.call("spf_serve_destroy", self._h)  # completes every queued request
+            self._h = None
+            self._inflight.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def poisson_schedule(total_frames: int, rate_fps: float, rng: np.random.Generator,

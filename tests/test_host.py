@@ -81,6 +81,38 @@ def test_library_rejects_bad_arguments_without_a_device(lib):
     assert lib.spf_status_string(_lib.SPF_ERR_TIMEOUT) == b"device wait timed out"
 
 
+def test_named_entry_points_and_server_reject_bad_arguments_without_a_device(lib):
+    from spinifel_gb300 import _lib
+
+    E = _lib.SPF_ERR_ARG
+    srv = ctypes.c_void_p()
+    P = ctypes.c_void_p(16)
+    args = [0, P, P, P, P, 1.0, 1000, 64, 64]
+    assert lib.spf_serve_create(*args, 2, 64, 2, 0, ctypes.byref(srv)) == E      # bad path
+    assert b"path" in lib.spf_last_error()
+    assert lib.spf_serve_create(0, None, P, P, None, 1.0, 1000, 64, 64, 0, 64, 2, 0,
+                                ctypes.byref(srv)) == E                          # bf16 refs missing
+    assert lib.spf_serve_create(*args[:7], 60, 60, 0, 64, 2, 0, ctypes.byref(srv)) == E  # ld % 8
+    assert lib.spf_serve_create(*args, 0, 0, 2, 0, ctypes.byref(srv)) == E       # no slot frames
+    assert lib.spf_serve_create(*args, 0, 64, 17, 0, ctypes.byref(srv)) == E     # too many slots
+    assert srv.value is None
+    t = ctypes.c_int64()
+    flag = ctypes.c_int()
+    assert lib.spf_serve_submit(None, P, 1, None, None, -1.0, ctypes.byref(t)) == E
+    assert lib.spf_serve_wait(None, 1, 0, ctypes.byref(flag)) == E
+    assert lib.spf_serve_stats(None, None, 0) == E
+    assert lib.spf_serve_destroy(None) == _lib.SPF_OK
+    c0 = lib.spf_serve_clock()
+    assert lib.spf_serve_clock() >= c0 > 0
+    # the scope-table names: argument checks before any device work
+    assert lib.spf_fft_deconv(None, 2, -1, P, None, None, None, None) == E       # no plan
+    assert lib.spf_spread_t1(None, P, P, P, P, 10, 1, P, None, None) == E
+    assert lib.spf_cg_solve(None, 0, P, P, 1, 10, 1e-5, None, None, None) == E
+    assert lib.spf_dist_argmin_fp32(None, None, 0, None, None, 5, 16, None, None, None,
+                                    None) == _lib.SPF_OK                         # empty: no-op
+    assert lib.spf_dist_argmin_fp32(P, P, 4, P, P, 5, 16, P, None, None, None) == E
+
+
 def test_product_path_has_no_cpu_fallback(tmp_path):
     from spinifel_gb300 import _lib
 
