@@ -324,6 +324,97 @@ def run_nufft(args):
     print(json.dumps(rec), flush=True)
 
 
+def _phasing_ac(M, seed):
+    """Centred autocorrelation of a compact density of 20 Gaussian blobs."""
+    rng = np.random.default_rng(seed)
+    ax = np.arange(M) - M // 2
+    X, Y, Z = np.meshgrid(ax, ax, ax, indexing="ij")
+    rho = np.zeros((M, M, M))
+    for _ in range(20):
+        c = rng.uniform(-M / 8, M / 8, 3)
+        sig = rng.uniform(1.0, 3.0)
+        rho += rng.uniform(0.5, 1.0) * np.exp(
+            -((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2) / (2 * sig ** 2))
+    F = np.fft.fftn(np.fft.ifftshift(rho))
+    return np.fft.fftshift(np.fft.ifftn(np.abs(F) ** 2).real), rng
+
+
+def run_phasing(args):
+    """Phase retrieval with the reference's default schedule (nER 10, nHIO 5,
+    5 phase loops, beta 0.9: 135 ER/HIO iterations + 5 shrink-wraps) at
+    M = 81 (Mquat 20, the default grid) and M = 149 (Mquat 37): ms per
+    phase() on the device (FP64), and the FP64 numpy oracle on the host
+    cores at M = 81 as the CPU baseline."""
+    import torch
+
+    from spinifel_gb300 import _lib
+    from spinifel_gb300.phasing import Phaser
+
+    sched = dict(n_phase_loops=5, nER=10, nHIO=5, beta=0.9)
+    iters = sched["n_phase_loops"] * (2 * sched["nER"] + sched["nHIO"]) + sched["nER"]
+    out = {"metric": "phase retrieval: ms per phase() (ER/HIO/shrink-wrap, FP64)",
+           "unit": "ms", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
+           "dtype": "f64", "config": {"workload": "phasing", **sched, "fft_iterations": iters},
+           "grids": {}}
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for Mquat in (20, 37):
+        M = 4 * Mquat + 1
+        ac, rng = _phasing_ac(M, 20261203 + M)
+        rho0 = rng.random((M, M, M))
+        ac_t = torch.as_tensor(ac, device=dev)
+        rho_t = torch.as_tensor(rho0, device=dev)
+        ph = Phaser(M)
+
+        def once():
+            ph.set_ac(ac_t)
+            ph.create_support(Mquat)
+            ph.set_state(rho_t)
+            ph.run(sched["n_phase_loops"], sched["nER"], sched["nHIO"], sched["beta"])
+            return ph.finish()
+
+        once()
+        torch.cuda.synchronize()
+        l0 = _lib.launch_count()
+        ts = []
+        for _ in range(max(args.steps, 3)):
+            e0.record()
+            once()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ms = float(np.median(ts))
+        # the iteration loop alone
+        ph.set_state(rho_t)
+        e0.record()
+        ph.er(100)
+        e1.record()
+        torch.cuda.synchronize()
+        per_iter = e0.elapsed_time(e1) / 100
+        n = M ** 3
+        # per ER iteration: D2Z + projection + Z2D + update, >= ~80 B per voxel
+        out["grids"][str(M)] = {"ms_per_phase": ms, "ms_per_er_iteration": per_iter,
+                                "launches_per_phase": (_lib.launch_count() - l0) // len(ts),
+                                "voxels": n, "min_bytes_per_iteration": 80 * n,
+                                "achieved_gbs_min_bytes": 80 * n / (per_iter / 1e3) / 1e9}
+        ph.close()
+    out["value"] = out["grids"]["81"]["ms_per_phase"]
+    if not args.no_cpu_baseline:
+        from oracle import phasing as oph
+
+        ac, rng = _phasing_ac(81, 20261203 + 81)
+        rho0 = rng.random((81, 81, 81))
+        t0 = time.perf_counter()
+        oph.phase(ac, 20, None, rho0, nER=sched["nER"], nHIO=sched["nHIO"], beta=sched["beta"],
+                  N_phase_loops=sched["n_phase_loops"])
+        t1 = time.perf_counter()
+        out["cpu_baseline"] = {"value": (t1 - t0) * 1e3, "unit": "ms", "cores": os.cpu_count(),
+                               "kind": "port", "sample": "one full phase() at M = 81 "
+                               "(numpy FP64 FFTs, scipy filters)"}
+    print(json.dumps(out), flush=True)
+
+
 def run_merge(args):
     """Autocorrelation merge at 151^3 with 2,000 frames x 65,536 pixels
     (1.31e8 points): setup (two type-1 NUFFTs), then 30 CG iterations in the
@@ -465,13 +556,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--workload", default="match",
-                    choices=["match", "merge", "serving", "nufft"])
+                    choices=["match", "merge", "serving", "nufft", "phasing"])
     args = ap.parse_args()
     if args.workload == "merge":
         run_merge(args)
         return
     if args.workload == "nufft":
         run_nufft(args)
+        return
+    if args.workload == "phasing":
+        run_phasing(args)
         return
     if args.workload == "serving":
         WORKLOAD.update(name="om-serving-200k", n_ref=200_000, n_img=20_000)

@@ -33,6 +33,7 @@ extern "C" {
 typedef struct spf_nufft_plan_s *spf_nufft_plan;
 typedef struct spf_merge_s *spf_merge;
 typedef struct spf_server_s *spf_server;
+typedef struct spf_phaser_s *spf_phaser;
 
 /* ---- library ---------------------------------------------------------- */
 const char *spf_version(void);
@@ -269,6 +270,20 @@ int spf_merge_apply(spf_merge merge, int form, const double *d_x, double *d_y,
  * synchronisation: the launch sequence can be captured in a CUDA graph. */
 int spf_merge_cg(spf_merge merge, int form, const double *d_b, double *d_x, int x0_is_zero,
                  int maxiter, double rtol, double *d_hist, int *d_iters, void *stream);
+/* Regularisation sweep (the MPI merge's per-rank lambdas,
+ * spinifel/mpi/autocorrelation.py:64-68,160-214) as one batched solve: n_lambda
+ * systems W_l x = conv(x) + rlambda_l x + flambda_l reg(x) = d_adb +
+ * rlambda_l x0 (h_rlambda / h_flambda: n_lambda host doubles; the merge's own
+ * rlambda / flambda are not used), each CG from x0 (d_x0 M^3 doubles, NULL =
+ * 0) with scipy's stopping rule, all systems advanced by the same launches
+ * (batched cuFFT plans, allocated on the first call for a given n_lambda).
+ * d_x: n_lambda x M^3 solutions; d_norms (may be NULL): 2 n_lambda doubles,
+ * ||x_l|| and ||W_l x_l - d_l||; d_hist (may be NULL): n_lambda x maxiter
+ * residual norms; d_iters (may be NULL): n_lambda ints.  Toeplitz form. */
+int spf_merge_cg_sweep(spf_merge merge, int n_lambda, const double *h_rlambda,
+                       const double *h_flambda, const double *d_adb, const double *d_x0,
+                       double *d_x, int maxiter, double rtol, double *d_norms, double *d_hist,
+                       int *d_iters, void *stream);
 /* The same solve under the name of the reference's step: Merge.solve_ac's
  * cg(W, d, maxiter=...) (spinifel/sequential/autocorrelation.py:198-225). */
 int spf_cg_solve(spf_merge merge, int form, const double *d_b, double *d_x, int x0_is_zero,
@@ -385,6 +400,44 @@ int spf_serve_wait(spf_server server, int64_t ticket, int64_t timeout_ms, int *d
 int spf_serve_stats(spf_server server, double *h_out, int n_out);
 int spf_serve_latencies(spf_server server, double *h_ms, int64_t cap, int64_t *n);
 int spf_serve_destroy(spf_server server);
+
+/* ---- phase retrieval ----------------------------------------------------
+ * ER / HIO / shrink-wrap of spinifel/sequential/phasing.py in FP64 on the
+ * device, for an M^3 grid (M odd in the reference: 4 Mquat + 1).  Arrays
+ * with a trailing underscore are ifftshifted, as in the reference.
+ * spf_phase_set_ac: ac (M^3 doubles, centred) -> ac_filt_ =
+ *   ifftshift(gaussian_filter(max(ac, 0), sigma 1, truncate 2, zero
+ *   boundary)) and amplitudes_ = sqrt(|fftn(ac_filt_)|)  (phasing.py:250-257).
+ * spf_phase_create_support: support_ = central cube [Mquat, M-Mquat)^3 &
+ *   ac_filt_ > 1e-2 max(ac_filt_)  (create_support_, :84-107).
+ * spf_phase_set_state / _get_state copy rho_ (M^3 doubles) and support_
+ *   (M^3 bytes, 0/1) in or out (either may be NULL).
+ * spf_phase_er / _hio: n_loops of ER (:130-147) / HIO (:151-169), the
+ *   Fourier projection replacing every amplitude but the (0,0,0) one.
+ * spf_phase_shrink_wrap: support_ = gaussian_filter(|rho_|, sigma, periodic)
+ *   > threshold, threshold std * weight (method 0) or max|rho_| * cutoff *
+ *   weight (method 1)  (:193-221).
+ * spf_phase_run: phase()'s schedule (:270-282): n_phase_loops x (ER, HIO,
+ *   ER, shrink-wrap sigma 1), then ER.
+ * spf_phase_finish: recenter rho_ and support_ on the centre of mass of
+ *   |rho_| (rounded half to even; the three shifts go to h_shift when not
+ *   NULL; synchronises the stream once), then d_ac_phased (M^3 doubles,
+ *   centred) = fftshift(|ifftn(|fftn(rho_)|^2)|)  (:287-309).
+ * No host synchronisation except in spf_phase_finish. */
+int spf_phase_create(int M, spf_phaser *out);
+int spf_phase_destroy(spf_phaser phaser);
+int spf_phase_set_ac(spf_phaser phaser, const double *d_ac, void *stream);
+int spf_phase_create_support(spf_phaser phaser, int Mquat, void *stream);
+int spf_phase_set_state(spf_phaser phaser, const double *d_rho_, const uint8_t *d_support_,
+                        void *stream);
+int spf_phase_get_state(spf_phaser phaser, double *d_rho_, uint8_t *d_support_, void *stream);
+int spf_phase_er(spf_phaser phaser, int n_loops, double rho_max, void *stream);
+int spf_phase_hio(spf_phaser phaser, int n_loops, double beta, double rho_max, void *stream);
+int spf_phase_shrink_wrap(spf_phaser phaser, double sigma, int method, double weight,
+                          double cutoff, void *stream);
+int spf_phase_run(spf_phaser phaser, int n_phase_loops, int n_er, int n_hio, double beta,
+                  double rho_max, int method, double weight, double cutoff, void *stream);
+int spf_phase_finish(spf_phaser phaser, double *d_ac_phased, int *h_shift, void *stream);
 
 /* d_out[p] = max over rows r of x[r, p]^2 (n_pix floats). */
 int spf_col_maxsq_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_out,

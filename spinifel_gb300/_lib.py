@@ -130,6 +130,20 @@ SIGNATURES = {
     "spf_serve_stats": [_c_void_p, ctypes.POINTER(_dbl), _int],
     "spf_serve_latencies": [_c_void_p, ctypes.POINTER(_dbl), _i64, ctypes.POINTER(_i64)],
     "spf_serve_destroy": [_c_void_p],
+    "spf_merge_cg_sweep": [_c_void_p, _int, ctypes.POINTER(_dbl), ctypes.POINTER(_dbl),
+                           _c_void_p, _c_void_p, _c_void_p, _int, _dbl, _c_void_p, _c_void_p,
+                           _c_void_p, _c_void_p],
+    "spf_phase_create": [_int, ctypes.POINTER(_c_void_p)],
+    "spf_phase_destroy": [_c_void_p],
+    "spf_phase_set_ac": [_c_void_p, _c_void_p, _c_void_p],
+    "spf_phase_create_support": [_c_void_p, _int, _c_void_p],
+    "spf_phase_set_state": [_c_void_p, _c_void_p, _c_void_p, _c_void_p],
+    "spf_phase_get_state": [_c_void_p, _c_void_p, _c_void_p, _c_void_p],
+    "spf_phase_er": [_c_void_p, _int, _dbl, _c_void_p],
+    "spf_phase_hio": [_c_void_p, _int, _dbl, _dbl, _c_void_p],
+    "spf_phase_shrink_wrap": [_c_void_p, _dbl, _int, _dbl, _dbl, _c_void_p],
+    "spf_phase_run": [_c_void_p, _int, _int, _int, _dbl, _dbl, _int, _dbl, _dbl, _c_void_p],
+    "spf_phase_finish": [_c_void_p, _c_void_p, ctypes.POINTER(_int), _c_void_p],
 }
 
 _RESTYPES = {

@@ -21,9 +21,14 @@
 // whole solve can be captured in one CUDA graph.
 #include <cufft.h>
 
+#include <vector>
+
 #include "common.cuh"
 
 #include "../../include/spinifel_gb300.h"
+
+struct Sweep;
+void free_sweep(Sweep *w);
 
 struct spf_merge_s {
   int dev = 0;
@@ -59,6 +64,7 @@ struct spf_merge_s {
   int det[3] = {0, 0, 0};
   bool sorted = false;
   double coord_scale = 0;
+  struct Sweep *sweep = nullptr;  // batched buffers of spf_merge_cg_sweep
 };
 
 // device scalar slots
@@ -450,6 +456,7 @@ int spf_merge_destroy(spf_merge_s *G) {
                   G->conv_out, G->reg_in, G->reg_freq, G->reg_out, G->modes, G->t1_out,
                   G->r, G->p, G->q, G->partial, G->scal, G->flags};
   for (void *b : bufs) cudaFree(b);
+  free_sweep(G->sweep);
   if (G->plans_ok) {
     cufftDestroy(G->r2c_L);
     cufftDestroy(G->c2r_L);
@@ -576,3 +583,390 @@ int spf_cg_solve(spf_merge_s *G, int form, const double *d_b, double *d_x, int x
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Regularisation sweep: the MPI merge gives every rank its own
+// (rlambda, flambda) and keeps the result the L-curve rule picks
+// (spinifel/mpi/autocorrelation.py:64-68, 173-214).  Here the n systems
+//   W_l x = conv(x) + rlambda_l x + flambda_l reg(x) = ADb + rlambda_l x0
+// run as one batched CG on one GPU: every vector is [n][M^3], the FFTs are
+// batched cuFFT plans, and each launch covers all systems (blockIdx.y, or one
+// block per system for the scalar stages), so an iteration costs the same
+// number of launches for any n.  Each system keeps its own CG scalars and
+// stops on scipy's rule independently.
+struct Sweep {
+  int nl = 0;
+  double *r = nullptr, *p = nullptr, *q = nullptr, *d = nullptr, *lam = nullptr;
+  float *conv_in = nullptr, *conv_out = nullptr;
+  float2 *conv_freq = nullptr;
+  double *reg_in = nullptr, *reg_out = nullptr;
+  double2 *reg_freq = nullptr;
+  double *partial = nullptr, *scal = nullptr;
+  int *flags = nullptr;
+  cufftHandle r2c = 0, c2r = 0, d2z = 0, z2d = 0;
+  bool plans = false;
+};
+
+void free_sweep(Sweep *w) {
+  if (!w) return;
+  void *bufs[] = {w->r,       w->p,        w->q,         w->d,       w->lam,
+                  w->conv_in, w->conv_out, w->conv_freq, w->reg_in,  w->reg_out,
+                  w->reg_freq, w->partial, w->scal,      w->flags};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  if (w->plans) {
+    cufftDestroy(w->r2c);
+    cufftDestroy(w->c2r);
+    cufftDestroy(w->d2z);
+    cufftDestroy(w->z2d);
+  }
+  delete w;
+}
+
+namespace spf {
+namespace cg {
+
+static int make_sweep(spf_merge_s *G, int nl) {
+  if (G->sweep && G->sweep->nl == nl) return SPF_OK;
+  free_sweep(G->sweep);
+  G->sweep = nullptr;
+  auto *w = new Sweep();
+  w->nl = nl;
+  const int64_t n = G->n;
+  int st = SPF_OK;
+  auto alloc = [&](void **ptr, size_t bytes) {
+    if (st == SPF_OK) st = check_cuda(cudaMalloc(ptr, bytes), "spf_merge_cg_sweep");
+  };
+  alloc((void **)&w->r, nl * n * sizeof(double));
+  alloc((void **)&w->p, nl * n * sizeof(double));
+  alloc((void **)&w->q, nl * n * sizeof(double));
+  alloc((void **)&w->d, nl * n * sizeof(double));
+  alloc((void **)&w->lam, 2 * nl * sizeof(double));
+  alloc((void **)&w->conv_in, nl * G->nL * sizeof(float));
+  alloc((void **)&w->conv_out, nl * G->nL * sizeof(float));
+  alloc((void **)&w->conv_freq, nl * G->nLh * sizeof(float2));
+  alloc((void **)&w->reg_in, nl * n * sizeof(double));
+  alloc((void **)&w->reg_out, nl * n * sizeof(double));
+  alloc((void **)&w->reg_freq, nl * G->nMh * sizeof(double2));
+  alloc((void **)&w->partial, nl * RED_BLOCKS * sizeof(double));
+  alloc((void **)&w->scal, nl * S_COUNT * sizeof(double));
+  alloc((void **)&w->flags, nl * 2 * sizeof(int));
+  if (st == SPF_OK) {
+    int dl[3] = {G->L, G->L, G->L}, dm[3] = {G->M, G->M, G->M};
+    const int Lh = G->L / 2 + 1, Mh = G->M / 2 + 1;
+    int el[3] = {G->L, G->L, Lh}, em[3] = {G->M, G->M, Mh};
+    bool ok =
+        cufftPlanMany(&w->r2c, 3, dl, dl, 1, (int)G->nL, el, 1, (int)G->nLh, CUFFT_R2C, nl) ==
+            CUFFT_SUCCESS &&
+        cufftPlanMany(&w->c2r, 3, dl, el, 1, (int)G->nLh, dl, 1, (int)G->nL, CUFFT_C2R, nl) ==
+            CUFFT_SUCCESS &&
+        cufftPlanMany(&w->d2z, 3, dm, dm, 1, (int)n, em, 1, (int)G->nMh, CUFFT_D2Z, nl) ==
+            CUFFT_SUCCESS &&
+        cufftPlanMany(&w->z2d, 3, dm, em, 1, (int)G->nMh, dm, 1, (int)n, CUFFT_Z2D, nl) ==
+            CUFFT_SUCCESS;
+    w->plans = ok;
+    if (!ok) {
+      set_error("spf_merge_cg_sweep: batched cuFFT plans failed (n = %d)", nl);
+      st = SPF_ERR_CUDA;
+    }
+  }
+  if (st == SPF_OK)
+    st = check_cuda(cudaMemset(w->conv_in, 0, nl * G->nL * sizeof(float)), "spf_merge_cg_sweep");
+  if (st != SPF_OK) {
+    free_sweep(w);
+    return st;
+  }
+  G->sweep = w;
+  return SPF_OK;
+}
+
+// d_l = adb + rlambda_l x0 and x_l = x0 (0 when x0 is NULL)
+__global__ void k_sw_rhs(const double *__restrict__ adb, const double *__restrict__ x0,
+                         const double *__restrict__ lam, double *__restrict__ d,
+                         double *__restrict__ x, int64_t n) {
+  const int l = blockIdx.y;
+  const double rl = lam[2 * l];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x0 ? x0[i] : 0.0;
+    d[l * n + i] = adb[i] + rl * v;
+    x[l * n + i] = v;
+  }
+}
+
+// operator inputs of every system: S.v into the padded L grid (FP32) and the
+// ifftshifted M grid (FP64); with p/r/scal/flags the CG update p = r + beta p
+// comes first (systems that stopped keep p)
+__global__ void k_sw_load(double *__restrict__ v, const double *__restrict__ r,
+                          const double *__restrict__ scal, const int *__restrict__ flags,
+                          const float *__restrict__ S, int M, int L, float *__restrict__ conv_in,
+                          double *__restrict__ reg_in) {
+  const int l = blockIdx.y;
+  const int64_t n = (int64_t)M * M * M, nL = (int64_t)L * L * L;
+  const bool update = r != nullptr && !flags[2 * l];
+  const double beta = r ? scal[l * S_COUNT + S_BETA] : 0.0;
+  const int h = M / 2;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double pv = v[l * n + i];
+    if (update) {
+      pv = r[l * n + i] + beta * pv;
+      v[l * n + i] = pv;
+    }
+    const double vd = pv * (double)S[i];
+    const int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
+    conv_in[l * nL + ((int64_t)a * L + b) * L + c] = (float)vd;
+    const int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
+    reg_in[l * n + ((int64_t)ja * M + jb) * M + jc] = vd;
+  }
+}
+
+__global__ void k_sw_mul(float2 *__restrict__ z, const float *__restrict__ w, int64_t n,
+                         int64_t total) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float s = w[i % n];
+    const float2 v = z[i];
+    z[i] = make_float2(v.x * s, v.y * s);
+  }
+}
+
+__global__ void k_sw_mul_d(double2 *__restrict__ z, const double *__restrict__ w, int64_t n,
+                           int64_t total) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double s = w[i % n];
+    const double2 v = z[i];
+    z[i] = make_double2(v.x * s, v.y * s);
+  }
+}
+
+// q_l = W_l v_l and the partials of v_l . q_l
+__global__ void __launch_bounds__(RED_THREADS)
+    k_sw_assemble(const double *__restrict__ v, const float *__restrict__ S, int M, int L,
+                  const float *__restrict__ conv_out, double conv_scale,
+                  const double *__restrict__ reg_out, const double *__restrict__ lam,
+                  double *__restrict__ q, double *__restrict__ partial) {
+  const int l = blockIdx.y;
+  const int64_t n = (int64_t)M * M * M, nL = (int64_t)L * L * L;
+  const int h = M / 2;
+  const double reg_scale = 1.0 / ((double)M * M * M);
+  const double rl = lam[2 * l], fl = lam[2 * l + 1];
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * RED_THREADS) {
+    const int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
+    const double sv = S[i];
+    const double cv = (double)conv_out[l * nL + ((int64_t)a * L + b) * L + c];
+    const int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
+    const double rv = reg_out[l * n + ((int64_t)ja * M + jb) * M + jc];
+    const double xv = v[l * n + i];
+    const double qv = sv * cv * conv_scale + rl * xv + fl * sv * rv * reg_scale;
+    q[l * n + i] = qv;
+    s = fma(xv, qv, s);
+  }
+  s = block_sum(s);
+  if (threadIdx.x == 0) partial[l * RED_BLOCKS + blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(RED_THREADS)
+    k_sw_dot(const double *__restrict__ a, const double *__restrict__ b, int64_t n,
+             double *__restrict__ partial) {
+  const int l = blockIdx.y;
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * RED_THREADS)
+    s = fma(a[l * n + i], b[l * n + i], s);
+  s = block_sum(s);
+  if (threadIdx.x == 0) partial[l * RED_BLOCKS + blockIdx.x] = s;
+}
+
+// out_l = a_l - b_l
+__global__ void k_sw_sub(const double *__restrict__ a, const double *__restrict__ b,
+                         double *__restrict__ out, int64_t n) {
+  const int l = blockIdx.y;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[l * n + i] = a[l * n + i] - b[l * n + i];
+}
+
+// one block per system: the scalar stages of the single-system CG
+__global__ void k_sw_init(const double *partial, double rtol, double *scal, int *flags) {
+  const int l = blockIdx.x;
+  const double bb = sum_partials(partial + l * RED_BLOCKS);
+  if (threadIdx.x == 0) {
+    const double bn = sqrt(bb);
+    double *sc = scal + l * S_COUNT;
+    sc[S_BNORM] = bn;
+    sc[S_ATOL] = rtol * bn;
+    sc[S_RHO_PREV] = 1.0;
+    flags[2 * l] = bn == 0.0 ? 1 : 0;
+    flags[2 * l + 1] = 0;
+  }
+}
+
+__global__ void k_sw_stage1(const double *partial, int it, double *scal, int *flags,
+                            double *hist, int maxiter) {
+  const int l = blockIdx.x;
+  const double rho = sum_partials(partial + l * RED_BLOCKS);
+  if (threadIdx.x == 0) {
+    double *sc = scal + l * S_COUNT;
+    if (hist) hist[(int64_t)l * maxiter + it] = sqrt(rho);
+    if (!flags[2 * l]) {
+      if (sqrt(rho) < sc[S_ATOL]) {
+        flags[2 * l] = 1;
+      } else {
+        sc[S_RHO] = rho;
+        sc[S_BETA] = it > 0 ? rho / sc[S_RHO_PREV] : 0.0;
+      }
+    }
+  }
+}
+
+__global__ void k_sw_stage2(const double *partial, double *scal, const int *flags) {
+  const int l = blockIdx.x;
+  const double pq = sum_partials(partial + l * RED_BLOCKS);
+  if (threadIdx.x == 0 && !flags[2 * l]) {
+    double *sc = scal + l * S_COUNT;
+    sc[S_PQ] = pq;
+    sc[S_ALPHA] = sc[S_RHO] / pq;
+    sc[S_RHO_PREV] = sc[S_RHO];
+  }
+}
+
+__global__ void k_sw_update_xr(double *__restrict__ x, double *__restrict__ r,
+                               const double *__restrict__ p, const double *__restrict__ q,
+                               const double *__restrict__ scal, int *__restrict__ flags,
+                               int64_t n) {
+  const int l = blockIdx.y;
+  if (flags[2 * l]) return;
+  const double alpha = scal[l * S_COUNT + S_ALPHA];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    x[l * n + i] = fma(alpha, p[l * n + i], x[l * n + i]);
+    r[l * n + i] = fma(-alpha, q[l * n + i], r[l * n + i]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) flags[2 * l + 1] += 1;
+}
+
+// norms[2l] = sqrt(partials of slot 0), norms[2l+1] = sqrt(slot 1)
+__global__ void k_sw_norm(const double *partial, double *norms, int slot) {
+  const int l = blockIdx.x;
+  const double v = sum_partials(partial + l * RED_BLOCKS);
+  if (threadIdx.x == 0) norms[2 * l + slot] = sqrt(v);
+}
+
+__global__ void k_sw_iters(const int *flags, int *iters, int nl) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l < nl) iters[l] = flags[2 * l + 1];
+}
+
+// W v for all systems (v already loaded into conv_in / reg_in): q = W v, and
+// the partials of v . q
+static int sweep_operator(spf_merge_s *G, Sweep *w, const double *v, cudaStream_t s) {
+  const int nl = w->nl;
+  cufftSetStream(w->r2c, s);
+  cufftSetStream(w->c2r, s);
+  cufftSetStream(w->d2z, s);
+  cufftSetStream(w->z2d, s);
+  SPF_TRY(cufft_ok(cufftExecR2C(w->r2c, w->conv_in, reinterpret_cast<cufftComplex *>(w->conv_freq)),
+                   "sweep conv R2C"));
+  k_sw_mul<<<grid1(nl * G->nLh), 256, 0, s>>>(w->conv_freq, G->kernel_hat, G->nLh, nl * G->nLh);
+  SPF_TRY(check_launch("k_sw_mul"));
+  SPF_TRY(cufft_ok(cufftExecC2R(w->c2r, reinterpret_cast<cufftComplex *>(w->conv_freq), w->conv_out),
+                   "sweep conv C2R"));
+  SPF_TRY(cufft_ok(cufftExecD2Z(w->d2z, w->reg_in, reinterpret_cast<cufftDoubleComplex *>(w->reg_freq)),
+                   "sweep reg D2Z"));
+  k_sw_mul_d<<<grid1(nl * G->nMh), 256, 0, s>>>(w->reg_freq, G->mask_hat, G->nMh, nl * G->nMh);
+  SPF_TRY(check_launch("k_sw_mul_d"));
+  SPF_TRY(cufft_ok(cufftExecZ2D(w->z2d, reinterpret_cast<cufftDoubleComplex *>(w->reg_freq), w->reg_out),
+                   "sweep reg Z2D"));
+  k_sw_assemble<<<dim3(RED_BLOCKS, nl), RED_THREADS, 0, s>>>(
+      v, G->support, G->M, G->L, w->conv_out, G->conv_scale, w->reg_out, w->lam, w->q, w->partial);
+  return check_launch("k_sw_assemble");
+}
+
+}  // namespace cg
+}  // namespace spf
+
+extern "C" int spf_merge_cg_sweep(spf_merge_s *G, int n_lambda, const double *h_rlambda,
+                                  const double *h_flambda, const double *d_adb,
+                                  const double *d_x0, double *d_x, int maxiter, double rtol,
+                                  double *d_norms, double *d_hist, int *d_iters, void *stream) {
+  using namespace spf::cg;
+  SPF_REQUIRE(G && h_rlambda && h_flambda && d_adb && d_x, "spf_merge_cg_sweep: NULL pointer");
+  SPF_REQUIRE(n_lambda >= 1 && n_lambda <= 64, "spf_merge_cg_sweep: n_lambda in 1..64");
+  SPF_REQUIRE(maxiter >= 0, "spf_merge_cg_sweep: maxiter < 0");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  SPF_REQUIRE(dev == G->dev, "spf_merge_cg_sweep: wrong device");
+  SPF_TRY(make_sweep(G, n_lambda));
+  Sweep *w = G->sweep;
+  cudaStream_t s = spf::as_stream(stream);
+  const int nl = n_lambda;
+  const int64_t n = G->n;
+  std::vector<double> lam(2 * nl);
+  for (int l = 0; l < nl; ++l) {
+    lam[2 * l] = h_rlambda[l];
+    lam[2 * l + 1] = h_flambda[l];
+  }
+  SPF_TRY(check_cuda(cudaMemcpyAsync(w->lam, lam.data(), 2 * nl * sizeof(double),
+                                     cudaMemcpyHostToDevice, s), "spf_merge_cg_sweep"));
+  // the host copy must stay valid until the copy ran
+  SPF_TRY(check_cuda(cudaStreamSynchronize(s), "spf_merge_cg_sweep"));
+  const dim3 gb(grid1(n), nl);
+  k_sw_rhs<<<gb, 256, 0, s>>>(d_adb, d_x0, w->lam, w->d, d_x, n);
+  SPF_TRY(check_launch("k_sw_rhs"));
+  // r = d - W x0
+  if (d_x0) {
+    k_sw_load<<<gb, 256, 0, s>>>(d_x, nullptr, nullptr, nullptr, G->support, G->M, G->L,
+                                 w->conv_in, w->reg_in);
+    SPF_TRY(check_launch("k_sw_load"));
+    SPF_TRY(sweep_operator(G, w, d_x, s));
+    k_sw_sub<<<gb, 256, 0, s>>>(w->d, w->q, w->r, n);
+  } else {
+    SPF_TRY(check_cuda(cudaMemcpyAsync(w->r, w->d, nl * n * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, s), "spf_merge_cg_sweep"));
+  }
+  SPF_TRY(check_launch("k_sw_sub"));
+  k_sw_dot<<<dim3(RED_BLOCKS, nl), RED_THREADS, 0, s>>>(w->d, w->d, n, w->partial);
+  SPF_TRY(check_launch("k_sw_dot"));
+  k_sw_init<<<nl, RED_THREADS, 0, s>>>(w->partial, rtol, w->scal, w->flags);
+  SPF_TRY(check_launch("k_sw_init"));
+  SPF_TRY(check_cuda(cudaMemsetAsync(w->p, 0, nl * n * sizeof(double), s), "spf_merge_cg_sweep"));
+  for (int it = 0; it < maxiter; ++it) {
+    k_sw_dot<<<dim3(RED_BLOCKS, nl), RED_THREADS, 0, s>>>(w->r, w->r, n, w->partial);
+    SPF_TRY(check_launch("k_sw_dot"));
+    k_sw_stage1<<<nl, RED_THREADS, 0, s>>>(w->partial, it, w->scal, w->flags, d_hist, maxiter);
+    SPF_TRY(check_launch("k_sw_stage1"));
+    k_sw_load<<<gb, 256, 0, s>>>(w->p, w->r, w->scal, w->flags, G->support, G->M, G->L,
+                                 w->conv_in, w->reg_in);
+    SPF_TRY(check_launch("k_sw_load"));
+    SPF_TRY(sweep_operator(G, w, w->p, s));
+    k_sw_stage2<<<nl, RED_THREADS, 0, s>>>(w->partial, w->scal, w->flags);
+    SPF_TRY(check_launch("k_sw_stage2"));
+    k_sw_update_xr<<<gb, 256, 0, s>>>(d_x, w->r, w->p, w->q, w->scal, w->flags, n);
+    SPF_TRY(check_launch("k_sw_update_xr"));
+  }
+  if (d_iters) {
+    k_sw_iters<<<(nl + 63) / 64, 64, 0, s>>>(w->flags, d_iters, nl);
+    SPF_TRY(check_launch("k_sw_iters"));
+  }
+  if (d_norms) {  // ||x_l|| and ||W_l x_l - d_l|| (the reference's v1, v2)
+    k_sw_dot<<<dim3(RED_BLOCKS, nl), RED_THREADS, 0, s>>>(d_x, d_x, n, w->partial);
+    SPF_TRY(check_launch("k_sw_dot"));
+    k_sw_norm<<<nl, RED_THREADS, 0, s>>>(w->partial, d_norms, 0);
+    SPF_TRY(check_launch("k_sw_norm"));
+    k_sw_load<<<gb, 256, 0, s>>>(d_x, nullptr, nullptr, nullptr, G->support, G->M, G->L,
+                                 w->conv_in, w->reg_in);
+    SPF_TRY(check_launch("k_sw_load"));
+    SPF_TRY(sweep_operator(G, w, d_x, s));
+    k_sw_sub<<<gb, 256, 0, s>>>(w->q, w->d, w->r, n);
+    SPF_TRY(check_launch("k_sw_sub"));
+    k_sw_dot<<<dim3(RED_BLOCKS, nl), RED_THREADS, 0, s>>>(w->r, w->r, n, w->partial);
+    SPF_TRY(check_launch("k_sw_dot"));
+    k_sw_norm<<<nl, RED_THREADS, 0, s>>>(w->partial, d_norms, 1);
+    SPF_TRY(check_launch("k_sw_norm"));
+  }
+  return SPF_OK;
+}

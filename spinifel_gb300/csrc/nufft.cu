@@ -309,6 +309,84 @@ __global__ void k_slice_t2(const float *__restrict__ re_pad, GridGeom g,
   if (out_bf16) out_bf16[idx] = __float2bfloat16_rn(v);
 }
 
+// Shared-memory boxes of the padded grid: a box of di x dj x dk cells at
+// (imin, jmin, kmin), stored with plane stride sp and row stride sr floats.  Rows are
+// walked by half-warps (dk <= 16) or warps with the lanes along the fastest
+// axis, so the global side is coalesced and there is one division per row,
+// not per cell.
+struct BoxShape {
+  int imin, jmin, kmin, di, dj, dk;
+  int sp, sr;  // plane and row strides in floats: cell (ii, jj, kk) at ii*sp + jj*sr + kk
+};
+
+template <class F>
+__device__ __forceinline__ void box_rows(const BoxShape &b, F &&f) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const bool half = b.dk <= 16;
+  const int l = half ? (lane & 15) : lane;
+  const int step = half ? 16 : 32;
+  const int rpw = half ? 2 : 1;
+  const int rows = b.di * b.dj;
+  for (int r = warp * rpw + (half ? (lane >> 4) : 0); r < rows; r += nw * rpw) {
+    const int ii = r / b.dj, jj = r - ii * b.dj;
+    for (int kk = l; kk < b.dk; kk += step) f(ii, jj, kk, ii * b.sp + jj * b.sr + kk);
+  }
+}
+
+__device__ __forceinline__ size_t box_global(const GridGeom &g, const BoxShape &b, int ii, int jj,
+                                             int kk) {
+  return ((size_t)(b.imin + ii) * g.p2 + (b.jmin + jj)) * g.p3 + b.kmin + kk;
+}
+
+// Box fill: thread t loads cells t, t + blockDim.x, ... (coalesced along the
+// fastest axis), four loads in flight before their stores; the cell index
+// advances by a mixed-radix step instead of a division per cell.
+__device__ __forceinline__ void box_load(float *box, const float *__restrict__ grid,
+                                         const GridGeom &g, const BoxShape &b) {
+  constexpr int U = 4;
+  const int vol = b.di * b.dj * b.dk;
+  const int nt = blockDim.x;
+  int idx = threadIdx.x;
+  int kk = idx % b.dk, jj = (idx / b.dk) % b.dj, ii = idx / (b.dk * b.dj);
+  const int stk = nt % b.dk, stj = (nt / b.dk) % b.dj, sti = nt / (b.dk * b.dj);
+  while (idx < vol) {
+    float v[U];
+    int dst[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      dst[u] = -1;
+      v[u] = 0.0f;
+      if (idx < vol) {
+        dst[u] = ii * b.sp + jj * b.sr + kk;
+        v[u] = __ldg(grid + box_global(g, b, ii, jj, kk));
+      }
+      idx += nt;
+      kk += stk;
+      jj += stj;
+      ii += sti;
+      if (kk >= b.dk) {
+        kk -= b.dk;
+        ++jj;
+      }
+      if (jj >= b.dj) {
+        jj -= b.dj;
+        ++ii;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (dst[u] >= 0) box[dst[u]] = v[u];
+  }
+}
+
+__device__ __forceinline__ void box_flush(const float *box, float *__restrict__ grid,
+                                          const GridGeom &g, const BoxShape &b) {
+  box_rows(b, [&](int ii, int jj, int kk, int s) {
+    const float v = box[s];
+    if (v != 0.0f) atomicAdd(grid + box_global(g, b, ii, jj, kk), v);
+  });
+}
+
 // Slicing on a multi-panel detector [n_panels][nx][ny]: a CTA of 256 threads
 // takes a 16 x 16 pixel patch of one panel at one orientation, so its points
 // are neighbours on the Ewald sphere.  It finds the bounding box of their
@@ -369,17 +447,10 @@ __global__ void __launch_bounds__(256)
   const int di = bb[3] - imin + W, dj = bb[4] - jmin + W, dk = bb[5] - kmin + W;
   // odd row strides spread neighbouring points' rows over the banks
   const int sj = dj | 1, sk = dk | 1;
-  const int64_t vol = (int64_t)di * dj * dk;
   const int64_t svol = (int64_t)di * sj * sk;
   float acc = 0.0f;
   if (bb[3] >= imin && svol <= SLICE_SMEM_FLOATS) {
-    for (int idx = threadIdx.x; idx < (int)vol; idx += blockDim.x) {
-      int kk = idx % dk;
-      int jj = (idx / dk) % dj;
-      int ii = idx / (dk * dj);
-      box[(ii * sj + jj) * sk + kk] =
-          __ldg(re_pad + ((size_t)(imin + ii) * g.p2 + (jmin + jj)) * g.p3 + kmin + kk);
-    }
+    box_load(box, re_pad, g, BoxShape{imin, jmin, kmin, di, dj, dk, sj * sk, sk});
     __syncthreads();
     // only valid points' footprints are inside the box
     if (!valid) return;
@@ -500,14 +571,12 @@ __global__ void __launch_bounds__(256)
   const int di = bb[3] - imin + W, dj = bb[4] - jmin + W, dk = bb[5] - kmin + W;
   const int64_t vol = (int64_t)di * dj * dk;
   const bool staged = vol <= SPREAD_SMEM_FLOATS;
+  const BoxShape shape{imin, jmin, kmin, di, dj, dk, dj * dk, dk};
   float v = 0.0f;
   if constexpr (INTERP) {
     // interpolate from the type-2 grid first (staged through the same box)
     if (staged) {
-      for (int idx = threadIdx.x; idx < (int)vol; idx += blockDim.x) {
-        int kk = idx % dk, jj = (idx / dk) % dj, ii = idx / (dk * dj);
-        box[idx] = __ldg(re_pad + ((size_t)(imin + ii) * g.p2 + (jmin + jj)) * g.p3 + kmin + kk);
-      }
+      box_load(box, re_pad, g, shape);
       __syncthreads();
     }
     const int li = pt.i0 - imin, lj = pt.j0 - jmin, lk = pt.k0 - kmin;
@@ -551,13 +620,7 @@ __global__ void __launch_bounds__(256)
       }
     }
     __syncthreads();
-    for (int idx = threadIdx.x; idx < (int)vol; idx += blockDim.x) {
-      float bv = box[idx];
-      if (bv != 0.0f) {
-        int kk = idx % dk, jj = (idx / dk) % dj, ii = idx / (dk * dj);
-        atomicAdd(acc_pad + ((size_t)(imin + ii) * g.p2 + (jmin + jj)) * g.p3 + kmin + kk, bv);
-      }
-    }
+    box_flush(box, acc_pad, g, shape);
   } else if (v != 0.0f) {
 #pragma unroll
     for (int a = 0; a < W; ++a) {
@@ -722,14 +785,25 @@ __global__ void k_bin_scatter(const int32_t *__restrict__ bin_of, int64_t n,
   }
 }
 
-// One work item (a bin, or a chunk of a big bin): stage the bin's box of the
-// type-2 grid, interpolate every point, weight it, spread it into a shared
-// box, and add the box to the type-1 accumulator.  Eight lanes serve one
-// point (four points per warp): lane c owns offset c along the fastest axis,
-// evaluates the c-th kernel weight of each axis and shares them by
-// shuffles; the interpolation is a sum over (a, b) per lane followed by an
-// 8-lane shuffle reduction, and each spreading instruction writes 8
-// consecutive cells of one row per point, so lanes rarely collide on a cell.
+// Fused type 2 -> weight -> type 1 over bin-sorted points.  A CTA takes one
+// work item (up to 2,048 points of one 8^3-cell bin), stages the bin's
+// footprint box of the type-2 grid in shared memory, and accumulates the
+// spread into a second box that is added to the type-1 accumulator at the
+// end.  A warp serves one point at a time: its 32 lanes are 4 footprint rows
+// x 8 cells along the fastest axis, so one instruction reads or updates 4
+// rows of one point.  The row stride (24 floats) and the plane stride
+// (== W * 24 mod 32) put 4 consecutive footprint rows on 4 disjoint groups of
+// 8 banks, so those accesses have no bank conflicts and no two lanes touch
+// the same cell.  Each point's coordinates are computed once by one lane and
+// broadcast; lanes 0-7 / 8-15 / 16-23 evaluate the kernel on axes 1 / 2 / 3.
+constexpr int SORTED_ROW_STRIDE = 24;
+
+constexpr int sorted_plane_stride(int d, int w) {
+  int x = d * SORTED_ROW_STRIDE;
+  while (x % 32 != (w * SORTED_ROW_STRIDE) % 32) ++x;
+  return x;
+}
+
 template <int W>
 __global__ void __launch_bounds__(256)
     k_interp_spread_sorted(const float *__restrict__ re_pad, float *__restrict__ acc_pad,
@@ -738,93 +812,100 @@ __global__ void __launch_bounds__(256)
                            const float *__restrict__ ppr, int64_t n_pix, float s1, float s2,
                            float s3, const float *__restrict__ weights,
                            unsigned int *__restrict__ err) {
-  static_assert(W <= 8, "eight lanes per point");
+  static_assert(W <= 8, "eight lanes per footprint row");
   constexpr int D = BIN + W - 1;
-  constexpr int S = D | 1;  // odd row stride
-  __shared__ float tbox[D * S * S];
-  __shared__ float abox[D * S * S];
+  constexpr int SR = SORTED_ROW_STRIDE;
+  constexpr int SP = sorted_plane_stride(D, W);
+  constexpr int ROWS = W * W;
+  constexpr int STEPS = (ROWS + 3) / 4;
+  static_assert(D <= SR, "row stride holds a footprint row");
+  __shared__ float tbox[D * SP];
+  __shared__ float abox[D * SP];
   const int4 it = items[blockIdx.x];
   const int b = it.x;
   const int bi = b / (bd.nb[1] * bd.nb[2]), bj = (b / bd.nb[2]) % bd.nb[1], bk = b % bd.nb[2];
   const int i0b = bi * BIN, j0b = bj * BIN, k0b = bk * BIN;
   const int di = min(D, g.p1 - i0b), dj = min(D, g.p2 - j0b), dk = min(D, g.p3 - k0b);
-  const int vol = di * dj * dk;
-  for (int idx = threadIdx.x; idx < vol; idx += blockDim.x) {
-    int kk = idx % dk, jj = (idx / dk) % dj, ii = idx / (dk * dj);
-    int sidx = (ii * S + jj) * S + kk;
-    tbox[sidx] = __ldg(re_pad + ((size_t)(i0b + ii) * g.p2 + (j0b + jj)) * g.p3 + k0b + kk);
-    abox[sidx] = 0.0f;
-  }
+  const BoxShape shape{i0b, j0b, k0b, di, dj, dk, SP, SR};
+  box_load(tbox, re_pad, g, shape);
+  box_rows(shape, [&](int, int, int, int s) { abox[s] = 0.0f; });
   __syncthreads();
+  const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const int grp = lane >> 3;   // point slot in the warp
-  const int c = lane & 7;      // offset along the fastest axis
+  const int grp = lane >> 3;  // footprint row within a step; kernel axis for the weights
+  const int c = lane & 7;     // offset along the fastest axis
   const int warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
   const float fn1 = (float)g.n1, fn2 = (float)g.n2, fn3 = (float)g.n3;
-  for (int base = warp * 4; base < it.z; base += nwarps * 4) {
-    const int q = base + grp;
-    const bool live = q < it.z;
-    const int32_t pi = live ? sorted[it.y + q] : sorted[it.y];
-    const int64_t o = pi / n_pix, p = pi % n_pix;
-    float h, k, l;
-    rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
-    // per-axis first index (same arithmetic as axis_setup) and this lane's weight
-    float t1 = __fmul_rn(h, s1), t2 = __fmul_rn(k, s2), t3 = __fmul_rn(l, s3);
-    t1 = __fsub_rn(t1, __fmul_rn(fn1, floorf(__fadd_rn(__fdiv_rn(t1, fn1), 0.5f))));
-    t2 = __fsub_rn(t2, __fmul_rn(fn2, floorf(__fadd_rn(__fdiv_rn(t2, fn2), 0.5f))));
-    t3 = __fsub_rn(t3, __fmul_rn(fn3, floorf(__fadd_rn(__fdiv_rn(t3, fn3), 0.5f))));
-    const float l1 = ceilf(__fsub_rn(t1, 0.5f * W)), l2 = ceilf(__fsub_rn(t2, 0.5f * W)),
-                l3 = ceilf(__fsub_rn(t3, 0.5f * W));
-    const float cf = (float)c;
-    float my1 = c < W ? es_eval((l1 + cf - t1) * g.inv_half_w, g.beta) : 0.0f;
-    float my2 = c < W ? es_eval((l2 + cf - t2) * g.inv_half_w, g.beta) : 0.0f;
-    float my3 = c < W ? es_eval((l3 + cf - t3) * g.inv_half_w, g.beta) : 0.0f;
-    float w1[W], w2[W];
-#pragma unroll
-    for (int a = 0; a < W; ++a) {
-      w1[a] = __shfl_sync(0xffffffffu, my1, a, 8);
-      w2[a] = __shfl_sync(0xffffffffu, my2, a, 8);
+  for (int q0 = warp * 32; q0 < it.z; q0 += nwarps * 32) {
+    const int cnt = min(32, it.z - q0);
+    // lane L prepares point q0 + L (same arithmetic as axis_setup / the bin sort)
+    int32_t my_pi = 0;
+    float t1 = 0.f, t2 = 0.f, t3 = 0.f, l1 = 0.f, l2 = 0.f, l3 = 0.f;
+    if (lane < cnt) {
+      my_pi = sorted[it.y + q0 + lane];
+      const int64_t o = my_pi / n_pix, p = my_pi % n_pix;
+      float h, k, l;
+      rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
+      t1 = __fmul_rn(h, s1);
+      t2 = __fmul_rn(k, s2);
+      t3 = __fmul_rn(l, s3);
+      t1 = __fsub_rn(t1, __fmul_rn(fn1, floorf(__fadd_rn(__fdiv_rn(t1, fn1), 0.5f))));
+      t2 = __fsub_rn(t2, __fmul_rn(fn2, floorf(__fadd_rn(__fdiv_rn(t2, fn2), 0.5f))));
+      t3 = __fsub_rn(t3, __fmul_rn(fn3, floorf(__fadd_rn(__fdiv_rn(t3, fn3), 0.5f))));
+      l1 = ceilf(__fsub_rn(t1, 0.5f * W));
+      l2 = ceilf(__fsub_rn(t2, 0.5f * W));
+      l3 = ceilf(__fsub_rn(t3, 0.5f * W));
     }
-    const int li = (int)l1 + g.off1 - i0b, lj = (int)l2 + g.off2 - j0b, lk = (int)l3 + g.off3 - k0b;
-    bool inside = li >= 0 && lj >= 0 && lk >= 0 && li + W <= di && lj + W <= dj && lk + W <= dk;
-    if (live && !inside && c == 0 && err) atomicExch(err, (unsigned int)(-SPF_ERR_CUDA));
-    const bool act = live && inside && c < W;
-    // interpolate: lane c sums over (a, b), then the 8 lanes are reduced
-    float part = 0.0f;
-    if (act) {
-#pragma unroll
-      for (int a = 0; a < W; ++a) {
-        float pa = 0.0f;
-#pragma unroll
-        for (int bb = 0; bb < W; ++bb)
-          pa = fmaf(w2[bb], tbox[((li + a) * S + (lj + bb)) * S + lk + c], pa);
-        part = fmaf(w1[a], pa, part);
+    for (int j = 0; j < cnt; ++j) {
+      const int32_t pi = __shfl_sync(FULL, my_pi, j);
+      const float T1 = __shfl_sync(FULL, t1, j), T2 = __shfl_sync(FULL, t2, j),
+                  T3 = __shfl_sync(FULL, t3, j);
+      const float L1 = __shfl_sync(FULL, l1, j), L2 = __shfl_sync(FULL, l2, j),
+                  L3 = __shfl_sync(FULL, l3, j);
+      const int li = (int)L1 + g.off1 - i0b, lj = (int)L2 + g.off2 - j0b,
+                lk = (int)L3 + g.off3 - k0b;
+      const bool inside =
+          li >= 0 && lj >= 0 && lk >= 0 && li + W <= di && lj + W <= dj && lk + W <= dk;
+      if (!inside) {  // cannot happen for a correctly binned point; never read outside
+        if (lane == 0 && err) atomicExch(err, (unsigned int)(-SPF_ERR_CUDA));
+        continue;
       }
-      part *= my3;
-    }
-    part += __shfl_xor_sync(0xffffffffu, part, 4, 8);
-    part += __shfl_xor_sync(0xffffffffu, part, 2, 8);
-    part += __shfl_xor_sync(0xffffffffu, part, 1, 8);
-    float v = part;
-    if (weights && live) v *= weights[pi];
-    if (act && v != 0.0f) {
-      const float wv = my3 * v;
+      const float tt = grp == 0 ? T1 : (grp == 1 ? T2 : T3);
+      const float ll = grp == 0 ? L1 : (grp == 1 ? L2 : L3);
+      const float kw = (c < W && grp < 3) ? es_eval((ll + (float)c - tt) * g.inv_half_w, g.beta)
+                                          : 0.0f;
+      const float w3c = __shfl_sync(FULL, kw, 16 + c);  // 0 for c >= W
+      // interpolate: step t covers footprint rows 4t .. 4t+3 (row r = a*W + b)
+      float w12[STEPS];
+      float part = 0.0f;
 #pragma unroll
-      for (int a = 0; a < W; ++a) {
+      for (int t = 0; t < STEPS; ++t) {
+        const int r = 4 * t + grp;
+        const int a = r / W, bb = r - a * W;
+        w12[t] = __shfl_sync(FULL, kw, a & 7) * __shfl_sync(FULL, kw, 8 + bb);
+        if (r < ROWS && c < W)
+          part = fmaf(w12[t], tbox[(li + a) * SP + (lj + bb) * SR + lk + c], part);
+      }
+      part *= w3c;
 #pragma unroll
-        for (int bb = 0; bb < W; ++bb)
-          atomicAdd(&abox[((li + a) * S + (lj + bb)) * S + lk + c], w1[a] * w2[bb] * wv);
+      for (int m = 16; m >= 1; m >>= 1) part += __shfl_xor_sync(FULL, part, m);
+      float v = part;
+      if (weights) v *= weights[pi];
+      if (v != 0.0f) {
+        const float wv = w3c * v;
+#pragma unroll
+        for (int t = 0; t < STEPS; ++t) {
+          const int r = 4 * t + grp;
+          const int a = r / W, bb = r - a * W;
+          if (r < ROWS && c < W) atomicAdd(&abox[(li + a) * SP + (lj + bb) * SR + lk + c],
+                                           w12[t] * wv);
+        }
       }
     }
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < vol; idx += blockDim.x) {
-    int kk = idx % dk, jj = (idx / dk) % dj, ii = idx / (dk * dj);
-    float bv = abox[(ii * S + jj) * S + kk];
-    if (bv != 0.0f)
-      atomicAdd(acc_pad + ((size_t)(i0b + ii) * g.p2 + (j0b + jj)) * g.p3 + k0b + kk, bv);
-  }
+  box_flush(abox, acc_pad, g, shape);
 }
 
 // fine[l] = sum of acc_pad[i] over padded i == l + off (mod n)  (Im = 0).

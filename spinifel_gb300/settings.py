@@ -2,7 +2,7 @@
 
 The reference reads a TOML file through the SpinifelSettings singleton
 (spinifel/settings.py:167-848).  Only the fields the slicing / matching /
-merge path reads are mirrored here, as a plain dataclass with the same names
+merge / phasing path reads are mirrored here, as a plain dataclass with the same names
 and derived values:
   Mquat = 20 * oversampling, M = 4 Mquat + 1, M_ups = 2 M
 (spinifel/settings.py:805-826) and
@@ -30,11 +30,18 @@ class Settings:
     verbose: bool = False
     M_override: int | None = None
     M_ups_override: int | None = None
+    Mquat_override: int | None = None
+    # phase retrieval (spinifel/settings.py:388-412)
+    beta: float = 0.9
+    cutoff: float = 5e-2
+    nER: int = 10
+    nHIO: int = 5
+    N_phase_loops: int = 5
     reduced_det_shape_override: tuple | None = field(default=None)
 
     @property
     def Mquat(self) -> int:
-        return int(self.oversampling * 20)
+        return self.Mquat_override if self.Mquat_override else int(self.oversampling * 20)
 
     @property
     def M(self) -> int:

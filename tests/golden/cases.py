@@ -12,6 +12,7 @@ SNM = dict(seed=7003, M=21, det_shape=(4, 16, 16), n_orient=300, batch=100, n_im
            photons=2.0)
 OPS = dict(seed=7004, M=15, npts=2000)
 MERGE = dict(seed=7005, M=15, det_shape=(4, 8, 8), n_images=40, maxiter=20, photons=2.0)
+PHASE = dict(seed=7006, Mquat=5, nER=4, nHIO=3, N_phase_loops=2, beta=0.9)
 
 
 def nn_inputs():
@@ -72,3 +73,23 @@ def merge_inputs():
     data = _images(model, orient, ppr, pdr, MERGE["photons"], rng)
     ac_est = model.copy()
     return data, ppr, pdr, orient, ac_est
+
+
+def phase_inputs():
+    """A centred autocorrelation of a compact density of 6 Gaussian blobs on
+    the M^3 grid (M = 4 Mquat + 1) and a uniform random starting density."""
+    c = PHASE
+    M = 4 * c["Mquat"] + 1
+    rng = np.random.default_rng(c["seed"])
+    ax = np.arange(M) - M // 2
+    X, Y, Z = np.meshgrid(ax, ax, ax, indexing="ij")
+    rho = np.zeros((M, M, M))
+    for _ in range(6):
+        cen = rng.uniform(-M / 8, M / 8, 3)
+        sig = rng.uniform(0.8, 1.6)
+        rho += rng.uniform(0.5, 1.0) * np.exp(
+            -((X - cen[0]) ** 2 + (Y - cen[1]) ** 2 + (Z - cen[2]) ** 2) / (2 * sig ** 2))
+    F = np.fft.fftn(np.fft.ifftshift(rho))
+    ac = np.fft.fftshift(np.fft.ifftn(np.abs(F) ** 2).real)
+    rho0 = rng.random((M, M, M))
+    return ac, rho0

@@ -17,6 +17,8 @@ oracle/nufft.py for the un-vendored finufft) and then calls, unmodified:
   * spinifel.sequential.autocorrelation.Merge.solve_ac (scipy cg)
                                                      -> golden_merge.npz
   * spinifel.autocorrelation.forward / adjoint glue  -> golden_ops.npz
+  * spinifel.sequential.phasing.phase (numpy branch) -> golden_phase.npz
+    (numpy 2 dropped numpy.infty, which phase() reads; it is set to inf)
 
 Inputs are regenerated from the stored seeds by tests (numpy PCG64 streams are
 stable), so only small outputs are committed.  Run in the build container:
@@ -110,6 +112,7 @@ def _settings_file(c: dict) -> str:
     text = f"""
 [debug]
 verbose = false
+show_image = false
 use_callmonitor = false
 [runtime]
 N_images_per_rank = {c.get("n_images", 10)}
@@ -124,7 +127,7 @@ N_orientations = {c["n_orient"]}
 N_batch_size = {c["batch"]}
 oversampling = 1
 solve_ac_maxiter = {c.get("maxiter", 100)}
-[detector]
+{c.get("extra", "")}[detector]
 shape = {det}
 """
     fd, path = tempfile.mkstemp(suffix=".toml")
@@ -244,6 +247,26 @@ def main():
     np.savez_compressed(os.path.join(HERE, "golden_merge.npz"), ac=ac_out,
                         iterations=np.array(merge.callback.counter))
     print("merge", ac_out.ravel()[:4], merge.callback.counter)
+
+
+    # --- phasing.phase -----------------------------------------------------------
+    p = cases.PHASE
+    sys.argv = ["spinifel", "--mode=sequential", "--settings=" + _settings_file(
+        {"det_shape": (1, 1, 1), "n_orient": 10, "batch": 10,
+         "extra": f"nER = {p['nER']}\nnHIO = {p['nHIO']}\nN_phase_loops = "
+                  f"{p['N_phase_loops']}\nbeta = {p['beta']}\n"})]
+    st._SpinifelSettings__toml = sys.argv[2].split("=", 1)[1]
+    st.refresh()
+    type(st).Mquat = property(lambda self: p["Mquat"])
+    if not hasattr(np, "infty"):
+        np.infty = np.inf
+    import spinifel.sequential.phasing as rph
+
+    ac, rho0 = cases.phase_inputs()
+    ac_phased, support_, rho_ = rph.phase(0, ac.copy(), None, rho0.copy())
+    np.savez_compressed(os.path.join(HERE, "golden_phase.npz"), ac_phased=ac_phased,
+                        support_=np.asarray(support_, dtype=np.uint8), rho_=rho_)
+    print("phase", ac_phased.ravel()[:3], int(np.asarray(support_).sum()))
 
 
 if __name__ == "__main__":

@@ -75,6 +75,42 @@ def test_type1_spread_matches_direct_sum(dev, m, isign):
     assert rel(got, exact) < TOL
 
 
+def test_one_call_type1_and_fft_deconv_stage(dev):
+    """spf_spread_t1 (zero + spread + finish in one call) against the direct
+    sum, and spf_fft_deconv's two directions against the calls they stand for."""
+    from spinifel_gb300 import _lib
+    from spinifel_gb300.nufft import NufftPlan
+
+    rng = np.random.default_rng(13)
+    m = (12, 11, 10)
+    x, y, z = rng.uniform(-3 * np.pi + 1e-3, 3 * np.pi - 1e-3, (3, 3000)).astype(np.float32)
+    c = rng.standard_normal(3000).astype(np.float32)
+    P = NufftPlan(m, 1e-6)
+    xt, yt, zt, ct = (t(v, dev) for v in (x, y, z, c))
+    re = torch.empty(m, dtype=torch.float32, device=dev)
+    im = torch.empty(m, dtype=torch.float32, device=dev)
+    sh = _lib.stream_handle()
+    _lib.call("spf_spread_t1", P.handle, _lib.ptr(xt), _lib.ptr(yt), _lib.ptr(zt), _lib.ptr(ct),
+              3000, 1, _lib.ptr(re), _lib.ptr(im), sh)
+    got = re.cpu().numpy() + 1j * im.cpu().numpy()
+    assert rel(got, onufft.nudft3d1(x, y, z, c, m, 1)) < TOL
+    # type 1 stage: spread, then spf_fft_deconv == spf_nufft_t1_finish
+    P.spread_zero()
+    P.spread(xt, yt, zt, ct)
+    re2 = torch.empty_like(re)
+    _lib.call("spf_fft_deconv", P.handle, 1, 1, None, None, _lib.ptr(re2), None, sh)
+    assert rel(re2.cpu().numpy(), re.cpu().numpy()) < 1e-6  # float atomics: order may differ
+    # type 2 stage: spf_fft_deconv then interpolation == set_modes then interpolation
+    f = t(rng.standard_normal(m), dev)
+    _lib.call("spf_fft_deconv", P.handle, 2, -1, _lib.ptr(f), None, None, None, sh)
+    a, _ = P.interp(xt, yt, zt)
+    P.set_modes(f, isign=-1)
+    b, _ = P.interp(xt, yt, zt)
+    assert torch.equal(a, b)
+    with pytest.raises(_lib.SpfError):
+        _lib.call("spf_fft_deconv", P.handle, 1, 1, _lib.ptr(f), None, _lib.ptr(re2), None, sh)
+
+
 def test_type1_is_adjoint_of_type2(dev):
     from spinifel_gb300.nufft import NufftPlan
 
