@@ -272,16 +272,19 @@ int spf_merge_cg(spf_merge merge, int form, const double *d_b, double *d_x, int 
                  int maxiter, double rtol, double *d_hist, int *d_iters, void *stream);
 /* Regularisation sweep (the MPI merge's per-rank lambdas,
  * spinifel/mpi/autocorrelation.py:64-68,160-214) as one batched solve: n_lambda
- * systems W_l x = conv(x) + rlambda_l x + flambda_l reg(x) = d_adb +
+ * systems W_l x = c conv(x) + rlambda_l x + flambda_l reg(x) = d_adb +
  * rlambda_l x0 (h_rlambda / h_flambda: n_lambda host doubles; the merge's own
  * rlambda / flambda are not used), each CG from x0 (d_x0 M^3 doubles, NULL =
- * 0) with scipy's stopping rule, all systems advanced by the same launches
+ * 0) with scipy's stopping rule, all systems advanced by the same launches;
+ * c = conv_factor (1: the sequential merge's conv; M^3: the MPI merge's,
+ * whose kernel transform lacks the 1/M^3, mpi/autocorrelation.py:95-104)
  * (batched cuFFT plans, allocated on the first call for a given n_lambda).
  * d_x: n_lambda x M^3 solutions; d_norms (may be NULL): 2 n_lambda doubles,
  * ||x_l|| and ||W_l x_l - d_l||; d_hist (may be NULL): n_lambda x maxiter
  * residual norms; d_iters (may be NULL): n_lambda ints.  Toeplitz form. */
-int spf_merge_cg_sweep(spf_merge merge, int n_lambda, const double *h_rlambda,
-                       const double *h_flambda, const double *d_adb, const double *d_x0,
+int spf_merge_cg_sweep(spf_merge merge, int n_lambda, double conv_factor,
+                       const double *h_rlambda, const double *h_flambda, const double *d_adb,
+                       const double *d_x0,
                        double *d_x, int maxiter, double rtol, double *d_norms, double *d_hist,
                        int *d_iters, void *stream);
 /* The same solve under the name of the reference's step: Merge.solve_ac's

@@ -91,3 +91,48 @@ class MergeOracle:
 
         x, info = cg(A, d, x0=x0.copy(), maxiter=maxiter or self.maxiter, rtol=rtol, callback=cb)
         return x.reshape((self.M,) * 3), info, F_conv, d
+
+
+def antisupport_mpi(M: int) -> np.ndarray:
+    """spinifel/mpi/autocorrelation.py:75-79: |q| rounded to 4 decimals > pi."""
+    lu = np.linspace(-np.pi, np.pi, M)
+    Hu, Ku, Lu = np.meshgrid(lu, lu, lu, indexing="ij")
+    return np.around(np.sqrt(Hu ** 2 + Ku ** 2 + Lu ** 2), 4) > np.pi
+
+
+def mpi_sweep(data, H_, K_, L_, ac_support, x0, M, size, maxiter, generation, eps=1e-12):
+    """The MPI merge (spinifel/mpi/autocorrelation.py:40-214) for ranks
+    0..size-1 in sequence: rank r solves with rlambda = M^3/N 2^(r - size/2),
+    flambda = 1e5 10^(r - size//2), the kernel transform without 1/M^3 and
+    the rounded antisupport; then rank 0's choice.  Returns (x of the chosen
+    rank, chosen rank, summary rows (rank, rlambda, ||x||, ||W x - d||))."""
+    N = np.asarray(data).size
+    mo = MergeOracle(M, 2 * M, N, 1, maxiter, eps)
+    mo.F_antisupport = antisupport_mpi(M)
+    F_conv = mo.kernel(H_, K_, L_) * M ** 3  # the MPI kernel is not divided by M^3
+    S = ac_support
+    adb = onufft.adjoint(np.asarray(data, dtype=np.float64).reshape(-1), H_, K_, L_, M, True, S,
+                         eps=eps).reshape(-1)
+    n = M ** 3
+    xs, rows = [], []
+    for r in range(size):
+        rl = M ** 3 / N * 2 ** (r - size / 2)
+        fl = 1e5 * pow(10, r - size // 2)
+
+        def W(u, rl=rl, fl=fl):
+            u = np.real(u)
+            return mo.conv(u, F_conv, S) + rl * u + fl * mo.reg(u, S)
+
+        d = adb + rl * x0
+        A = LinearOperator(dtype=np.float64, shape=(n, n), matvec=W)
+        x, info = cg(A, d, x0=x0.copy(), maxiter=maxiter, rtol=1e-5)
+        xs.append(x)
+        rows.append((r, rl, float(np.linalg.norm(x)), float(np.linalg.norm(W(x) - d))))
+    rows = np.array(rows)
+    v1s, v2s, lam = rows[:, 2], rows[:, 3], rows[:, 1]
+    if generation == 0:
+        idx = v1s >= np.mean(v1s)
+        iref = int(np.arange(size)[idx][np.argmax(lam[idx])])
+    else:
+        iref = int(np.argmin(v1s + v2s))
+    return xs[iref].reshape((M,) * 3), iref, rows

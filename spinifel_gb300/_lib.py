@@ -130,7 +130,7 @@ SIGNATURES = {
     "spf_serve_stats": [_c_void_p, ctypes.POINTER(_dbl), _int],
     "spf_serve_latencies": [_c_void_p, ctypes.POINTER(_dbl), _i64, ctypes.POINTER(_i64)],
     "spf_serve_destroy": [_c_void_p],
-    "spf_merge_cg_sweep": [_c_void_p, _int, ctypes.POINTER(_dbl), ctypes.POINTER(_dbl),
+    "spf_merge_cg_sweep": [_c_void_p, _int, _dbl, ctypes.POINTER(_dbl), ctypes.POINTER(_dbl),
                            _c_void_p, _c_void_p, _c_void_p, _int, _dbl, _c_void_p, _c_void_p,
                            _c_void_p, _c_void_p],
     "spf_phase_create": [_int, ctypes.POINTER(_c_void_p)],

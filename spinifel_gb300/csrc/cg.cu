@@ -588,7 +588,9 @@ int spf_cg_solve(spf_merge_s *G, int form, const double *d_b, double *d_x, int x
 // Regularisation sweep: the MPI merge gives every rank its own
 // (rlambda, flambda) and keeps the result the L-curve rule picks
 // (spinifel/mpi/autocorrelation.py:64-68, 173-214).  Here the n systems
-//   W_l x = conv(x) + rlambda_l x + flambda_l reg(x) = ADb + rlambda_l x0
+//   W_l x = c conv(x) + rlambda_l x + flambda_l reg(x) = ADb + rlambda_l x0
+// (c = 1 for the sequential merge's scaling, M^3 for the MPI merge, whose
+// kernel transform is not divided by M^3: mpi/autocorrelation.py:95-104)
 // run as one batched CG on one GPU: every vector is [n][M^3], the FFTs are
 // batched cuFFT plans, and each launch covers all systems (blockIdx.y, or one
 // block per system for the scalar stages), so an iteration costs the same
@@ -863,7 +865,8 @@ __global__ void k_sw_iters(const int *flags, int *iters, int nl) {
 
 // W v for all systems (v already loaded into conv_in / reg_in): q = W v, and
 // the partials of v . q
-static int sweep_operator(spf_merge_s *G, Sweep *w, const double *v, cudaStream_t s) {
+static int sweep_operator(spf_merge_s *G, Sweep *w, const double *v, double conv_factor,
+                          cudaStream_t s) {
   const int nl = w->nl;
   cufftSetStream(w->r2c, s);
   cufftSetStream(w->c2r, s);
@@ -882,15 +885,17 @@ static int sweep_operator(spf_merge_s *G, Sweep *w, const double *v, cudaStream_
   SPF_TRY(cufft_ok(cufftExecZ2D(w->z2d, reinterpret_cast<cufftDoubleComplex *>(w->reg_freq), w->reg_out),
                    "sweep reg Z2D"));
   k_sw_assemble<<<dim3(RED_BLOCKS, nl), RED_THREADS, 0, s>>>(
-      v, G->support, G->M, G->L, w->conv_out, G->conv_scale, w->reg_out, w->lam, w->q, w->partial);
+      v, G->support, G->M, G->L, w->conv_out, G->conv_scale * conv_factor, w->reg_out, w->lam,
+      w->q, w->partial);
   return check_launch("k_sw_assemble");
 }
 
 }  // namespace cg
 }  // namespace spf
 
-extern "C" int spf_merge_cg_sweep(spf_merge_s *G, int n_lambda, const double *h_rlambda,
-                                  const double *h_flambda, const double *d_adb,
+extern "C" int spf_merge_cg_sweep(spf_merge_s *G, int n_lambda, double conv_factor,
+                                  const double *h_rlambda, const double *h_flambda,
+                                  const double *d_adb,
                                   const double *d_x0, double *d_x, int maxiter, double rtol,
                                   double *d_norms, double *d_hist, int *d_iters, void *stream) {
   using namespace spf::cg;
@@ -922,7 +927,7 @@ extern "C" int spf_merge_cg_sweep(spf_merge_s *G, int n_lambda, const double *h_
     k_sw_load<<<gb, 256, 0, s>>>(d_x, nullptr, nullptr, nullptr, G->support, G->M, G->L,
                                  w->conv_in, w->reg_in);
     SPF_TRY(check_launch("k_sw_load"));
-    SPF_TRY(sweep_operator(G, w, d_x, s));
+    SPF_TRY(sweep_operator(G, w, d_x, conv_factor, s));
     k_sw_sub<<<gb, 256, 0, s>>>(w->d, w->q, w->r, n);
   } else {
     SPF_TRY(check_cuda(cudaMemcpyAsync(w->r, w->d, nl * n * sizeof(double),
@@ -942,7 +947,7 @@ extern "C" int spf_merge_cg_sweep(spf_merge_s *G, int n_lambda, const double *h_
     k_sw_load<<<gb, 256, 0, s>>>(w->p, w->r, w->scal, w->flags, G->support, G->M, G->L,
                                  w->conv_in, w->reg_in);
     SPF_TRY(check_launch("k_sw_load"));
-    SPF_TRY(sweep_operator(G, w, w->p, s));
+    SPF_TRY(sweep_operator(G, w, w->p, conv_factor, s));
     k_sw_stage2<<<nl, RED_THREADS, 0, s>>>(w->partial, w->scal, w->flags);
     SPF_TRY(check_launch("k_sw_stage2"));
     k_sw_update_xr<<<gb, 256, 0, s>>>(d_x, w->r, w->p, w->q, w->scal, w->flags, n);
@@ -960,7 +965,7 @@ extern "C" int spf_merge_cg_sweep(spf_merge_s *G, int n_lambda, const double *h_
     k_sw_load<<<gb, 256, 0, s>>>(d_x, nullptr, nullptr, nullptr, G->support, G->M, G->L,
                                  w->conv_in, w->reg_in);
     SPF_TRY(check_launch("k_sw_load"));
-    SPF_TRY(sweep_operator(G, w, d_x, s));
+    SPF_TRY(sweep_operator(G, w, d_x, conv_factor, s));
     k_sw_sub<<<gb, 256, 0, s>>>(w->q, w->d, w->r, n);
     SPF_TRY(check_launch("k_sw_sub"));
     k_sw_dot<<<dim3(RED_BLOCKS, nl), RED_THREADS, 0, s>>>(w->r, w->r, n, w->partial);

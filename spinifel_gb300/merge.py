@@ -100,3 +100,30 @@ class MergeOperator:
                   int(maxiter), float(rtol), _lib.ptr(hist), _lib.ptr(iters),
                   _lib.stream_handle())
         return x, iters, hist
+
+    def cg_sweep(self, rlambdas, flambdas, adb: torch.Tensor, x0: torch.Tensor | None,
+                 maxiter: int, rtol: float = 1e-5, conv_factor: float = 1.0,
+                 history: bool = False):
+        """All (rlambda_l, flambda_l) systems in one batched device CG
+        (Toeplitz form): returns x [n, M^3], norms [n, 2] = (||x_l||,
+        ||W_l x_l - d_l||), iterations [n] and, if asked, residual histories."""
+        rl = np.ascontiguousarray(rlambdas, dtype=np.float64)
+        fl = np.ascontiguousarray(flambdas, dtype=np.float64)
+        if rl.shape != fl.shape or rl.ndim != 1:
+            raise ValueError("rlambdas and flambdas must be 1-D of the same length")
+        nl = rl.size
+        n = self.M ** 3
+        adb = adb.to(device=self.device, dtype=torch.float64).contiguous().reshape(-1)
+        if x0 is not None:
+            x0 = x0.to(device=self.device, dtype=torch.float64).contiguous().reshape(-1)
+        x = torch.empty(nl, n, dtype=torch.float64, device=self.device)
+        norms = torch.empty(nl, 2, dtype=torch.float64, device=self.device)
+        iters = torch.zeros(nl, dtype=torch.int32, device=self.device)
+        hist = torch.zeros(nl, max(maxiter, 1), dtype=torch.float64, device=self.device) \
+            if history else None
+        P = ctypes.POINTER(ctypes.c_double)
+        _lib.call("spf_merge_cg_sweep", self._h, nl, float(conv_factor),
+                  rl.ctypes.data_as(P), fl.ctypes.data_as(P), _lib.ptr(adb), _lib.ptr(x0),
+                  _lib.ptr(x), int(maxiter), float(rtol), _lib.ptr(norms), _lib.ptr(hist),
+                  _lib.ptr(iters), _lib.stream_handle())
+        return x, norms, iters, hist

@@ -12,6 +12,7 @@ SNM = dict(seed=7003, M=21, det_shape=(4, 16, 16), n_orient=300, batch=100, n_im
            photons=2.0)
 OPS = dict(seed=7004, M=15, npts=2000)
 MERGE = dict(seed=7005, M=15, det_shape=(4, 8, 8), n_images=40, maxiter=20, photons=2.0)
+SWEEP = dict(size=4)  # MPI ranks of the regularisation sweep, on MERGE's inputs
 PHASE = dict(seed=7006, Mquat=5, nER=4, nHIO=3, N_phase_loops=2, beta=0.9)
 
 

@@ -17,6 +17,9 @@ oracle/nufft.py for the un-vendored finufft) and then calls, unmodified:
   * spinifel.sequential.autocorrelation.Merge.solve_ac (scipy cg)
                                                      -> golden_merge.npz
   * spinifel.autocorrelation.forward / adjoint glue  -> golden_ops.npz
+  * spinifel.mpi.autocorrelation.MergeMPI.solve_ac, its ranks run as
+    threads over an in-process communicator (gather / bcast / Bcast)
+                                                     -> golden_sweep.npz
   * spinifel.sequential.phasing.phase (numpy branch) -> golden_phase.npz
     (numpy 2 dropped numpy.infty, which phase() reads; it is set to inf)
 
@@ -267,6 +270,97 @@ def main():
     np.savez_compressed(os.path.join(HERE, "golden_phase.npz"), ac_phased=ac_phased,
                         support_=np.asarray(support_, dtype=np.uint8), rho_=rho_)
     print("phase", ac_phased.ravel()[:3], int(np.asarray(support_).sum()))
+
+
+    # --- MergeMPI: ranks as threads ----------------------------------------------
+    sweep = _mpi_merge_sweep(st, g, rsac)
+    np.savez_compressed(os.path.join(HERE, "golden_sweep.npz"), **sweep)
+    print("sweep", sweep["ref_rank_gen0"], sweep["ref_rank_gen1"], sweep["summary_gen0"][:, 2])
+
+
+class _ThreadComm:
+    """An in-process stand-in for an MPI communicator whose ranks are
+    threads: gather / bcast / Bcast through a barrier."""
+
+    def __init__(self, size):
+        import threading
+
+        self.size = size
+        self._bar = threading.Barrier(size)
+        self._slots = [None] * size
+        self._local = threading.local()
+        self._data = None
+
+    @property
+    def rank(self):
+        return self._local.rank
+
+    def gather(self, obj, root=0):
+        self._slots[self.rank] = obj
+        self._bar.wait()
+        out = list(self._slots) if self.rank == root else None
+        if out is not None:
+            self.last_gather = out
+        self._bar.wait()
+        return out
+
+    def bcast(self, obj, root=0):
+        if self.rank == root:
+            self._data = obj
+        self._bar.wait()
+        out = self._data
+        self._bar.wait()
+        return out
+
+    def Bcast(self, buf, root=0):
+        if self.rank == root:
+            self._data = np.array(buf, copy=True)
+        self._bar.wait()
+        buf[...] = self._data
+        self._bar.wait()
+
+
+def _mpi_merge_sweep(st, g, rsac):
+    import threading
+
+    size = cases.SWEEP["size"]
+    comm = _ThreadComm(size)
+    ctx = types.ModuleType("spinifel.contexts")
+    ctx.comm_compute = comm
+    sys.modules["spinifel.contexts"] = ctx
+    import spinifel
+    spinifel.contexts = ctx
+    mpi4py = types.ModuleType("mpi4py")
+    mpi4py.MPI = types.SimpleNamespace(COMM_WORLD=comm)
+    sys.modules["mpi4py"] = mpi4py
+    mpi_pkg = types.ModuleType("spinifel.mpi")
+    mpi_pkg.__path__ = [os.path.join(REF, "spinifel", "mpi")]
+    sys.modules["spinifel.mpi"] = mpi_pkg
+    import spinifel.mpi.autocorrelation as rmac
+
+    data, ppr, pdr, orient, ac_est = cases.merge_inputs()
+    out = {}
+    for gen, est in ((0, None), (1, ac_est)):
+        res = [None] * size
+        merges = [None] * size
+
+        def run(rank):
+            comm._local.rank = rank
+            m = rmac.MergeMPI(st, data, ppr, pdr, OracleNUFFT(orient, ppr, pdr))
+            merges[rank] = m
+            res[rank] = m.solve_ac(gen, orient, None if est is None else est.copy())
+
+        th = [threading.Thread(target=run, args=(r,)) for r in range(size)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        out[f"ac_gen{gen}"] = np.asarray(res[0].real)
+        out[f"ref_rank_gen{gen}"] = np.array(merges[0].ref_rank)
+        # (rank, rlambda, ||x||, ||W x - d||) as rank 0 gathered them
+        out[f"summary_gen{gen}"] = np.array(comm.last_gather, dtype=np.float64)
+        assert all(np.array_equal(res[0], r) for r in res)
+    return out
 
 
 if __name__ == "__main__":

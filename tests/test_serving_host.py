@@ -15,3 +15,18 @@ def test_poisson_schedule_sizes_and_rate():
     assert 1700 < rate < 2300
     # log-uniform sizes: the median is near sqrt(512)
     assert 12 < np.median(sizes) < 40
+
+
+def test_mpi_sweep_lambdas_and_choice():
+    """The per-rank lambdas and rank 0's L-curve choice of the MPI merge
+    (spinifel/mpi/autocorrelation.py:64-67,188-196), host logic only."""
+    from spinifel_gb300.mpi.autocorrelation import choose, lambdas
+
+    rl, fl = lambdas(15, 2560, 4)
+    np.testing.assert_allclose(rl, 15 ** 3 / 2560 * 2.0 ** (np.arange(4) - 2))
+    np.testing.assert_allclose(fl, [1e3, 1e4, 1e5, 1e6])
+    v1 = np.array([8.5, 7.8, 6.9, 5.7])
+    v2 = np.array([0.1, 0.3, 1.0, 2.5])
+    assert choose(0, rl, v1, v2) == 1        # largest lambda among norms >= mean
+    assert choose(1, rl, v1, v2) == 2        # smallest v1 + v2 (6.9 + 1.0)
+    assert choose(1, rl, v1, v1 * 0) == 3
