@@ -442,6 +442,40 @@ int spf_phase_run(spf_phaser phaser, int n_phase_loops, int n_er, int n_hio, dou
                   double rho_max, int method, double weight, double cutoff, void *stream);
 int spf_phase_finish(spf_phaser phaser, double *d_ac_phased, int *h_shift, void *stream);
 
+/* ---- frame preparation ---------------------------------------------------
+ * Clipping and 2^n_bin x 2^n_bin binning of uint16 photon-count frames
+ * [n_img][n_panels][sa][sb] in one pass (spinifel/prep.py:37-125,
+ * binning_sum / binning_mean): the high-resolution border is clipped by
+ * 2^n_clip (four PnCCD panels: panels 0 and 2 keep the last rows and columns,
+ * 1 and 3 the last rows and first columns; one panel: the central region),
+ * then blocks are summed (mean = 0) or averaged (mean = 1) exactly.
+ * d_out: [n_img][n_panels][ca >> n_bin][cb >> n_bin] floats, ca x cb the
+ * clipped panel.  Clipping of other panel counts is rejected (the reference
+ * prints a message and returns zeros). */
+int spf_bin_frames_u16(const uint16_t *d_raw, int64_t n_img, int n_panels, int sa, int sb,
+                       int n_clip, int n_bin, int mean, float *d_out, void *stream);
+
+/* ---- reconstruction quality (eval/fsc.py, eval/align.py) ----------------
+ * Volumes are M^3 doubles, C order; quaternions [w, x, y, z] doubles.
+ * spf_eval_score_rotations: d_cc[q] = Pearson correlation between vol1
+ *   rotated by quaternion q (rotate_volume, align.py:36-67: trilinear,
+ *   zero outside the grid) and vol2 -- score_deformations (align.py:92-120)
+ *   without materialising the rotated copies.
+ * spf_eval_rotate_volume: d_out [n_quat][M^3] = the rotated copies.
+ * spf_eval_fsc_shells: d_sums [n_shells][3] = per shell i (i*spacing < |q| <
+ *   i*spacing + spacing, |q| = |(c_a, c_b, c_c)| * scale on the fftshifted
+ *   grid, d_coord = the M mesh coordinates) the sums of Re(F1 conj F2),
+ *   |F1|^2 and |F2|^2 of F = fftshift(fftn(vol)) (fsc.py:67-125); the FSC is
+ *   sums[0] / sqrt(sums[1] sums[2]).  These evaluation calls allocate
+ *   stream-ordered scratch (cudaMallocAsync). */
+int spf_eval_score_rotations(const double *d_vol1, const double *d_vol2, int M,
+                             const double *d_quats, int64_t n_quat, double *d_cc, void *stream);
+int spf_eval_rotate_volume(const double *d_vol, int M, const double *d_quats, int64_t n_quat,
+                           double *d_out, void *stream);
+int spf_eval_fsc_shells(const double *d_vol1, const double *d_vol2, int M, const double *d_coord,
+                        double scale, double spacing, int n_shells, double *d_sums,
+                        void *stream);
+
 /* d_out[p] = max over rows r of x[r, p]^2 (n_pix floats). */
 int spf_col_maxsq_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_out,
                       void *stream);

@@ -133,6 +133,13 @@ SIGNATURES = {
     "spf_merge_cg_sweep": [_c_void_p, _int, _dbl, ctypes.POINTER(_dbl), ctypes.POINTER(_dbl),
                            _c_void_p, _c_void_p, _c_void_p, _int, _dbl, _c_void_p, _c_void_p,
                            _c_void_p, _c_void_p],
+    "spf_eval_score_rotations": [_c_void_p, _c_void_p, _int, _c_void_p, _i64, _c_void_p,
+                                 _c_void_p],
+    "spf_eval_rotate_volume": [_c_void_p, _int, _c_void_p, _i64, _c_void_p, _c_void_p],
+    "spf_eval_fsc_shells": [_c_void_p, _c_void_p, _int, _c_void_p, _dbl, _dbl, _int, _c_void_p,
+                            _c_void_p],
+    "spf_bin_frames_u16": [_c_void_p, _i64, _int, _int, _int, _int, _int, _int, _c_void_p,
+                           _c_void_p],
     "spf_phase_create": [_int, ctypes.POINTER(_c_void_p)],
     "spf_phase_destroy": [_c_void_p],
     "spf_phase_set_ac": [_c_void_p, _c_void_p, _c_void_p],

@@ -21,6 +21,12 @@ oracle/nufft.py for the un-vendored finufft) and then calls, unmodified:
     threads over an in-process communicator (gather / bcast / Bcast)
                                                      -> golden_sweep.npz
   * spinifel.sequential.phasing.phase (numpy branch) -> golden_phase.npz
+  * spinifel.prep clipping / binning / SAXS on seeded frames and geometry
+    (numpy 2 dropped numpy.int, which get_saxs reads; it is set to int)
+                                                     -> golden_prep.npz
+  * eval.fsc.compute_fsc, eval.align.rotate_volume / score_deformations /
+    center_volume / align_volumes (numpy branch; skopi's samplers and
+    numpy's global generator seeded)               -> golden_eval.npz
     (numpy 2 dropped numpy.infty, which phase() reads; it is set to inf)
 
 Inputs are regenerated from the stored seeds by tests (numpy PCG64 streams are
@@ -272,10 +278,65 @@ def main():
     print("phase", ac_phased.ravel()[:3], int(np.asarray(support_).sum()))
 
 
+    # --- prep: clipping and binning ------------------------------------------------
+    pr = _prep_golden()
+    np.savez_compressed(os.path.join(HERE, "golden_prep.npz"), **pr)
+    print("prep", {k: v.shape for k, v in pr.items()})
+
+    # --- eval: FSC and alignment -------------------------------------------------
+    ev = _eval_golden()
+    np.savez_compressed(os.path.join(HERE, "golden_eval.npz"), **ev)
+    print("eval", ev["resolution"], ev["final_cc"])
+
     # --- MergeMPI: ranks as threads ----------------------------------------------
     sweep = _mpi_merge_sweep(st, g, rsac)
     np.savez_compressed(os.path.join(HERE, "golden_sweep.npz"), **sweep)
     print("sweep", sweep["ref_rank_gen0"], sweep["ref_rank_gen1"], sweep["summary_gen0"][:, 2])
+
+
+def _prep_golden():
+    sys.modules["h5py"] = types.ModuleType("h5py")
+    sys.modules.setdefault("mrcfile", types.ModuleType("mrcfile"))
+    if not hasattr(np, "int"):
+        np.int = int
+    import spinifel.prep as rprep
+
+    c = cases.PREP
+    f4, f1, index_map, ppr = cases.prep_inputs()
+    nc, nb = c["n_clip"], c["n_bin"]
+    dist = rprep.compute_pixel_distance(ppr)
+    qs, saxs = rprep.get_saxs(dist, f4.mean(axis=0))
+    return dict(sum4=rprep.bin2nx2n_sum(rprep.clipping(f4, nc), nb),
+                mean4=rprep.bin2nx2n_mean(rprep.clipping(f4, nc), nb),
+                sum1=rprep.bin2nx2n_sum(rprep.clipping(f1, nc), nb),
+                sum4_noclip=rprep.bin2nx2n_sum(rprep.clipping(f4, 0), nb),
+                index4=rprep.bin2nx2n_index(rprep.clipping_index(index_map.copy(), nc), nb),
+                dist=dist, saxs_q=qs, saxs=saxs)
+
+
+def _eval_golden():
+    mpl = sys.modules["matplotlib"]
+    mpl.use = lambda *a, **k: None
+    mrc = types.ModuleType("mrcfile")
+    sys.modules["mrcfile"] = mrc
+    v1, v2, uniform_quat, random_quat, randn = cases.eval_inputs()
+    skp = sys.modules["skopi"]
+    skp.get_uniform_quat = lambda n, avoid_symmetric=True: uniform_quat(n)
+    skp.get_random_quat = lambda n: random_quat(n)
+    import eval.align as ral
+    import eval.fsc as rfsc
+
+    c = cases.EVAL
+    res, rshell, fsc = rfsc.compute_fsc(v1, v2, c["dmax"], spacing=c["spacing"])
+    quats = uniform_quat(12)
+    rot = ral.rotate_volume(v1, quats[:3])
+    ccs = ral.score_deformations(v1, v2, quats)
+    cen = ral.center_volume(v2)
+    np.random.seed(c["seed"] + 2)  # the search's randn draws
+    r_vol, m2, final_cc = ral.align_volumes(v1, v2, n_iterations=c["n_iterations"],
+                                            n_search=c["n_search"])
+    return dict(resolution=np.array(res), rshell=rshell, fsc=fsc, quats=quats, rot=rot,
+                ccs=ccs, centred=cen, r_vol=r_vol, mrc2=m2, final_cc=np.array(final_cc))
 
 
 class _ThreadComm:

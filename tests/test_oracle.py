@@ -159,3 +159,46 @@ def test_oracle_mpi_sweep_matches_reference_golden():
         assert iref == int(g[f"ref_rank_gen{gen}"])
         np.testing.assert_allclose(rows, g[f"summary_gen{gen}"], rtol=1e-7)
         assert np.linalg.norm(x - g[f"ac_gen{gen}"]) / np.linalg.norm(g[f"ac_gen{gen}"]) < 1e-7
+
+
+def test_oracle_eval_matches_reference_golden():
+    """FSC and alignment restatements against eval/fsc.py and eval/align.py
+    run on the same volumes and sampler streams."""
+    from oracle import evaluate as oev
+
+    c = cases.EVAL
+    g = np.load(os.path.join(GOLD, "golden_eval.npz"))
+    v1, v2, uq, rq, rn = cases.eval_inputs()
+    with np.errstate(invalid="ignore"):
+        res, rshell, fsc = oev.compute_fsc(v1, v2, c["dmax"], c["spacing"])
+    assert res == float(g["resolution"])
+    np.testing.assert_array_equal(fsc, g["fsc"])
+    quats = uq(12)
+    np.testing.assert_array_equal(oev.rotate_volume(v1, quats[:3]), g["rot"])
+    np.testing.assert_array_equal(oev.score_deformations(v1, v2, quats), g["ccs"])
+    np.testing.assert_array_equal(oev.center_volume(v2), g["centred"])
+    r_vol, m2, fc, _, _ = oev.align_volumes(v1, v2, uq, rq, rn, n_iterations=c["n_iterations"],
+                                            n_search=c["n_search"])
+    assert fc == float(g["final_cc"])
+    np.testing.assert_array_equal(r_vol, g["r_vol"])
+
+
+def test_prep_restatement_matches_reference_golden():
+    """spinifel_gb300.prep's numpy functions (detector geometry) against
+    spinifel/prep.py run on the same arrays: identical."""
+    from spinifel_gb300 import prep
+
+    c = cases.PREP
+    g = np.load(os.path.join(GOLD, "golden_prep.npz"))
+    f4, f1, index_map, ppr = cases.prep_inputs()
+    nc, nb = c["n_clip"], c["n_bin"]
+    np.testing.assert_array_equal(prep.bin2nx2n_sum(prep.clipping(f4, nc), nb), g["sum4"])
+    np.testing.assert_array_equal(prep.bin2nx2n_mean(prep.clipping(f4, nc), nb), g["mean4"])
+    np.testing.assert_array_equal(prep.bin2nx2n_sum(prep.clipping(f1, nc), nb), g["sum1"])
+    np.testing.assert_array_equal(prep.bin2nx2n_index(prep.clipping_index(index_map.copy(), nc),
+                                                      nb), g["index4"])
+    dist = prep.compute_pixel_distance(ppr)
+    np.testing.assert_array_equal(dist, g["dist"])
+    q, saxs = prep.get_saxs(dist, f4.mean(axis=0))
+    np.testing.assert_array_equal(q, g["saxs_q"])
+    np.testing.assert_array_equal(saxs, g["saxs"])
