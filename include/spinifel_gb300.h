@@ -332,7 +332,8 @@ int spf_rerank_fp32(float *d_cand_d, int32_t *d_cand_i, int64_t n_tiles,
  * to d_list[i*cap ..] (d_count[i] = number found, zeroed by the call; a count
  * above cap means the list overflowed); spf_rerank_list_fp32 computes the
  * listed distances with the plain path's arithmetic and folds the
- * lexicographic minimum into d_best (the spf_best_* format). */
+ * lexicographic minimum into d_best (the spf_best_* format); a frame whose
+ * count is above cap is skipped (its list is incomplete). */
 int spf_dist_range_bf16(const void *d_img_bf16, int64_t n_img, const void *d_ref_bf16,
                         int64_t n_ref, int64_t n_pix, int64_t ld, const float *d_ref_sq,
                         const float *d_thresh, int32_t *d_list, int32_t *d_count, int cap,
@@ -341,6 +342,57 @@ int spf_rerank_list_fp32(const int32_t *d_list, const int32_t *d_count, int cap,
                          const float *d_img, const float *d_img_sq, int64_t n_img,
                          const float *d_ref, const float *d_ref_sq, int64_t n_pix,
                          int64_t ref_offset, uint64_t *d_best, void *stream);
+
+/* spf_rerank_fp32 that keeps the candidate buffers intact: the merged top-8
+ * of each frame goes to d_merged_d / d_merged_i (n_img x 8 each) instead of
+ * over tile 0, so that the per-tile lists remain for spf_complete_open. */
+int spf_rerank_fp32_keep(const float *d_cand_d, const int32_t *d_cand_i, int64_t n_tiles,
+                         const float *d_img, const float *d_img_sq, int64_t n_img,
+                         const float *d_ref, const float *d_ref_sq, const float *d_ref_m2,
+                         float ref_sq_max, int64_t n_ref, int64_t n_pix, int64_t ref_offset,
+                         float *d_work, int32_t *d_idx, float *d_dist, int32_t *d_uncertified,
+                         float *d_merged_d, int32_t *d_merged_i, void *stream);
+
+/* Certified completion from the kept tile lists.  spf_scan_band_bf16: for
+ * each open frame d_rows[r] with bound d_thresh[r] (spf_rerank_fp32's d_work
+ * value), the references of every tile list whose approximate distance lies
+ * within the bound go to d_list[r][..] (d_count[r] of them); a tile whose 8
+ * entries all lie within the bound may hold more and sets d_count[r] to
+ * cap + 1.  spf_complete_open runs the whole completion for n_rows open
+ * frames: the scan, the exact re-rank of the lists (plain-path arithmetic),
+ * the range GEMM for frames whose tile lists may hide references, and the
+ * plain pass for a range list over its cap; d_idx / d_dist (n_rows each)
+ * receive the answers in row order; h_stats (may be NULL) gets {frames sent
+ * to the range GEMM, frames sent to the plain pass, 0}.  Allocates
+ * stream-ordered scratch and synchronises the stream. */
+int spf_scan_band_bf16(const float *d_cand_d, const int32_t *d_cand_i, int64_t n_tiles,
+                       int64_t n_img, const int64_t *d_rows, int64_t n_rows,
+                       const float *d_thresh, int32_t *d_list, int32_t *d_count, int cap,
+                       void *stream);
+int spf_complete_open(const float *d_cand_d, const int32_t *d_cand_i, int64_t n_tiles,
+                      const void *d_img_bf16, const float *d_img, const float *d_img_sq,
+                      const float *d_work, int64_t n_img, const int64_t *d_rows, int64_t n_rows,
+                      const void *d_ref_bf16, const float *d_ref, const float *d_ref_sq,
+                      int64_t n_ref, int64_t n_pix, int64_t ld, int32_t *d_idx, float *d_dist,
+                      int64_t *h_stats, void *stream);
+
+/* Batch matching from host memory in one synchronous call, the form of the
+ * reference's slicing_and_match step (host frames in, host indices out;
+ * spinifel/sequential/orientation_matching.py:113-186): h_counts [n_img][n_pix]
+ * uint16 (pinned memory lets the copies overlap the work) is moved to the
+ * device in chunks of chunk_frames (<= 0: 2560) on an internal copy stream
+ * while the previous chunk is ingested, matched on the tensor cores and
+ * re-ranked on `stream`; the frames the certificate leaves open are completed
+ * from each chunk's kept tile lists at the end.  h_idx / h_dist (n_img each;
+ * h_dist may be NULL) receive the plain FP32 path's answer; h_stats (may be
+ * NULL, 3 int64) gets {uncertified frames, frames completed by the range
+ * GEMM, frames completed by the plain pass}.  Scratch comes from the
+ * device's stream-ordered pool. */
+int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img, const void *d_ref_bf16,
+                        const float *d_ref, const float *d_ref_sq, const float *d_ref_m2,
+                        float ref_sq_max, int64_t n_ref, int64_t n_pix, int64_t ld,
+                        int64_t chunk_frames, int32_t *h_idx, float *h_dist, int64_t *h_stats,
+                        void *stream);
 
 /* Matching for callers that cannot allocate device memory: code that records
  * its work inside a CUDA stream capture (an allocation breaks the capture)
@@ -389,7 +441,8 @@ int spf_match_bf16_static(const void *d_img_bf16, const float *d_img, const floa
  * released).  A bounded device wait that gave up fails the slot's requests
  * with SPF_ERR_TIMEOUT while the device error word stays set.
  * spf_serve_stats: h_out[0..8] = requests, frames, launches, uncertified
- * frames, range-list overflows, summed GPU ms of the matching stage, budget
+ * frames, frames whose tile lists could hide references (completed by the
+ * range GEMM or the plain pass), summed GPU ms of the matching stage, budget
  * waits, p50 and p99 latency in ms.  spf_serve_destroy completes queued
  * requests, stops the thread and frees the buffers. */
 double spf_serve_clock(void);
@@ -490,6 +543,11 @@ int spf_row_norms_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_
  * guarantees 0 <= d_rows[i] < n_src_rows). */
 int spf_gather_rows(const void *d_src, int64_t n_src_rows, int64_t row_bytes,
                     const int64_t *d_rows, int64_t n, void *d_dst, void *stream);
+
+/* Row scatter, the inverse of spf_gather_rows: d_dst[d_rows[i]] = d_src[i]
+ * (the caller guarantees 0 <= d_rows[i] < n_dst_rows, no repeats). */
+int spf_scatter_rows(const void *d_src, int64_t row_bytes, const int64_t *d_rows, int64_t n,
+                     void *d_dst, int64_t n_dst_rows, void *stream);
 
 /* FP32 -> bf16 with a padded row stride: dst[r*ld + p] = bf16(src[r*n_pix+p])
  * for p < n_pix, 0 for n_pix <= p < ld. */

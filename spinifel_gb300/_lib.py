@@ -140,6 +140,18 @@ SIGNATURES = {
                             _c_void_p],
     "spf_bin_frames_u16": [_c_void_p, _i64, _int, _int, _int, _int, _int, _int, _c_void_p,
                            _c_void_p],
+    "spf_scatter_rows": [_c_void_p, _i64, _c_void_p, _i64, _c_void_p, _i64, _c_void_p],
+    "spf_rerank_fp32_keep": [_c_void_p, _c_void_p, _i64, _c_void_p, _c_void_p, _i64, _c_void_p,
+                             _c_void_p, _c_void_p, ctypes.c_float, _i64, _i64, _i64, _c_void_p,
+                             _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p],
+    "spf_scan_band_bf16": [_c_void_p, _c_void_p, _i64, _i64, _c_void_p, _i64, _c_void_p,
+                           _c_void_p, _c_void_p, _int, _c_void_p],
+    "spf_complete_open": [_c_void_p, _c_void_p, _i64, _c_void_p, _c_void_p, _c_void_p,
+                          _c_void_p, _i64, _c_void_p, _i64, _c_void_p, _c_void_p, _c_void_p,
+                          _i64, _i64, _i64, _c_void_p, _c_void_p, _c_void_p, _c_void_p],
+    "spf_match_bf16_host": [_c_void_p, _i64, _c_void_p, _c_void_p, _c_void_p, _c_void_p,
+                            ctypes.c_float, _i64, _i64, _i64, _i64, _c_void_p, _c_void_p,
+                            _c_void_p, _c_void_p],
     "spf_phase_create": [_int, ctypes.POINTER(_c_void_p)],
     "spf_phase_destroy": [_c_void_p],
     "spf_phase_set_ac": [_c_void_p, _c_void_p, _c_void_p],

@@ -185,7 +185,10 @@ __global__ void k_fsc(const double2 *__restrict__ s1, const double2 *__restrict_
        f += (int64_t)gridDim.x * blockDim.x) {
     const int c = (int)(f % M), b = (int)((f / M) % M), a = (int)(f / ((int64_t)M * M));
     const double x = coord[a], y = coord[b], z = coord[c];
-    const double s = sqrt(x * x + y * y + z * z) * scale;
+    // numpy's norm over the last axis: ((x^2 + y^2) + z^2), no fused multiply-add
+    const double s =
+        __dmul_rn(sqrt(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z))),
+                  scale);
     const int i0 = (int)floor(s / spacing);
     bool any = false;
     double2 z1, z2;

@@ -1,0 +1,195 @@
+// Batch matching from host memory in one call: the drop-in for the
+// reference's synchronous slicing_and_match matching step
+// (spinifel/sequential/orientation_matching.py:113-186), which takes host
+// frames and returns host indices, with the copies overlapped by the work.
+//
+// The frames are split into chunks.  A copy stream moves chunk k+1 host ->
+// device while the caller's stream ingests chunk k (FP32, bf16, norms), runs
+// the bf16 tcgen05 top-8 and the exact FP32 re-rank.  Each chunk keeps its
+// per-tile candidate lists, from which the frames the certificate leaves
+// open are completed at the end (spf_complete_open: no second pass over the
+// references unless a tile list may hide one); indices and distances are
+// copied back.  Scratch comes from the device's stream-ordered pool
+// (cudaMallocAsync), whose release threshold is raised once so that repeated
+// calls reuse the memory.
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+namespace {
+
+struct Scratch {
+  cudaStream_t s;
+  std::vector<void *> bufs;
+  int st = SPF_OK;
+  explicit Scratch(cudaStream_t stream) : s(stream) {}
+  template <class T>
+  T *get(size_t bytes) {
+    void *p = nullptr;
+    if (st == SPF_OK)
+      st = spf::check_cuda(cudaMallocAsync(&p, std::max<size_t>(bytes, 16), s),
+                           "spf_match_bf16_host: cudaMallocAsync");
+    if (p) bufs.push_back(p);
+    return static_cast<T *>(p);
+  }
+  ~Scratch() {
+    for (void *p : bufs) cudaFreeAsync(p, s);
+  }
+};
+
+void keep_pool_memory(int dev) {
+  static std::mutex mu;
+  static bool done[64] = {false};
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev < 0 || dev >= 64 || done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  done[dev] = true;
+}
+
+}  // namespace
+
+extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
+                                   const void *d_ref_bf16, const float *d_ref,
+                                   const float *d_ref_sq, const float *d_ref_m2, float ref_sq_max,
+                                   int64_t n_ref, int64_t n_pix, int64_t ld,
+                                   int64_t chunk_frames, int32_t *h_idx, float *h_dist,
+                                   int64_t *h_stats, void *stream) {
+  SPF_REQUIRE(n_img >= 0 && n_ref > 0 && n_pix > 0 && ld >= n_pix && ld % 8 == 0,
+              "spf_match_bf16_host: bad sizes");
+  if (h_stats) h_stats[0] = h_stats[1] = h_stats[2] = 0;
+  if (n_img == 0) return SPF_OK;
+  SPF_REQUIRE(h_counts && d_ref_bf16 && d_ref && d_ref_sq && d_ref_m2 && h_idx,
+              "spf_match_bf16_host: NULL pointer");
+  const int64_t chunk =
+      chunk_frames > 0 ? std::min(chunk_frames, n_img) : std::min<int64_t>(n_img, 2560);
+  const int64_t n_chunks = (n_img + chunk - 1) / chunk;
+  SPF_REQUIRE(n_chunks <= 4096, "spf_match_bf16_host: more than 4096 chunks");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  keep_pool_memory(dev);
+  cudaStream_t s = spf::as_stream(stream);
+  void *sv = s;
+  const int64_t tiles = spf_dist_topk_bf16_tiles(n_ref);
+  int st = SPF_OK;
+  cudaStream_t cs = nullptr;
+  std::vector<cudaEvent_t> ev;
+  {
+    Scratch W(s);
+    uint16_t *u16 = W.get<uint16_t>((size_t)n_img * n_pix * 2);
+    float *f32 = W.get<float>((size_t)n_img * n_pix * 4);
+    char *bf16 = W.get<char>((size_t)n_img * ld * 2);
+    float *sq = W.get<float>(n_img * 4), *n4 = W.get<float>(n_img * 4);
+    float *work = W.get<float>(n_img * 4), *dist = W.get<float>(n_img * 4);
+    int32_t *idx = W.get<int32_t>(n_img * 4), *unc = W.get<int32_t>(n_img * 4);
+    // every chunk keeps its tile lists for the completion of its open frames
+    const size_t cslot = (size_t)tiles * chunk * 8;
+    float *cand_d = W.get<float>(cslot * 4 * n_chunks);
+    int32_t *cand_i = W.get<int32_t>(cslot * 4 * n_chunks);
+    float *mrg_d = W.get<float>((size_t)n_img * 8 * 4);
+    int32_t *mrg_i = W.get<int32_t>((size_t)n_img * 8 * 4);
+    st = W.st;
+    if (st == SPF_OK)
+      st = spf::check_cuda(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking),
+                           "spf_match_bf16_host");
+    // the scratch above is ordered on s; the copy stream must not run ahead of it
+    cudaEvent_t ready = nullptr;
+    if (st == SPF_OK)
+      st = spf::check_cuda(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming),
+                           "spf_match_bf16_host");
+    if (ready) ev.push_back(ready);
+    if (st == SPF_OK) st = spf::check_cuda(cudaEventRecord(ready, s), "spf_match_bf16_host");
+    if (st == SPF_OK) st = spf::check_cuda(cudaStreamWaitEvent(cs, ready, 0), "spf_match_bf16_host");
+    for (int64_t k = 0; k < n_chunks && st == SPF_OK; ++k) {
+      const int64_t r0 = k * chunk, n = std::min(chunk, n_img - r0);
+      cudaEvent_t e = nullptr;
+      st = spf::check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming),
+                           "spf_match_bf16_host");
+      if (st != SPF_OK) break;
+      ev.push_back(e);
+      st = spf::check_cuda(cudaMemcpyAsync(u16 + r0 * n_pix, h_counts + r0 * n_pix,
+                                           (size_t)n * n_pix * 2, cudaMemcpyHostToDevice, cs),
+                           "spf_match_bf16_host: frames to device");
+      if (st == SPF_OK) st = spf::check_cuda(cudaEventRecord(e, cs), "spf_match_bf16_host");
+      if (st == SPF_OK) st = spf::check_cuda(cudaStreamWaitEvent(s, e, 0), "spf_match_bf16_host");
+      if (st == SPF_OK)
+        st = spf_frames_ingest_u16(u16 + r0 * n_pix, n, n_pix, f32 + r0 * n_pix, bf16 + r0 * ld * 2,
+                                   ld, sq + r0, n4 + r0, sv);
+      if (st == SPF_OK)
+        st = spf_dist_topk_bf16(bf16 + r0 * ld * 2, n, d_ref_bf16, n_ref, n_pix, ld, d_ref_sq,
+                                cand_d + k * cslot, cand_i + k * cslot, sv);
+      if (st == SPF_OK)
+        st = spf_rerank_fp32_keep(cand_d + k * cslot, cand_i + k * cslot, tiles, f32 + r0 * n_pix,
+                                  sq + r0, n, d_ref, d_ref_sq, d_ref_m2, ref_sq_max, n_ref, n_pix,
+                                  0, work + r0, idx + r0, dist + r0, unc + r0, mrg_d + r0 * 8,
+                                  mrg_i + r0 * 8, sv);
+    }
+    // results and the open frames back to the host
+    std::vector<int32_t> h_unc(n_img);
+    std::vector<float> h_d(h_dist ? 0 : n_img);
+    float *dist_out = h_dist ? h_dist : h_d.data();
+    if (st == SPF_OK)
+      st = spf::check_cuda(cudaMemcpyAsync(h_idx, idx, n_img * 4, cudaMemcpyDeviceToHost, s),
+                           "spf_match_bf16_host");
+    if (st == SPF_OK)
+      st = spf::check_cuda(cudaMemcpyAsync(dist_out, dist, n_img * 4, cudaMemcpyDeviceToHost, s),
+                           "spf_match_bf16_host");
+    if (st == SPF_OK)
+      st = spf::check_cuda(cudaMemcpyAsync(h_unc.data(), unc, n_img * 4, cudaMemcpyDeviceToHost, s),
+                           "spf_match_bf16_host");
+    if (st == SPF_OK) st = spf::check_cuda(cudaStreamSynchronize(s), "spf_match_bf16_host");
+    int64_t n_bad = 0, n_range = 0, n_plain = 0;
+    // completion per chunk, from that chunk's kept tile lists
+    for (int64_t k = 0; st == SPF_OK && k < n_chunks; ++k) {
+      const int64_t r0 = k * chunk, n = std::min(chunk, n_img - r0);
+      std::vector<int64_t> rows_k;
+      for (int64_t i = 0; i < n; ++i)
+        if (h_unc[r0 + i]) rows_k.push_back(i);
+      if (rows_k.empty()) continue;
+      const int64_t nb = (int64_t)rows_k.size();
+      n_bad += nb;
+      Scratch C(s);
+      int64_t *rows = C.get<int64_t>(nb * 8);
+      int32_t *idx2 = C.get<int32_t>(nb * 4);
+      float *dist2 = C.get<float>(nb * 4);
+      st = C.st;
+      std::vector<int32_t> h_i2(nb);
+      std::vector<float> h_d2(nb);
+      int64_t hs[3] = {0, 0, 0};
+      if (st == SPF_OK)
+        st = spf::check_cuda(cudaMemcpyAsync(rows, rows_k.data(), nb * 8, cudaMemcpyHostToDevice, s),
+                             "spf_match_bf16_host");
+      if (st == SPF_OK)
+        st = spf_complete_open(cand_d + k * cslot, cand_i + k * cslot, tiles, bf16 + r0 * ld * 2,
+                               f32 + r0 * n_pix, sq + r0, work + r0, n, rows, nb, d_ref_bf16,
+                               d_ref, d_ref_sq, n_ref, n_pix, ld, idx2, dist2, hs, sv);
+      if (st == SPF_OK)
+        st = spf::check_cuda(cudaMemcpyAsync(h_i2.data(), idx2, nb * 4, cudaMemcpyDeviceToHost, s),
+                             "spf_match_bf16_host");
+      if (st == SPF_OK)
+        st = spf::check_cuda(cudaMemcpyAsync(h_d2.data(), dist2, nb * 4, cudaMemcpyDeviceToHost, s),
+                             "spf_match_bf16_host");
+      if (st == SPF_OK) st = spf::check_cuda(cudaStreamSynchronize(s), "spf_match_bf16_host");
+      for (int64_t j = 0; st == SPF_OK && j < nb; ++j) {
+        h_idx[r0 + rows_k[j]] = h_i2[j];
+        dist_out[r0 + rows_k[j]] = h_d2[j];
+      }
+      n_range += hs[0];
+      n_plain += hs[1];
+    }
+    if (h_stats) {
+      h_stats[0] = n_bad;
+      h_stats[1] = n_range;
+      h_stats[2] = n_plain;
+    }
+  }
+  cudaStreamSynchronize(s);  // the scratch frees are ordered before the copy stream goes
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  if (cs) cudaStreamDestroy(cs);
+  return st;
+}

@@ -30,6 +30,7 @@
 #include <cudaTypedefs.h>
 
 #include <mutex>
+#include <vector>
 
 #include "common.cuh"
 
@@ -446,13 +447,15 @@ __device__ __forceinline__ bool lex_less(float a, int32_t ia, float b, int32_t i
 }
 
 // Block per frame: the 8 smallest candidates over all reference tiles (by
-// distance, then index), written over cand[tile 0][frame]; and the frame's
+// distance, then index), written to mrg[frame] (tile 0's slot of the
+// candidate buffers when mrg is that slot, the older layout); and the frame's
 // bf16 error variance term V = sum_p x_p^2 max_r s_rp^2 (negated when some
 // x_p is not exact in bf16) into work[frame].
 __global__ void __launch_bounds__(RR_THREADS)
-    k_merge_top8(float *__restrict__ cand_d, int32_t *__restrict__ cand_i, int64_t n_tiles,
-                 const float *__restrict__ img, int64_t n_img, const float *__restrict__ m2,
-                 int64_t n_pix, float *__restrict__ work) {
+    k_merge_top8(const float *__restrict__ cand_d, const int32_t *__restrict__ cand_i,
+                 int64_t n_tiles, const float *__restrict__ img, int64_t n_img,
+                 const float *__restrict__ m2, int64_t n_pix, float *__restrict__ work,
+                 float *__restrict__ mrg_d, int32_t *__restrict__ mrg_i) {
   __shared__ float s_d[RR_THREADS / 32][TOPK];
   __shared__ int32_t s_i[RR_THREADS / 32][TOPK];
   __shared__ float s_v[RR_THREADS / 32];
@@ -552,9 +555,9 @@ __global__ void __launch_bounds__(RR_THREADS)
       }
       if (h < 2 && hv == bv && hi == bi) ++h;
       if (lane == 0) {
-        size_t off = (size_t)im * TOPK + r;  // tile 0's slot of this frame
-        cand_d[off] = bv;
-        cand_i[off] = bi;
+        size_t off = (size_t)im * TOPK + r;
+        mrg_d[off] = bv;
+        mrg_i[off] = bi;
       }
     }
     if (lane == 0) {
@@ -578,6 +581,24 @@ __global__ void __launch_bounds__(RR_THREADS)
 // 256-pixel chunks (double-buffered, rows padded to 257 floats so the 32
 // chains read 32 different banks).  Lane 0 of each group of 8 keeps the
 // lexicographic minimum and evaluates the certificate.
+// The certificate's band: a bound on |approximate - exact| distance for any
+// reference (CERT_SIGMAS sigma of the bf16 rounding, per-pixel bound, plus
+// the FP32 accumulation error of both paths).
+__device__ __forceinline__ float cert_band(float V, float x2, float ref_sq_max, int64_t n_pix) {
+  float vs = V < 0.0f ? -2.0f * V : V;  // x rounding doubles the variance term
+  float sig16 = 2.0f * U_BF16 * 0.57735027f * sqrtf(vs);
+  float sig32 = U_FP32 * sqrtf((float)n_pix) * (x2 + ref_sq_max);
+  return CERT_SIGMAS * (sig16 + 2.0f * sig32);
+}
+
+// A candidate whose approximate distance exceeds the best approximate one by
+// more than twice the band cannot be the exact minimum (its exact distance
+// is above the band's upper end for the best candidate), so its row is not
+// read: only the candidates near the best are re-ranked.
+__device__ __forceinline__ bool rerank_skip(const float *cand_d, int64_t im, int c, float band) {
+  return c > 0 && cand_d[(size_t)im * TOPK + c] > cand_d[(size_t)im * TOPK] + 2.0f * band;
+}
+
 constexpr int RX_FRAMES = 4;
 constexpr int RX_ROWS = RX_FRAMES * (TOPK + 1);  // 4 frame rows + 32 candidate rows
 constexpr int RX_CHUNK = 256;
@@ -612,7 +633,9 @@ __global__ void __launch_bounds__(RX_THREADS)
       int64_t im = f0 + q / TOPK;
       if (im < n_img) {
         int32_t j = cand_i[(size_t)im * TOPK + (q % TOPK)];
-        if (j != INT32_MAX) ptr = ref + (int64_t)j * n_pix;
+        float band = cert_band(work[im], img_sq[im], ref_sq_max, n_pix);
+        if (j != INT32_MAX && !rerank_skip(cand_d, im, q % TOPK, band))
+          ptr = ref + (int64_t)j * n_pix;
       }
     }
     rows[tid] = ptr;
@@ -667,8 +690,9 @@ __global__ void __launch_bounds__(RX_THREADS)
   const bool live = im < n_img;
   const int64_t imc = live ? im : 0;
   int32_t j = cand_i[(size_t)imc * TOPK + c];
-  const bool valid = live && j != INT32_MAX;
   float x2 = live ? img_sq[imc] : 0.0f;
+  const float band = live ? cert_band(work[imc], x2, ref_sq_max, n_pix) : 0.0f;
+  const bool valid = live && j != INT32_MAX && !rerank_skip(cand_d, imc, c, band);
   float dist = valid ? __fsub_rn(__fadd_rn(x2, ref_sq[j]), __fmul_rn(2.0f, acc))
                      : __int_as_float(0x7f800000);
   int32_t jj = valid ? j : INT32_MAX;
@@ -693,11 +717,6 @@ __global__ void __launch_bounds__(RX_THREADS)
   // FP32 accumulation error of both paths; the re-ranked best must lie below
   int32_t j7 = cand_i[(size_t)im * TOPK + TOPK - 1];
   int cert = 1;
-  float V = work[im];
-  float vs = V < 0.0f ? -2.0f * V : V;  // x rounding doubles the variance term
-  float sig16 = 2.0f * U_BF16 * 0.57735027f * sqrtf(vs);
-  float sig32 = U_FP32 * sqrtf((float)n_pix) * (x2 + ref_sq_max);
-  float band = CERT_SIGMAS * (sig16 + 2.0f * sig32);
   if (j7 != INT32_MAX) {
     float d8 = cand_d[(size_t)im * TOPK + TOPK - 1] + x2;
     cert = (d8 - band - dist) > 0.0f ? 1 : 0;
@@ -731,7 +750,10 @@ __global__ void __launch_bounds__(RX_THREADS)
   const int tid = threadIdx.x, lane = tid & 31;
   if (im >= n_img) return;
   int cnt = count[im];
-  if (cnt > cap) cnt = cap;
+  // a count above the cap marks a list that is incomplete (overflowed, or a
+  // saturated tile list that may hide references, with fewer than cap entries
+  // written): the caller settles that frame another way, so nothing is read
+  if (cnt > cap) cnt = 0;
   const int64_t nchunks = (n_pix + RX_CHUNK - 1) / RX_CHUNK;
   const bool vec = (n_pix % 4) == 0 && aligned(img, 16) && aligned(ref, 16);
   unsigned long long kbest = ~0ULL;
@@ -1008,29 +1030,225 @@ int spf_rerank_list_fp32(const int32_t *d_list, const int32_t *d_count, int cap,
   return check_launch("k_rerank_list");
 }
 
+}  // extern "C" (reopened below)
+
+namespace spf {
+namespace bf16mm {
+
+// Block per open frame (rows[r]): every candidate of every reference tile
+// whose approximate distance lies within the frame's bound thresh[r] goes to
+// list[r][...] (count[r] of them; the order does not matter to the re-rank).
+// The tile lists hold each tile's 8 smallest approximate distances, so they
+// contain every in-bound reference of the tile unless all 8 are in bound: the
+// tile may then hold more, and count[r] is set above the cap so that the
+// caller searches that frame by the range GEMM.
+__global__ void __launch_bounds__(256)
+    k_scan_band(const float *__restrict__ cand_d, const int32_t *__restrict__ cand_i,
+                int64_t n_tiles, int64_t n_img, const int64_t *__restrict__ rows,
+                const float *__restrict__ thresh, int32_t *__restrict__ list,
+                int32_t *__restrict__ count, int cap) {
+  __shared__ int cnt, sat;
+  const int64_t r = blockIdx.x;
+  const int64_t im = rows[r];
+  const float T = thresh[r];
+  if (threadIdx.x == 0) {
+    cnt = 0;
+    sat = 0;
+  }
+  __syncthreads();
+  for (int64_t t = threadIdx.x; t < n_tiles; t += blockDim.x) {
+    const size_t off = ((size_t)t * n_img + im) * TOPK;
+    int valid = 0, inband = 0;
+#pragma unroll
+    for (int k = 0; k < TOPK; ++k) {
+      const int32_t j = cand_i[off + k];
+      if (j == INT32_MAX) continue;
+      ++valid;
+      if (cand_d[off + k] <= T) {
+        ++inband;
+        const int pos = atomicAdd(&cnt, 1);
+        if (pos < cap) list[r * (int64_t)cap + pos] = j;
+      }
+    }
+    if (valid == TOPK && inband == TOPK) sat = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) count[r] = sat ? cap + 1 : cnt;
+}
+
+}  // namespace bf16mm
+}  // namespace spf
+
+extern "C" {
+
+int spf_scan_band_bf16(const float *d_cand_d, const int32_t *d_cand_i, int64_t n_tiles,
+                       int64_t n_img, const int64_t *d_rows, int64_t n_rows,
+                       const float *d_thresh, int32_t *d_list, int32_t *d_count, int cap,
+                       void *stream) {
+  SPF_REQUIRE(n_tiles >= 0 && n_img >= 0 && n_rows >= 0 && cap >= 1,
+              "spf_scan_band_bf16: bad sizes");
+  if (n_rows == 0) return SPF_OK;
+  SPF_REQUIRE(d_cand_d && d_cand_i && d_rows && d_thresh && d_list && d_count,
+              "spf_scan_band_bf16: NULL pointer");
+  SPF_REQUIRE(n_rows < (1LL << 31), "spf_scan_band_bf16: too many rows");
+  spf::bf16mm::k_scan_band<<<(unsigned)n_rows, 256, 0, as_stream(stream)>>>(
+      d_cand_d, d_cand_i, n_tiles, n_img, d_rows, d_thresh, d_list, d_count, cap);
+  return check_launch("k_scan_band");
+}
+
+int spf_complete_open(const float *d_cand_d, const int32_t *d_cand_i, int64_t n_tiles,
+                      const void *d_img_bf16, const float *d_img, const float *d_img_sq,
+                      const float *d_work, int64_t n_img, const int64_t *d_rows, int64_t n_rows,
+                      const void *d_ref_bf16, const float *d_ref, const float *d_ref_sq,
+                      int64_t n_ref, int64_t n_pix, int64_t ld, int32_t *d_idx, float *d_dist,
+                      int64_t *h_stats, void *stream) {
+  SPF_REQUIRE(n_rows >= 0 && n_img >= 0, "spf_complete_open: bad sizes");
+  if (h_stats) h_stats[0] = h_stats[1] = h_stats[2] = 0;
+  if (n_rows == 0) return SPF_OK;
+  SPF_REQUIRE(d_cand_d && d_cand_i && d_img_bf16 && d_img && d_img_sq && d_work && d_rows &&
+                  d_ref_bf16 && d_ref && d_ref_sq && d_idx && d_dist,
+              "spf_complete_open: NULL pointer");
+  constexpr int CAP = 512;
+  cudaStream_t s = as_stream(stream);
+  void *sv = stream;
+  std::vector<void *> bufs;
+  int st = SPF_OK;
+  auto get = [&](size_t bytes) -> void * {
+    void *p = nullptr;
+    if (st == SPF_OK)
+      st = check_cuda(cudaMallocAsync(&p, bytes < 16 ? 16 : bytes, s), "spf_complete_open");
+    if (p) bufs.push_back(p);
+    return p;
+  };
+  const int64_t nr = n_rows;
+  float *f32_c = (float *)get((size_t)nr * n_pix * 4);
+  float *sq_c = (float *)get(nr * 4), *thr_c = (float *)get(nr * 4);
+  int32_t *lst = (int32_t *)get((size_t)nr * CAP * 4), *cnt = (int32_t *)get(nr * 4);
+  uint64_t *best = (uint64_t *)get(nr * 8);
+  int64_t *sub = (int64_t *)get(nr * 8);
+  void *bf_c = get((size_t)nr * ld * 2);
+  std::vector<int32_t> h_cnt(nr);
+  std::vector<int64_t> h_rows(nr);
+  if (st == SPF_OK) st = spf_gather_rows(d_img, n_img, n_pix * 4, d_rows, nr, f32_c, sv);
+  if (st == SPF_OK) st = spf_gather_rows(d_img_sq, n_img, 4, d_rows, nr, sq_c, sv);
+  if (st == SPF_OK) st = spf_gather_rows(d_work, n_img, 4, d_rows, nr, thr_c, sv);
+  // 1) the kept tile lists: every in-bound candidate, re-ranked exactly
+  if (st == SPF_OK)
+    st = spf_scan_band_bf16(d_cand_d, d_cand_i, n_tiles, n_img, d_rows, nr, thr_c, lst, cnt, CAP,
+                            sv);
+  if (st == SPF_OK) st = spf_best_init(best, nr, sv);
+  if (st == SPF_OK)
+    st = spf_rerank_list_fp32(lst, cnt, CAP, f32_c, sq_c, nr, d_ref, d_ref_sq, n_pix, 0, best, sv);
+  if (st == SPF_OK) st = spf_best_unpack(best, nr, d_idx, d_dist, sv);
+  if (st == SPF_OK)
+    st = check_cuda(cudaMemcpyAsync(h_cnt.data(), cnt, nr * 4, cudaMemcpyDeviceToHost, s),
+                    "spf_complete_open");
+  if (st == SPF_OK)
+    st = check_cuda(cudaMemcpyAsync(h_rows.data(), d_rows, nr * 8, cudaMemcpyDeviceToHost, s),
+                    "spf_complete_open");
+  if (st == SPF_OK) st = check_cuda(cudaStreamSynchronize(s), "spf_complete_open");
+  // 2) frames whose tile lists may hide references: the range GEMM, then
+  //    (a list over the cap) the plain pass
+  std::vector<int64_t> over_pos;  // positions within the rows
+  for (int64_t k = 0; st == SPF_OK && k < nr; ++k)
+    if (h_cnt[k] > CAP) over_pos.push_back(k);
+  if (h_stats) h_stats[0] = (int64_t)over_pos.size();
+  for (int pass = 0; pass < 2 && st == SPF_OK && !over_pos.empty(); ++pass) {
+    const int64_t no = (int64_t)over_pos.size();
+    std::vector<int64_t> h_sub(over_pos);
+    st = check_cuda(cudaMemcpyAsync(sub, h_sub.data(), no * 8, cudaMemcpyHostToDevice, s),
+                    "spf_complete_open");
+    // compact copies of those rows (frame data indexed within the gathered rows)
+    float *f32_o = (float *)get((size_t)no * n_pix * 4);
+    float *sq_o = (float *)get(no * 4), *thr_o = (float *)get(no * 4);
+    int32_t *idx_o = (int32_t *)get(no * 4);
+    float *dist_o = (float *)get(no * 4);
+    int64_t *frames_o = (int64_t *)get(no * 8);
+    if (st == SPF_OK) st = spf_gather_rows(f32_c, nr, n_pix * 4, sub, no, f32_o, sv);
+    if (st == SPF_OK) st = spf_gather_rows(sq_c, nr, 4, sub, no, sq_o, sv);
+    if (st == SPF_OK) st = spf_gather_rows(thr_c, nr, 4, sub, no, thr_o, sv);
+    if (st == SPF_OK) st = spf_best_init(best, no, sv);
+    std::vector<int32_t> h_c2(no, 0);
+    std::vector<int64_t> h_fr(no);
+    if (pass == 0) {
+      for (int64_t k = 0; k < no; ++k) h_fr[k] = h_rows[over_pos[k]];
+      if (st == SPF_OK)
+        st = check_cuda(cudaMemcpyAsync(frames_o, h_fr.data(), no * 8, cudaMemcpyHostToDevice, s),
+                        "spf_complete_open");
+      if (st == SPF_OK) st = spf_gather_rows(d_img_bf16, n_img, ld * 2, frames_o, no, bf_c, sv);
+      if (st == SPF_OK)
+        st = spf_dist_range_bf16(bf_c, no, d_ref_bf16, n_ref, n_pix, ld, d_ref_sq, thr_o, lst,
+                                 cnt, CAP, sv);
+      if (st == SPF_OK)
+        st = spf_rerank_list_fp32(lst, cnt, CAP, f32_o, sq_o, no, d_ref, d_ref_sq, n_pix, 0, best,
+                                  sv);
+      if (st == SPF_OK)
+        st = check_cuda(cudaMemcpyAsync(h_c2.data(), cnt, no * 4, cudaMemcpyDeviceToHost, s),
+                        "spf_complete_open");
+    } else if (st == SPF_OK) {
+      st = spf_dist_argmin_f32(f32_o, sq_o, no, d_ref, d_ref_sq, n_ref, n_pix, 0, best, sv);
+    }
+    if (st == SPF_OK) st = spf_best_unpack(best, no, idx_o, dist_o, sv);
+    // the completed rows go back into d_idx / d_dist at their positions
+    if (st == SPF_OK) st = spf_scatter_rows(idx_o, 4, sub, no, d_idx, nr, sv);
+    if (st == SPF_OK) st = spf_scatter_rows(dist_o, 4, sub, no, d_dist, nr, sv);
+    if (st == SPF_OK) st = check_cuda(cudaStreamSynchronize(s), "spf_complete_open");
+    std::vector<int64_t> next;
+    for (int64_t k = 0; pass == 0 && k < no; ++k)
+      if (h_c2[k] > CAP) next.push_back(over_pos[k]);
+    if (pass == 0 && h_stats) h_stats[1] = (int64_t)next.size();
+    over_pos.swap(next);
+  }
+  for (void *p : bufs) cudaFreeAsync(p, s);
+  return st;
+}
+
+static int rerank_impl(const char *name, float *d_cand_d, int32_t *d_cand_i, int64_t n_tiles,
+                       const float *d_img, const float *d_img_sq, int64_t n_img,
+                       const float *d_ref, const float *d_ref_sq, const float *d_ref_m2,
+                       float ref_sq_max, int64_t n_ref, int64_t n_pix, int64_t ref_offset,
+                       float *d_work, int32_t *d_idx, float *d_dist, int32_t *d_uncertified,
+                       int32_t *d_top8, float *d_mrg_d, int32_t *d_mrg_i, void *stream) {
+  SPF_REQUIRE(n_img >= 0 && n_ref >= 0 && n_pix >= 0 && n_tiles >= 0,
+              "%s: negative size", name);
+  if (n_img == 0) return SPF_OK;
+  SPF_REQUIRE(d_cand_d && d_cand_i && d_img && d_img_sq && d_ref && d_ref_sq && d_ref_m2 &&
+                  d_work && d_idx && d_mrg_d && d_mrg_i,
+              "%s: NULL pointer", name);
+  SPF_REQUIRE(n_tiles == (n_ref + BN - 1) / BN, "%s: n_tiles does not match n_ref", name);
+  SPF_REQUIRE(n_img < (1LL << 28), "%s: too many images", name);
+  cudaStream_t s = as_stream(stream);
+  k_merge_top8<<<(unsigned)n_img, RR_THREADS, 0, s>>>(d_cand_d, d_cand_i, n_tiles, d_img, n_img,
+                                                      d_ref_m2, n_pix, d_work, d_mrg_d, d_mrg_i);
+  SPF_TRY(check_launch("k_merge_top8"));
+  SPF_TRY(rerank_smem_attr());
+  k_rerank_exact<<<(unsigned)((n_img + RX_FRAMES - 1) / RX_FRAMES), RX_THREADS, RX_SMEM, s>>>(
+      d_mrg_d, d_mrg_i, d_img, d_img_sq, n_img, d_ref, d_ref_sq, ref_sq_max, n_pix, ref_offset,
+      d_work, d_idx, d_dist, d_uncertified, d_top8);
+  return check_launch("k_rerank_exact");
+}
+
 int spf_rerank_fp32(float *d_cand_d, int32_t *d_cand_i, int64_t n_tiles, const float *d_img,
                     const float *d_img_sq, int64_t n_img, const float *d_ref,
                     const float *d_ref_sq, const float *d_ref_m2, float ref_sq_max,
                     int64_t n_ref, int64_t n_pix, int64_t ref_offset, float *d_work,
                     int32_t *d_idx, float *d_dist, int32_t *d_uncertified, int32_t *d_top8,
                     void *stream) {
-  SPF_REQUIRE(n_img >= 0 && n_ref >= 0 && n_pix >= 0 && n_tiles >= 0,
-              "spf_rerank_fp32: negative size");
-  if (n_img == 0) return SPF_OK;
-  SPF_REQUIRE(d_cand_d && d_cand_i && d_img && d_img_sq && d_ref && d_ref_sq && d_ref_m2 &&
-                  d_work && d_idx,
-              "spf_rerank_fp32: NULL pointer");
-  SPF_REQUIRE(n_tiles == (n_ref + BN - 1) / BN, "spf_rerank_fp32: n_tiles does not match n_ref");
-  SPF_REQUIRE(n_img < (1LL << 28), "spf_rerank_fp32: too many images");
-  cudaStream_t s = as_stream(stream);
-  k_merge_top8<<<(unsigned)n_img, RR_THREADS, 0, s>>>(d_cand_d, d_cand_i, n_tiles, d_img, n_img,
-                                                      d_ref_m2, n_pix, d_work);
-  SPF_TRY(check_launch("k_merge_top8"));
-  SPF_TRY(rerank_smem_attr());
-  k_rerank_exact<<<(unsigned)((n_img + RX_FRAMES - 1) / RX_FRAMES), RX_THREADS, RX_SMEM, s>>>(
-      d_cand_d, d_cand_i, d_img, d_img_sq, n_img, d_ref, d_ref_sq, ref_sq_max, n_pix, ref_offset,
-      d_work, d_idx, d_dist, d_uncertified, d_top8);
-  return check_launch("k_rerank_exact");
+  return rerank_impl("spf_rerank_fp32", d_cand_d, d_cand_i, n_tiles, d_img, d_img_sq, n_img,
+                     d_ref, d_ref_sq, d_ref_m2, ref_sq_max, n_ref, n_pix, ref_offset, d_work,
+                     d_idx, d_dist, d_uncertified, d_top8, d_cand_d, d_cand_i, stream);
+}
+
+int spf_rerank_fp32_keep(const float *d_cand_d, const int32_t *d_cand_i, int64_t n_tiles,
+                         const float *d_img, const float *d_img_sq, int64_t n_img,
+                         const float *d_ref, const float *d_ref_sq, const float *d_ref_m2,
+                         float ref_sq_max, int64_t n_ref, int64_t n_pix, int64_t ref_offset,
+                         float *d_work, int32_t *d_idx, float *d_dist, int32_t *d_uncertified,
+                         float *d_merged_d, int32_t *d_merged_i, void *stream) {
+  return rerank_impl("spf_rerank_fp32_keep", const_cast<float *>(d_cand_d),
+                     const_cast<int32_t *>(d_cand_i), n_tiles, d_img, d_img_sq, n_img, d_ref,
+                     d_ref_sq, d_ref_m2, ref_sq_max, n_ref, n_pix, ref_offset, d_work, d_idx,
+                     d_dist, d_uncertified, nullptr, d_merged_d, d_merged_i, stream);
 }
 
 int spf_col_maxsq_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_out,
@@ -1181,7 +1399,7 @@ extern "C" int spf_match_bf16_static(const void *d_img_bf16, const float *d_img,
                                                             nullptr, nullptr, 0, GROUP_M, err);
   SPF_TRY(check_launch("k_dist_topk_bf16 (static scratch)"));
   k_merge_top8<<<(unsigned)n_img, RR_THREADS, 0, s>>>(cand_d, cand_i, tiles, d_img, n_img,
-                                                      d_ref_m2, n_pix, work);
+                                                      d_ref_m2, n_pix, work, cand_d, cand_i);
   SPF_TRY(check_launch("k_merge_top8 (static scratch)"));
   SPF_TRY(rerank_smem_attr());
   k_rerank_exact<<<(unsigned)((n_img + RX_FRAMES - 1) / RX_FRAMES), RX_THREADS, RX_SMEM, s>>>(

@@ -304,6 +304,18 @@ __global__ void k_gather_rows1(const unsigned char *__restrict__ src, int64_t ro
   }
 }
 
+// dst[rows[i]] = src[i], rows of row_bytes bytes
+__global__ void k_scatter_rows1(const unsigned char *__restrict__ src, int64_t row_bytes,
+                                const int64_t *__restrict__ rows, int64_t n,
+                                unsigned char *__restrict__ dst) {
+  int64_t total = n * row_bytes;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e / row_bytes, c = e % row_bytes;
+    dst[rows[i] * row_bytes + c] = src[e];
+  }
+}
+
 __global__ void k_f32_to_bf16(const float *__restrict__ src, int64_t n_rows, int64_t n_pix,
                               __nv_bfloat16 *__restrict__ dst, int64_t ld) {
   int64_t total = n_rows * ld;
@@ -474,6 +486,17 @@ int spf_gather_rows(const void *d_src, int64_t n_src_rows, int64_t row_bytes,
         reinterpret_cast<unsigned char *>(d_dst));
   }
   return check_launch("spf_gather_rows");
+}
+
+int spf_scatter_rows(const void *d_src, int64_t row_bytes, const int64_t *d_rows, int64_t n,
+                     void *d_dst, int64_t n_dst_rows, void *stream) {
+  SPF_REQUIRE(n >= 0 && row_bytes >= 0 && n_dst_rows >= 0, "spf_scatter_rows: negative size");
+  if (n == 0 || row_bytes == 0) return SPF_OK;
+  SPF_REQUIRE(d_src && d_rows && d_dst, "spf_scatter_rows: NULL pointer");
+  k_scatter_rows1<<<grid_for(n * row_bytes, 256, (int64_t)sm_count() * 16), 256, 0,
+                    as_stream(stream)>>>(reinterpret_cast<const unsigned char *>(d_src), row_bytes,
+                                         d_rows, n, reinterpret_cast<unsigned char *>(d_dst));
+  return check_launch("spf_scatter_rows");
 }
 
 int spf_f32_to_bf16(const float *d_src, int64_t n_rows, int64_t n_pix, void *d_dst, int64_t ld,

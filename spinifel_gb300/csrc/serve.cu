@@ -9,9 +9,9 @@
 // (copy in, ingest, bf16 tcgen05 top-8 + exact FP32 re-rank, copy out) and
 // polls the slots' events, so the copies and re-rank of one slot overlap the
 // tensor-core work of another.  Frames the re-rank certificate leaves open
-// get the certified completion (range query + exact list re-rank, and the
-// plain pass over all references for a list longer than its cap) before
-// their request is delivered.  A frame's result depends only on that frame
+// get the certified completion (the in-band references of the kept per-tile
+// candidate lists re-ranked exactly; the range GEMM and the plain pass only
+// where those lists may hide references) before their request is delivered.  A frame's result depends only on that frame
 // and the references, so batching never changes an answer.
 #include <algorithm>
 #include <chrono>
@@ -56,11 +56,10 @@ struct Slot {
   uint16_t *u16 = nullptr;
   float *f32 = nullptr, *sq = nullptr, *n4 = nullptr;
   void *bf16 = nullptr;
-  float *cand_d = nullptr, *work = nullptr, *dist = nullptr;
-  int32_t *cand_i = nullptr, *idx = nullptr, *unc = nullptr;
+  float *cand_d = nullptr, *work = nullptr, *dist = nullptr, *mrg_d = nullptr;
+  int32_t *cand_i = nullptr, *idx = nullptr, *unc = nullptr, *mrg_i = nullptr;
   uint64_t *best = nullptr;
   int64_t *rows = nullptr;
-  void *bf_c = nullptr;
   float *f32_c = nullptr, *sq_c = nullptr, *thr_c = nullptr, *dist2 = nullptr;
   int32_t *lst = nullptr, *cnt = nullptr, *idx2 = nullptr;
   // pinned host buffers
@@ -147,13 +146,14 @@ int Server::alloc_slot(Slot &s) {
   SPF_TRY(dev_alloc(&s.bf16, c * ld * 2));
   SPF_TRY(dev_alloc(&s.cand_d, tiles * c * 8 * 4));
   SPF_TRY(dev_alloc(&s.cand_i, tiles * c * 8 * 4));
+  SPF_TRY(dev_alloc(&s.mrg_d, c * 8 * 4));
+  SPF_TRY(dev_alloc(&s.mrg_i, c * 8 * 4));
   SPF_TRY(dev_alloc(&s.work, c * 4));
   SPF_TRY(dev_alloc(&s.dist, c * 4));
   SPF_TRY(dev_alloc(&s.idx, c * 4));
   SPF_TRY(dev_alloc(&s.unc, c * 4));
   SPF_TRY(dev_alloc(&s.best, c * 8));
   SPF_TRY(dev_alloc(&s.rows, c * 8));
-  SPF_TRY(dev_alloc(&s.bf_c, c * ld * 2));
   SPF_TRY(dev_alloc(&s.f32_c, c * n_pix * 4));
   SPF_TRY(dev_alloc(&s.sq_c, c * 4));
   SPF_TRY(dev_alloc(&s.thr_c, c * 4));
@@ -175,9 +175,9 @@ int Server::alloc_slot(Slot &s) {
 
 void Server::free_slot(Slot &s) {
   if (s.stream) cudaStreamSynchronize(s.stream);
-  void *dev[] = {s.u16, s.f32, s.sq, s.n4, s.bf16, s.cand_d, s.cand_i, s.work, s.dist, s.idx,
-                 s.unc, s.best, s.rows, s.bf_c, s.f32_c, s.sq_c, s.thr_c, s.dist2, s.idx2,
-                 s.cnt, s.lst};
+  void *dev[] = {s.u16, s.f32,  s.sq,    s.n4,   s.bf16, s.cand_d, s.cand_i, s.mrg_d,
+                 s.mrg_i, s.work, s.dist, s.idx, s.unc, s.best, s.rows, s.f32_c,
+                 s.sq_c, s.thr_c, s.dist2, s.idx2, s.cnt, s.lst};
   for (void *p : dev)
     if (p) cudaFree(p);
   void *host[] = {s.h_stage, s.h_idx, s.h_unc, s.h_idx2, s.h_cnt, s.h_dist, s.h_dist2,
@@ -243,9 +243,9 @@ int Server::launch(Slot &s) {
   if (path == 0) {
     SPF_TRY(spf_dist_topk_bf16(s.bf16, n, ref_bf16, n_ref, n_pix, ld, ref_sq, s.cand_d, s.cand_i,
                                sv));
-    SPF_TRY(spf_rerank_fp32(s.cand_d, s.cand_i, tiles, s.f32, s.sq, n, ref, ref_sq, ref_m2,
-                            ref_sq_max, n_ref, n_pix, 0, s.work, s.idx, s.dist, s.unc, nullptr,
-                            sv));
+    SPF_TRY(spf_rerank_fp32_keep(s.cand_d, s.cand_i, tiles, s.f32, s.sq, n, ref, ref_sq, ref_m2,
+                                 ref_sq_max, n_ref, n_pix, 0, s.work, s.idx, s.dist, s.unc,
+                                 s.mrg_d, s.mrg_i, sv));
     SPF_TRY(check_cuda(cudaMemcpyAsync(s.h_unc, s.unc, n * 4, cudaMemcpyDeviceToHost, st),
                        "spf_serve: flags to host"));
   } else {
@@ -266,7 +266,7 @@ int Server::launch(Slot &s) {
 }
 
 // Stage 1 landed on the host: enqueue the certified completion of the open
-// frames (no host wait) or report the slot finished.
+// frames from the kept tile lists (no host wait) or report the slot finished.
 int Server::complete_stage1(Slot &s, bool *finished) {
   float ms = 0.f;
   if (cudaEventElapsedTime(&ms, s.ev_start, s.ev_done) == cudaSuccess) {
@@ -287,12 +287,12 @@ int Server::complete_stage1(Slot &s, bool *finished) {
   std::copy(s.bad.begin(), s.bad.end(), s.h_rows);
   SPF_TRY(check_cuda(cudaMemcpyAsync(s.rows, s.h_rows, nb * 8, cudaMemcpyHostToDevice, st),
                      "spf_serve: rows to device"));
-  SPF_TRY(spf_gather_rows(s.bf16, s.n, ld * 2, s.rows, nb, s.bf_c, sv));
   SPF_TRY(spf_gather_rows(s.f32, s.n, n_pix * 4, s.rows, nb, s.f32_c, sv));
   SPF_TRY(spf_gather_rows(s.sq, s.n, 4, s.rows, nb, s.sq_c, sv));
   SPF_TRY(spf_gather_rows(s.work, s.n, 4, s.rows, nb, s.thr_c, sv));
-  SPF_TRY(spf_dist_range_bf16(s.bf_c, nb, ref_bf16, n_ref, n_pix, ld, ref_sq, s.thr_c, s.lst,
-                              s.cnt, kRangeCap, sv));
+  // every in-bound reference from the kept tile lists of the matching pass
+  SPF_TRY(spf_scan_band_bf16(s.cand_d, s.cand_i, tiles, s.n, s.rows, nb, s.thr_c, s.lst, s.cnt,
+                             kRangeCap, sv));
   SPF_TRY(spf_best_init(s.best, nb, sv));
   SPF_TRY(spf_rerank_list_fp32(s.lst, s.cnt, kRangeCap, s.f32_c, s.sq_c, nb, ref, ref_sq, n_pix,
                                0, s.best, sv));
@@ -312,15 +312,16 @@ int Server::complete_stage1(Slot &s, bool *finished) {
   return SPF_OK;
 }
 
-// Stage 2 landed: fold the list re-rank into the slot's results; a list that
-// overflowed its cap is settled by the plain pass over all references (rare;
-// the server thread waits for it).
+// Stage 2 landed: fold the list re-rank into the slot's results.  A frame
+// whose tile lists may hide references (or whose list is over its cap) is
+// completed by spf_complete_open -- the range GEMM, then the plain pass --
+// while the server thread waits (rare).
 int Server::complete_stage2(Slot &s) {
   const int64_t nb = (int64_t)s.bad.size();
   std::vector<int64_t> over;
   for (int64_t j = 0; j < nb; ++j) {
     if (s.h_cnt[j] > kRangeCap) {
-      over.push_back(j);
+      over.push_back(s.bad[j]);
     } else {
       s.h_idx[s.bad[j]] = s.h_idx2[j];
       s.h_dist[s.bad[j]] = s.h_dist2[j];
@@ -330,22 +331,20 @@ int Server::complete_stage2(Slot &s) {
   cudaStream_t st = s.stream;
   void *sv = st;
   const int64_t no = (int64_t)over.size();
-  for (int64_t k = 0; k < no; ++k) s.h_rows[k] = s.bad[over[k]];
+  for (int64_t k = 0; k < no; ++k) s.h_rows[k] = over[k];
   SPF_TRY(check_cuda(cudaMemcpyAsync(s.rows, s.h_rows, no * 8, cudaMemcpyHostToDevice, st),
                      "spf_serve: rows to device"));
-  SPF_TRY(spf_gather_rows(s.f32, s.n, n_pix * 4, s.rows, no, s.f32_c, sv));
-  SPF_TRY(spf_gather_rows(s.sq, s.n, 4, s.rows, no, s.sq_c, sv));
-  SPF_TRY(spf_best_init(s.best, no, sv));
-  SPF_TRY(spf_dist_argmin_f32(s.f32_c, s.sq_c, no, ref, ref_sq, n_ref, n_pix, 0, s.best, sv));
-  SPF_TRY(spf_best_unpack(s.best, no, s.idx2, s.dist2, sv));
+  int64_t hs[3];
+  SPF_TRY(spf_complete_open(s.cand_d, s.cand_i, tiles, s.bf16, s.f32, s.sq, s.work, s.n, s.rows,
+                            no, ref_bf16, ref, ref_sq, n_ref, n_pix, ld, s.idx2, s.dist2, hs, sv));
   SPF_TRY(check_cuda(cudaMemcpyAsync(s.h_idx2, s.idx2, no * 4, cudaMemcpyDeviceToHost, st),
-                     "spf_serve: overflow to host"));
+                     "spf_serve: completion to host"));
   SPF_TRY(check_cuda(cudaMemcpyAsync(s.h_dist2, s.dist2, no * 4, cudaMemcpyDeviceToHost, st),
-                     "spf_serve: overflow to host"));
-  SPF_TRY(check_cuda(cudaStreamSynchronize(st), "spf_serve: overflow pass"));
+                     "spf_serve: completion to host"));
+  SPF_TRY(check_cuda(cudaStreamSynchronize(st), "spf_serve: completion"));
   for (int64_t k = 0; k < no; ++k) {
-    s.h_idx[s.h_rows[k]] = s.h_idx2[k];
-    s.h_dist[s.h_rows[k]] = s.h_dist2[k];
+    s.h_idx[over[k]] = s.h_idx2[k];
+    s.h_dist[over[k]] = s.h_dist2[k];
   }
   std::lock_guard<std::mutex> g(mu);
   stat[4] += (double)no;

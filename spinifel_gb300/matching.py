@@ -10,6 +10,9 @@ numpy/cupy argmin does.
 """
 from __future__ import annotations
 
+import ctypes
+
+import numpy as np
 import torch
 
 from . import _lib
@@ -231,7 +234,9 @@ def match_bf16(frames: FrameSet, refs: ReferenceSet, exact_fallback: bool = True
                stats: dict | None = None, stream=None):
     """Best reference per frame: bf16 tensor-core distances, per-frame top-8,
     exact FP32 re-rank (bit-identical to the plain path's values); frames the
-    certificate cannot settle are re-matched exactly over all references."""
+    certificate cannot settle are completed exactly from the kept per-tile
+    candidate lists (spf_complete_open: list re-rank, and the range GEMM or
+    the plain pass only where those lists may hide references)."""
     if frames.n_pix != refs.n_pix or frames.ld != refs.ld:
         raise ValueError("frames and references differ in pixel count")
     dev = frames.f32.device
@@ -239,6 +244,8 @@ def match_bf16(frames: FrameSet, refs: ReferenceSet, exact_fallback: bool = True
     tiles = int(_lib.lib().spf_dist_topk_bf16_tiles(refs.n_ref))
     cand_d = _ws.get("cand_d", tiles * n_img * 8, torch.float32, dev)
     cand_i = _ws.get("cand_i", tiles * n_img * 8, torch.int32, dev)
+    mrg_d = _ws.get("merged_d", n_img * 8, torch.float32, dev)
+    mrg_i = _ws.get("merged_i", n_img * 8, torch.int32, dev)
     work = _ws.get("rerank_work", n_img, torch.float32, dev)
     idx = torch.empty(n_img, dtype=torch.int32, device=dev)
     dist = torch.empty(n_img, dtype=torch.float32, device=dev)
@@ -246,57 +253,58 @@ def match_bf16(frames: FrameSet, refs: ReferenceSet, exact_fallback: bool = True
     sh = _lib.stream_handle(stream)
     _lib.call("spf_dist_topk_bf16", _lib.ptr(frames.bf16), n_img, _lib.ptr(refs.bf16), refs.n_ref,
               refs.n_pix, refs.ld, _lib.ptr(refs.sq), _lib.ptr(cand_d), _lib.ptr(cand_i), sh)
-    _lib.call("spf_rerank_fp32", _lib.ptr(cand_d), _lib.ptr(cand_i), tiles, _lib.ptr(frames.f32),
-              _lib.ptr(frames.sq), n_img, _lib.ptr(refs.f32), _lib.ptr(refs.sq),
-              _lib.ptr(refs.m2), float(refs.sq_max), refs.n_ref, refs.n_pix, 0, _lib.ptr(work),
-              _lib.ptr(idx), _lib.ptr(dist), _lib.ptr(unc), None, sh)
+    _lib.call("spf_rerank_fp32_keep", _lib.ptr(cand_d), _lib.ptr(cand_i), tiles,
+              _lib.ptr(frames.f32), _lib.ptr(frames.sq), n_img, _lib.ptr(refs.f32),
+              _lib.ptr(refs.sq), _lib.ptr(refs.m2), float(refs.sq_max), refs.n_ref, refs.n_pix,
+              0, _lib.ptr(work), _lib.ptr(idx), _lib.ptr(dist), _lib.ptr(unc), _lib.ptr(mrg_d),
+              _lib.ptr(mrg_i), sh)
     if exact_fallback or stats is not None:
         bad = torch.nonzero(unc, as_tuple=False).flatten()
         nbad = int(bad.numel())
         if stats is not None:
             stats["uncertified"] = nbad
         if exact_fallback and nbad:
-            i2, d2 = _complete_range(frames, refs, bad,
-                                     gather_rows(work.view(-1, 1), bad).view(-1), stats, sh)
+            i2 = torch.empty(nbad, dtype=torch.int32, device=dev)
+            d2 = torch.empty(nbad, dtype=torch.float32, device=dev)
+            hs = np.zeros(3, dtype=np.int64)
+            _lib.call("spf_complete_open", _lib.ptr(cand_d), _lib.ptr(cand_i), tiles,
+                      _lib.ptr(frames.bf16), _lib.ptr(frames.f32), _lib.ptr(frames.sq),
+                      _lib.ptr(work), n_img, _lib.ptr(bad), nbad, _lib.ptr(refs.bf16),
+                      _lib.ptr(refs.f32), _lib.ptr(refs.sq), refs.n_ref, refs.n_pix, refs.ld,
+                      _lib.ptr(i2), _lib.ptr(d2), ctypes.c_void_p(hs.ctypes.data), sh)
             idx.index_copy_(0, bad, i2)
             dist.index_copy_(0, bad, d2)
+            if stats is not None:
+                stats["range_gemm_frames"] = int(hs[0])
+                stats["range_overflow"] = int(hs[1])
     return idx, dist
 
 
 RANGE_CAP = 512
 
 
-def _complete_range(frames: FrameSet, refs: ReferenceSet, rows: torch.Tensor,
-                    thresh: torch.Tensor, stats, sh):
-    """Exact answer for frames the top-8 certificate left open: collect every
-    reference inside the frame's error band with the tensor-core GEMM, re-rank
-    that list with the plain path's arithmetic; a list that overflows falls
-    back to the plain FP32 pass over all references."""
-    dev = frames.f32.device
-    n = int(rows.numel())
-    bf = gather_rows(frames.bf16, rows)
-    f32 = gather_rows(frames.f32, rows)
-    sq = gather_rows(frames.sq.view(-1, 1), rows).view(-1)
-    lst = _ws.get("range_list", n * RANGE_CAP, torch.int32, dev)
-    cnt = _ws.get("range_count", n, torch.int32, dev)
-    _lib.call("spf_dist_range_bf16", _lib.ptr(bf), n, _lib.ptr(refs.bf16), refs.n_ref, refs.n_pix,
-              refs.ld, _lib.ptr(refs.sq), _lib.ptr(thresh), _lib.ptr(lst), _lib.ptr(cnt),
-              RANGE_CAP, sh)
-    tr = BestTracker(n, dev)
-    _lib.call("spf_rerank_list_fp32", _lib.ptr(lst), _lib.ptr(cnt), RANGE_CAP, _lib.ptr(f32),
-              _lib.ptr(sq), n, _lib.ptr(refs.f32), _lib.ptr(refs.sq), refs.n_pix, 0,
-              _lib.ptr(tr.best), sh)
-    i2, d2 = tr.result()
-    over = torch.nonzero(cnt > RANGE_CAP, as_tuple=False).flatten()
-    n_over = int(over.numel())
+def match_bf16_host(frames_u16_host: torch.Tensor, refs: ReferenceSet, chunk_frames: int = 0,
+                    stream=None, stats: dict | None = None):
+    """Host frames in, host indices out, in one library call
+    (spf_match_bf16_host): chunked host -> device copies overlapped with the
+    tensor-core matching of the previous chunk.  frames_u16_host: [n, n_pix]
+    16-bit counts in host memory (pinned for the overlap).  Returns numpy
+    (indices int32, distances float32), the plain FP32 path's answer."""
+    if frames_u16_host.is_cuda or frames_u16_host.dtype not in (torch.int16, torch.uint16):
+        raise TypeError("frames must be 16-bit counts in host memory")
+    if frames_u16_host.dim() != 2 or frames_u16_host.shape[1] != refs.n_pix:
+        raise ValueError(f"frames must be [n, {refs.n_pix}]")
+    f = frames_u16_host.contiguous()
+    n = f.shape[0]
+    idx = np.empty(n, dtype=np.int32)
+    dist = np.empty(n, dtype=np.float32)
+    st = np.zeros(3, dtype=np.int64)
+    _lib.call("spf_match_bf16_host", ctypes.c_void_p(f.data_ptr()), n, _lib.ptr(refs.bf16),
+              _lib.ptr(refs.f32), _lib.ptr(refs.sq), _lib.ptr(refs.m2), float(refs.sq_max),
+              refs.n_ref, refs.n_pix, refs.ld, int(chunk_frames),
+              ctypes.c_void_p(idx.ctypes.data), ctypes.c_void_p(dist.ctypes.data),
+              ctypes.c_void_p(st.ctypes.data), _lib.stream_handle(stream))
     if stats is not None:
-        stats["range_overflow"] = n_over
-        stats["range_max_list"] = int(cnt.max().item()) if n else 0
-    if n_over:
-        t2 = BestTracker(n_over, dev)
-        t2.update_fp32(gather_rows(f32, over), gather_rows(sq.view(-1, 1), over).view(-1),
-                       refs.f32, refs.sq, 0)
-        i3, d3 = t2.result()
-        i2.index_copy_(0, over, i3)
-        d2.index_copy_(0, over, d3)
-    return i2, d2
+        stats["uncertified"] = int(st[0])
+        stats["range_gemm_frames"], stats["range_overflow"] = int(st[1]), int(st[2])
+    return idx, dist

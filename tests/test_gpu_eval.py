@@ -59,7 +59,11 @@ def test_align_volumes_matches_reference(gold):
 def test_rotation_round_trip_and_fsc_like_reference_test(lib):
     """The shape of the reference's tests/test_FSC.py with a synthetic 81^3
     density (its PDB-derived density needs skopi): rotate by q^-1 and back by
-    q; correlation > 0.85 and FSC resolution < 1.25 x 9 Angstrom."""
+    q, correlation > 0.85 as there; the blob density has less high-resolution
+    content than the PDB map, so instead of the 1.25 x 9 Angstrom bound the
+    FSC curve and resolution must equal the FP64 oracle's on the same
+    volumes."""
+    from oracle import evaluate as oev
     from spinifel_gb300 import geom
     from spinifel_gb300.eval.align import rotate_volume
     from spinifel_gb300.eval.fsc import compute_fsc
@@ -77,5 +81,9 @@ def test_rotation_round_trip_and_fsc_like_reference_test(lib):
     q_inv = q * np.array([1, -1, -1, -1])
     back = rotate_volume(rotate_volume(ref, q_inv)[0], q)
     assert np.corrcoef(ref.flatten(), back.flatten())[0, 1] > 0.85
-    res, _, _ = compute_fsc(ref, back[0], 1e10 / res_target, 0.01)
-    assert 0 < res < res_target * 1.25
+    res, _, fsc = compute_fsc(ref, back[0], 1e10 / res_target, 0.01)
+    with np.errstate(invalid="ignore"):
+        res_o, _, fsc_o = oev.compute_fsc(ref, back[0], 1e10 / res_target, 0.01)
+    ok = ~np.isnan(fsc_o)
+    np.testing.assert_allclose(fsc[ok], fsc_o[ok], rtol=1e-9, atol=1e-12)
+    assert res > 0 and abs(res - res_o) <= 1e-9 * res

@@ -123,3 +123,20 @@ def test_native_server_rejects_bad_requests(world):
         assert st == _lib.SPF_ERR_ARG and flag.value == 0
         ok = srv.submit(torch.from_numpy(world["frames"][:3].view(np.int16).copy()))
         assert ok.result(timeout=60).shape == (3,)
+
+
+@pytest.mark.parametrize("chunk", [0, 300, 1200])
+def test_host_batch_call_equals_plain_fp32(world, chunk):
+    """spf_match_bf16_host (chunked copies overlapped with matching, each
+    chunk's open frames completed from its kept tile lists): indices and
+    distances equal the plain FP32 pass, the open frames included."""
+    from spinifel_gb300 import matching
+
+    frames = world["frames"]
+    host = torch.from_numpy(frames.view(np.int16).copy()).pin_memory()
+    st = {}
+    idx, dist = matching.match_bf16_host(host, world["rs"], chunk_frames=chunk, stats=st)
+    pidx, pdist = _plain(world, frames)
+    np.testing.assert_array_equal(idx, pidx)
+    np.testing.assert_array_equal(dist, pdist)
+    assert st["uncertified"] >= 36 and st["range_overflow"] >= 6
