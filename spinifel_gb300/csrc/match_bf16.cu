@@ -643,21 +643,24 @@ __global__ void __launch_bounds__(RX_THREADS)
   __syncthreads();
   const int64_t nchunks = (n_pix + RX_CHUNK - 1) / RX_CHUNK;
   const bool vec = (n_pix % 4) == 0 && aligned(img, 16) && aligned(ref, 16);
-  // asynchronous 16-byte copies of one chunk of every row (ragged ends and
-  // missing rows filled with zeros by plain stores)
+  // asynchronous 16-byte copies of one chunk of every row (ragged ends by
+  // plain loads)
   auto stage = [&](int buf, int64_t chunk) {
     float *dst = rx + (size_t)buf * RX_ROWS * RX_STRIDE;
     const int64_t base = chunk * RX_CHUNK;
     for (int e = tid; e < RX_ROWS * (RX_CHUNK / 4); e += RX_THREADS) {
       int r = e / (RX_CHUNK / 4), q4 = (e % (RX_CHUNK / 4)) * 4;
       const float *src = rows[r];
+      // a row without source (a skipped candidate, a list slot past the end,
+      // a frame past the last) is not staged: its chain's result is discarded
+      if (!src) continue;
       int64_t p = base + q4;
       float *d = dst + r * RX_STRIDE + q4;
-      if (src && vec && p + 3 < n_pix) {
+      if (vec && p + 3 < n_pix) {
         cp_async16(d, src + p);
       } else {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) d[u] = (src && p + u < n_pix) ? __ldg(src + p + u) : 0.0f;
+        for (int u = 0; u < 4; ++u) d[u] = p + u < n_pix ? __ldg(src + p + u) : 0.0f;
       }
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
@@ -775,13 +778,14 @@ __global__ void __launch_bounds__(RX_THREADS)
       for (int e = tid; e < RL_ROWS * (RX_CHUNK / 4); e += RX_THREADS) {
         int r = e / (RX_CHUNK / 4), q4 = (e % (RX_CHUNK / 4)) * 4;
         const float *src = rows[r];
+        if (!src) continue;  // a slot past the list's end: its chain is discarded
         int64_t p = base + q4;
         float *d = dst + r * RX_STRIDE + q4;
-        if (src && vec && p + 3 < n_pix) {
+        if (vec && p + 3 < n_pix) {
           cp_async16(d, src + p);
         } else {
 #pragma unroll
-          for (int u = 0; u < 4; ++u) d[u] = (src && p + u < n_pix) ? __ldg(src + p + u) : 0.0f;
+          for (int u = 0; u < 4; ++u) d[u] = p + u < n_pix ? __ldg(src + p + u) : 0.0f;
         }
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
