@@ -6,10 +6,10 @@
 // The frames are split into chunks.  A copy stream moves chunk k+1 host ->
 // device while the caller's stream ingests chunk k (FP32, bf16, norms), runs
 // the bf16 tcgen05 top-8 and the exact FP32 re-rank.  Each chunk keeps its
-// per-tile candidate lists, from which the frames the certificate leaves
-// open are completed at the end (spf_complete_open: no second pass over the
-// references unless a tile list may hide one); indices and distances are
-// copied back.  Scratch comes from the device's stream-ordered pool
+// per-tile candidate lists; the frames the certificate leaves open are
+// completed at the end in one pass over all chunks (their in-band list
+// entries re-ranked exactly; no second pass over the references unless a
+// tile list may hide one); indices and distances are copied back.  Scratch comes from the device's stream-ordered pool
 // (cudaMallocAsync), whose release threshold is raised once so that repeated
 // calls reuse the memory.
 #include <algorithm>
@@ -84,7 +84,7 @@ extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
     uint16_t *u16 = W.get<uint16_t>((size_t)n_img * n_pix * 2);
     float *f32 = W.get<float>((size_t)n_img * n_pix * 4);
     char *bf16 = W.get<char>((size_t)n_img * ld * 2);
-    float *sq = W.get<float>(n_img * 4), *n4 = W.get<float>(n_img * 4);
+    float *sq = W.get<float>(n_img * 4);
     float *work = W.get<float>(n_img * 4), *dist = W.get<float>(n_img * 4);
     int32_t *idx = W.get<int32_t>(n_img * 4), *unc = W.get<int32_t>(n_img * 4);
     // every chunk keeps its tile lists for the completion of its open frames
@@ -119,7 +119,7 @@ extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
       if (st == SPF_OK) st = spf::check_cuda(cudaStreamWaitEvent(s, e, 0), "spf_match_bf16_host");
       if (st == SPF_OK)
         st = spf_frames_ingest_u16(u16 + r0 * n_pix, n, n_pix, f32 + r0 * n_pix, bf16 + r0 * ld * 2,
-                                   ld, sq + r0, n4 + r0, sv);
+                                   ld, sq + r0, nullptr, sv);
       if (st == SPF_OK)
         st = spf_dist_topk_bf16(bf16 + r0 * ld * 2, n, d_ref_bf16, n_ref, n_pix, ld, d_ref_sq,
                                 cand_d + k * cslot, cand_i + k * cslot, sv);
@@ -144,43 +144,103 @@ extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
                            "spf_match_bf16_host");
     if (st == SPF_OK) st = spf::check_cuda(cudaStreamSynchronize(s), "spf_match_bf16_host");
     int64_t n_bad = 0, n_range = 0, n_plain = 0;
-    // completion per chunk, from that chunk's kept tile lists
-    for (int64_t k = 0; st == SPF_OK && k < n_chunks; ++k) {
+    // completion of the open frames of all chunks in one pass: each chunk's
+    // kept tile lists are scanned into one list array, then one exact
+    // re-rank over every open frame; a frame whose tile lists may hide
+    // references is completed by spf_complete_open (range GEMM, plain pass)
+    constexpr int CAP = 512;
+    std::vector<int64_t> rows_g, rows_l, off(n_chunks + 1, 0);
+    for (int64_t k = 0; k < n_chunks; ++k) {
       const int64_t r0 = k * chunk, n = std::min(chunk, n_img - r0);
-      std::vector<int64_t> rows_k;
+      off[k] = (int64_t)rows_g.size();
       for (int64_t i = 0; i < n; ++i)
-        if (h_unc[r0 + i]) rows_k.push_back(i);
-      if (rows_k.empty()) continue;
-      const int64_t nb = (int64_t)rows_k.size();
-      n_bad += nb;
+        if (h_unc[r0 + i]) {
+          rows_g.push_back(r0 + i);
+          rows_l.push_back(i);
+        }
+    }
+    off[n_chunks] = (int64_t)rows_g.size();
+    const int64_t nb = (int64_t)rows_g.size();
+    n_bad = nb;
+    if (st == SPF_OK && nb > 0) {
       Scratch C(s);
-      int64_t *rows = C.get<int64_t>(nb * 8);
+      int64_t *d_rg = C.get<int64_t>(nb * 8), *d_rl = C.get<int64_t>(nb * 8);
+      float *f32_c = C.get<float>((size_t)nb * n_pix * 4);
+      float *sq_c = C.get<float>(nb * 4), *thr_c = C.get<float>(nb * 4);
+      int32_t *lst = C.get<int32_t>((size_t)nb * CAP * 4), *cnt = C.get<int32_t>(nb * 4);
+      uint64_t *best = C.get<uint64_t>(nb * 8);
       int32_t *idx2 = C.get<int32_t>(nb * 4);
       float *dist2 = C.get<float>(nb * 4);
       st = C.st;
-      std::vector<int32_t> h_i2(nb);
+      std::vector<int32_t> h_i2(nb), h_cnt(nb);
       std::vector<float> h_d2(nb);
-      int64_t hs[3] = {0, 0, 0};
       if (st == SPF_OK)
-        st = spf::check_cuda(cudaMemcpyAsync(rows, rows_k.data(), nb * 8, cudaMemcpyHostToDevice, s),
+        st = spf::check_cuda(cudaMemcpyAsync(d_rg, rows_g.data(), nb * 8, cudaMemcpyHostToDevice, s),
                              "spf_match_bf16_host");
       if (st == SPF_OK)
-        st = spf_complete_open(cand_d + k * cslot, cand_i + k * cslot, tiles, bf16 + r0 * ld * 2,
-                               f32 + r0 * n_pix, sq + r0, work + r0, n, rows, nb, d_ref_bf16,
-                               d_ref, d_ref_sq, n_ref, n_pix, ld, idx2, dist2, hs, sv);
+        st = spf::check_cuda(cudaMemcpyAsync(d_rl, rows_l.data(), nb * 8, cudaMemcpyHostToDevice, s),
+                             "spf_match_bf16_host");
+      if (st == SPF_OK) st = spf_gather_rows(f32, n_img, n_pix * 4, d_rg, nb, f32_c, sv);
+      if (st == SPF_OK) st = spf_gather_rows(sq, n_img, 4, d_rg, nb, sq_c, sv);
+      if (st == SPF_OK) st = spf_gather_rows(work, n_img, 4, d_rg, nb, thr_c, sv);
+      for (int64_t k = 0; st == SPF_OK && k < n_chunks; ++k) {
+        const int64_t nk = off[k + 1] - off[k];
+        if (!nk) continue;
+        const int64_t n = std::min(chunk, n_img - k * chunk);
+        st = spf_scan_band_bf16(cand_d + k * cslot, cand_i + k * cslot, tiles, n, d_rl + off[k], nk,
+                                thr_c + off[k], lst + off[k] * CAP, cnt + off[k], CAP, sv);
+      }
+      if (st == SPF_OK) st = spf_best_init(best, nb, sv);
+      if (st == SPF_OK)
+        st = spf_rerank_list_fp32(lst, cnt, CAP, f32_c, sq_c, nb, d_ref, d_ref_sq, n_pix, 0, best,
+                                  sv);
+      if (st == SPF_OK) st = spf_best_unpack(best, nb, idx2, dist2, sv);
       if (st == SPF_OK)
         st = spf::check_cuda(cudaMemcpyAsync(h_i2.data(), idx2, nb * 4, cudaMemcpyDeviceToHost, s),
                              "spf_match_bf16_host");
       if (st == SPF_OK)
         st = spf::check_cuda(cudaMemcpyAsync(h_d2.data(), dist2, nb * 4, cudaMemcpyDeviceToHost, s),
                              "spf_match_bf16_host");
+      if (st == SPF_OK)
+        st = spf::check_cuda(cudaMemcpyAsync(h_cnt.data(), cnt, nb * 4, cudaMemcpyDeviceToHost, s),
+                             "spf_match_bf16_host");
       if (st == SPF_OK) st = spf::check_cuda(cudaStreamSynchronize(s), "spf_match_bf16_host");
-      for (int64_t j = 0; st == SPF_OK && j < nb; ++j) {
-        h_idx[r0 + rows_k[j]] = h_i2[j];
-        dist_out[r0 + rows_k[j]] = h_d2[j];
+      for (int64_t j = 0; st == SPF_OK && j < nb; ++j)
+        if (h_cnt[j] <= CAP) {
+          h_idx[rows_g[j]] = h_i2[j];
+          dist_out[rows_g[j]] = h_d2[j];
+        }
+      // the rare frames whose tile lists may hide references, per chunk
+      for (int64_t k = 0; st == SPF_OK && k < n_chunks; ++k) {
+        const int64_t r0 = k * chunk, n = std::min(chunk, n_img - r0);
+        std::vector<int64_t> ov;
+        for (int64_t j = off[k]; j < off[k + 1]; ++j)
+          if (h_cnt[j] > CAP) ov.push_back(rows_l[j]);
+        if (ov.empty()) continue;
+        const int64_t no = (int64_t)ov.size();
+        int64_t hs[3] = {0, 0, 0};
+        std::vector<int32_t> o_i(no);
+        std::vector<float> o_d(no);
+        st = spf::check_cuda(cudaMemcpyAsync(d_rl, ov.data(), no * 8, cudaMemcpyHostToDevice, s),
+                             "spf_match_bf16_host");
+        if (st == SPF_OK)
+          st = spf_complete_open(cand_d + k * cslot, cand_i + k * cslot, tiles, bf16 + r0 * ld * 2,
+                                 f32 + r0 * n_pix, sq + r0, work + r0, n, d_rl, no, d_ref_bf16,
+                                 d_ref, d_ref_sq, n_ref, n_pix, ld, idx2, dist2, hs, sv);
+        if (st == SPF_OK)
+          st = spf::check_cuda(cudaMemcpyAsync(o_i.data(), idx2, no * 4, cudaMemcpyDeviceToHost, s),
+                               "spf_match_bf16_host");
+        if (st == SPF_OK)
+          st = spf::check_cuda(cudaMemcpyAsync(o_d.data(), dist2, no * 4, cudaMemcpyDeviceToHost, s),
+                               "spf_match_bf16_host");
+        if (st == SPF_OK) st = spf::check_cuda(cudaStreamSynchronize(s), "spf_match_bf16_host");
+        for (int64_t j = 0; st == SPF_OK && j < no; ++j) {
+          h_idx[r0 + ov[j]] = o_i[j];
+          dist_out[r0 + ov[j]] = o_d[j];
+        }
+        n_range += hs[0];
+        n_plain += hs[1];
       }
-      n_range += hs[0];
-      n_plain += hs[1];
     }
     if (h_stats) {
       h_stats[0] = n_bad;

@@ -249,33 +249,78 @@ __global__ void k_row_sqnorm(const float *__restrict__ x, int64_t n_rows, int64_
   }
 }
 
-// uint16 counts -> f32 (+ bf16) (+ squared norm, 4-norm); one warp per frame
+// uint16 counts -> f32 (+ bf16) (+ squared norm, 4-norm); one warp per frame.
+// The squared norm of integer counts is summed exactly in 64-bit integers
+// (at most 65535^2 * n_pix, far below 2^64) and rounded once to float, the
+// same value an exact FP64 sum gives; the 4-norm (FP64) is only computed when
+// asked for.  Rows move as 16-byte vectors (8 counts) when aligned.
 __global__ void k_ingest_u16(const uint16_t *__restrict__ in, int64_t n_img, int64_t n_pix,
                              float *__restrict__ f32, __nv_bfloat16 *__restrict__ bf, int64_t ld,
-                             float *__restrict__ sq, float *__restrict__ n4) {
+                             float *__restrict__ sq, float *__restrict__ n4, int vec) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const bool want4 = n4 != nullptr;
   for (int64_t r = warp; r < n_img; r += nwarps) {
     const uint16_t *p = in + r * n_pix;
-    double s2 = 0.0, s4 = 0.0;
-    for (int64_t k = lane; k < n_pix; k += 32) {
-      float v = (float)p[k];
-      f32[r * n_pix + k] = v;
-      if (bf) bf[r * ld + k] = __float2bfloat16_rn(v);
-      double v2 = (double)v * (double)v;
-      s2 += v2;
-      s4 = fma(v2, v2, s4);
+    unsigned long long s2 = 0;
+    double s4 = 0.0;
+    if (vec) {
+      const uint4 *pv = reinterpret_cast<const uint4 *>(p);
+      float4 *fv = reinterpret_cast<float4 *>(f32 + r * n_pix);
+      uint4 *bv = bf ? reinterpret_cast<uint4 *>(bf + r * ld) : nullptr;
+      const int64_t n8 = n_pix / 8;
+      for (int64_t k = lane; k < n8; k += 32) {
+        const uint4 raw = __ldg(pv + k);
+        const uint32_t w[4] = {raw.x, raw.y, raw.z, raw.w};
+        float v[8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const uint32_t lo = w[q] & 0xffffu, hi = w[q] >> 16;
+          v[2 * q] = (float)lo;
+          v[2 * q + 1] = (float)hi;
+          s2 += (unsigned long long)(lo * lo) + (unsigned long long)(hi * hi);
+          if (want4) {
+            const double a = (double)lo * (double)lo, b = (double)hi * (double)hi;
+            s4 = fma(a, a, s4);
+            s4 = fma(b, b, s4);
+          }
+        }
+        fv[2 * k] = make_float4(v[0], v[1], v[2], v[3]);
+        fv[2 * k + 1] = make_float4(v[4], v[5], v[6], v[7]);
+        if (bv) {
+          uint4 o;
+          uint32_t *ow = reinterpret_cast<uint32_t *>(&o);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+            ow[q] = *reinterpret_cast<uint32_t *>(&h);
+          }
+          bv[k] = o;
+        }
+      }
+    } else {
+      for (int64_t k = lane; k < n_pix; k += 32) {
+        const uint32_t c = p[k];
+        const float v = (float)c;
+        f32[r * n_pix + k] = v;
+        if (bf) bf[r * ld + k] = __float2bfloat16_rn(v);
+        s2 += (unsigned long long)(c * c);
+        if (want4) {
+          const double a = (double)c * (double)c;
+          s4 = fma(a, a, s4);
+        }
+      }
     }
     if (bf)
       for (int64_t k = n_pix + lane; k < ld; k += 32) bf[r * ld + k] = __float2bfloat16_rn(0.0f);
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
       s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-      s4 += __shfl_xor_sync(0xffffffffu, s4, o);
+      if (want4) s4 += __shfl_xor_sync(0xffffffffu, s4, o);
     }
     if (lane == 0) {
-      if (sq) sq[r] = (float)s2;
+      if (sq) sq[r] = __ull2float_rn(s2);
       if (n4) n4[r] = (float)sqrt(s4);
     }
   }
@@ -464,8 +509,11 @@ int spf_frames_ingest_u16(const uint16_t *d_counts, int64_t n_img, int64_t n_pix
   if (n_img == 0 || n_pix == 0) return SPF_OK;
   SPF_REQUIRE(d_counts && d_f32, "spf_frames_ingest_u16: NULL pointer");
   int blocks = grid_for(n_img * 32, 256, (int64_t)sm_count() * 32);
+  const int vec = n_pix % 8 == 0 && aligned(d_counts, 16) && aligned(d_f32, 16) &&
+                  (!d_bf16 || (aligned(d_bf16, 16) && ld % 8 == 0));
   k_ingest_u16<<<blocks, 256, 0, as_stream(stream)>>>(
-      d_counts, n_img, n_pix, d_f32, reinterpret_cast<__nv_bfloat16 *>(d_bf16), ld, d_sq, d_n4);
+      d_counts, n_img, n_pix, d_f32, reinterpret_cast<__nv_bfloat16 *>(d_bf16), ld, d_sq, d_n4,
+      vec);
   return check_launch("spf_frames_ingest_u16");
 }
 

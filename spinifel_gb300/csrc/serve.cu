@@ -239,7 +239,7 @@ int Server::launch(Slot &s) {
     row += r->n;
   }
   const int64_t n = s.n;
-  SPF_TRY(spf_frames_ingest_u16(s.u16, n, n_pix, s.f32, s.bf16, ld, s.sq, s.n4, sv));
+  SPF_TRY(spf_frames_ingest_u16(s.u16, n, n_pix, s.f32, s.bf16, ld, s.sq, nullptr, sv));
   if (path == 0) {
     SPF_TRY(spf_dist_topk_bf16(s.bf16, n, ref_bf16, n_ref, n_pix, ld, ref_sq, s.cand_d, s.cand_i,
                                sv));

@@ -189,7 +189,7 @@ class OrientationServer:
                 row += r.n
             n = slot.n
             fs = slot.view(n)
-            matching.ingest_u16(slot.u16[:n], fs.f32, fs.bf16, fs.sq, fs.n4)
+            matching.ingest_u16(slot.u16[:n], fs.f32, fs.bf16, fs.sq, None)
             sh = _lib.stream_handle(slot.stream)
             if self.path == "bf16":
                 _lib.call("spf_dist_topk_bf16", _lib.ptr(fs.bf16), n, _lib.ptr(self.refs.bf16),

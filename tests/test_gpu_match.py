@@ -172,3 +172,33 @@ def test_gather_rows_matches_indexing(dev, dtype, shape):
     rows = torch.tensor([3, 0, 49 % shape[0], 3, shape[0] - 1], dtype=torch.int64, device=dev)
     out = matching.gather_rows(src, rows)
     assert torch.equal(out, src[rows])
+
+
+@pytest.mark.parametrize("n_pix,ld", [(4096, 4096), (1003, 1008)])
+def test_frame_ingest_exact(lib, n_pix, ld):
+    """uint16 counts -> FP32, bf16 (zero-padded to ld), squared norm and
+    4-norm: FP32 and bf16 exactly as converted by torch, the squared norm
+    the exactly rounded integer sum, on the vector (16-byte) and the scalar
+    path, counts up to 65535."""
+    from spinifel_gb300 import matching
+
+    rng = np.random.default_rng(33)
+    c = rng.integers(0, 65536, (37, n_pix)).astype(np.uint16)
+    c[0, :] = 65535
+    dev = torch.device("cuda", 0)
+    t = torch.as_tensor(c.view(np.int16), device=dev)
+    f32 = torch.empty(37, n_pix, device=dev)
+    bf = torch.empty(37, ld, dtype=torch.bfloat16, device=dev)
+    sq = torch.empty(37, device=dev)
+    n4 = torch.empty(37, device=dev)
+    matching.ingest_u16(t, f32, bf, sq, n4)
+    torch.cuda.synchronize()
+    ref = c.astype(np.float32)
+    np.testing.assert_array_equal(f32.cpu().numpy(), ref)
+    rb = torch.zeros(37, ld, dtype=torch.bfloat16)
+    rb[:, :n_pix] = torch.as_tensor(ref).to(torch.bfloat16)
+    assert torch.equal(bf.cpu(), rb)
+    exact = (c.astype(np.int64) ** 2).sum(axis=1)
+    np.testing.assert_array_equal(sq.cpu().numpy(), exact.astype(np.float32))
+    s4 = ((c.astype(np.float64) ** 2) ** 2).sum(axis=1)
+    np.testing.assert_allclose(n4.cpu().numpy(), np.sqrt(s4).astype(np.float32), rtol=1e-6)
