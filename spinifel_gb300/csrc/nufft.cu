@@ -395,6 +395,13 @@ __device__ __forceinline__ void box_flush(const float *box, float *__restrict__ 
 // large for shared memory (a patch seen edge-on) reads the grid directly.
 // The arithmetic per point is that of k_slice_t2, so the values are identical.
 constexpr int SLICE_PATCH = 16;
+
+// Pixel of thread t within its 16 x 16 patch: warp w takes the 4 x 8 block at
+// rows 4 (w / 2), columns 8 (w % 2), so a warp's 32 pixels are compact on the
+// detector, their footprints overlap more and their shared-memory reads hit
+// fewer distinct cells.
+__device__ __forceinline__ int patch_dx(int t) { return ((t >> 5) >> 1) * 4 + ((t & 31) >> 3); }
+__device__ __forceinline__ int patch_dy(int t) { return ((t >> 5) & 1) * 8 + (t & 7); }
 constexpr int SLICE_SMEM_FLOATS = 11264;  // 44 KB
 
 template <int W>
@@ -411,8 +418,8 @@ __global__ void __launch_bounds__(256)
   const int pid = blockIdx.y;
   const int panel = pid / (patches_x * patches_y);
   const int rem = pid % (patches_x * patches_y);
-  const int px = (rem / patches_y) * SLICE_PATCH + (int)(threadIdx.x / SLICE_PATCH);
-  const int py = (rem % patches_y) * SLICE_PATCH + (int)(threadIdx.x % SLICE_PATCH);
+  const int px = (rem / patches_y) * SLICE_PATCH + patch_dx((int)threadIdx.x);
+  const int py = (rem % patches_y) * SLICE_PATCH + patch_dy((int)threadIdx.x);
   const bool valid = px < nx && py < ny && panel < n_panels;
   const int64_t n_pix = (int64_t)n_panels * nx * ny;
   const int64_t p = ((int64_t)panel * nx + (valid ? px : 0)) * ny + (valid ? py : 0);
@@ -508,8 +515,8 @@ __device__ __forceinline__ PatchPoint patch_point(const GridGeom &g, const float
   const int pid = blockIdx.y;
   const int panel = pid / (patches_x * patches_y);
   const int rem = pid % (patches_x * patches_y);
-  const int px = (rem / patches_y) * SLICE_PATCH + (int)(threadIdx.x / SLICE_PATCH);
-  const int py = (rem % patches_y) * SLICE_PATCH + (int)(threadIdx.x % SLICE_PATCH);
+  const int px = (rem / patches_y) * SLICE_PATCH + patch_dx((int)threadIdx.x);
+  const int py = (rem % patches_y) * SLICE_PATCH + patch_dy((int)threadIdx.x);
   PatchPoint pt;
   pt.valid = px < nx && py < ny && panel < n_panels;
   const int64_t n_pix = (int64_t)n_panels * nx * ny;
