@@ -792,42 +792,113 @@ __global__ void k_bin_scatter(const int32_t *__restrict__ bin_of, int64_t n,
   }
 }
 
-// Fused type 2 -> weight -> type 1 over bin-sorted points.  A CTA takes one
-// work item (up to 2,048 points of one 8^3-cell bin), stages the bin's
-// footprint box of the type-2 grid in shared memory, and accumulates the
-// spread into a second box that is added to the type-1 accumulator at the
-// end.  A warp serves one point at a time: its 32 lanes are 4 footprint rows
-// x 8 cells along the fastest axis, so one instruction reads or updates 4
-// rows of one point.  The row stride (24 floats) and the plane stride
-// (== W * 24 mod 32) put 4 consecutive footprint rows on 4 disjoint groups of
-// 8 banks, so those accesses have no bank conflicts and no two lanes touch
-// the same cell.  Each point's coordinates are computed once by one lane and
-// broadcast; lanes 0-7 / 8-15 / 16-23 evaluate the kernel on axes 1 / 2 / 3.
-constexpr int SORTED_ROW_STRIDE = 24;
-
-constexpr int sorted_plane_stride(int d, int w) {
-  int x = d * SORTED_ROW_STRIDE;
-  while (x % 32 != (w * SORTED_ROW_STRIDE) % 32) ++x;
-  return x;
+// Padded first footprint index of a point along one axis: the index
+// arithmetic of axis_setup without the weights (same explicitly rounded
+// operations, so the cell agrees with the one the kernels use).
+template <int W>
+__device__ __forceinline__ int axis_cell(float x, float s, int n, int off) {
+  float fn = (float)n;
+  float t = __fmul_rn(x, s);
+  t = __fsub_rn(t, __fmul_rn(fn, floorf(__fadd_rn(__fdiv_rn(t, fn), 0.5f))));
+  return (int)ceilf(__fsub_rn(t, 0.5f * W)) + off;
 }
 
+// Orders the points of each work item by their first footprint cell within
+// the bin (a counting sort over the 8^3 cells in shared memory), so that
+// points sharing a footprint are consecutive.  The point set of every item is
+// unchanged; only its order within the item is.
 template <int W>
 __global__ void __launch_bounds__(256)
+    k_item_cellsort(GridGeom g, BinDims bd, const int4 *__restrict__ items,
+                    int32_t *__restrict__ sorted, const float *__restrict__ quats,
+                    const float *__restrict__ ppr, int64_t n_pix, float s1, float s2, float s3) {
+  constexpr int NC = BIN * BIN * BIN;
+  __shared__ int32_t idx[BIN_CHUNK];
+  __shared__ int16_t key[BIN_CHUNK];
+  __shared__ int32_t cnt[NC];
+  const int4 it = items[blockIdx.x];
+  const int b = it.x;
+  const int bi = b / (bd.nb[1] * bd.nb[2]), bj = (b / bd.nb[2]) % bd.nb[1], bk = b % bd.nb[2];
+  const int i0b = bi * BIN, j0b = bj * BIN, k0b = bk * BIN;
+  for (int t = threadIdx.x; t < NC; t += blockDim.x) cnt[t] = 0;
+  __syncthreads();
+  for (int q = threadIdx.x; q < it.z; q += blockDim.x) {
+    const int32_t pi = sorted[it.y + q];
+    const int64_t o = pi / n_pix, p = pi % n_pix;
+    float h, k, l;
+    rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
+    const int ci = min(max(axis_cell<W>(h, s1, g.n1, g.off1) - i0b, 0), BIN - 1);
+    const int cj = min(max(axis_cell<W>(k, s2, g.n2, g.off2) - j0b, 0), BIN - 1);
+    const int ck = min(max(axis_cell<W>(l, s3, g.n3, g.off3) - k0b, 0), BIN - 1);
+    const int kk = (ci * BIN + cj) * BIN + ck;
+    idx[q] = pi;
+    key[q] = (int16_t)kk;
+    atomicAdd(&cnt[kk], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {  // exclusive scan of the NC counters by one warp
+    constexpr int PER = NC / 32;
+    const int lane = threadIdx.x;
+    int local = 0;
+#pragma unroll
+    for (int u = 0; u < PER; ++u) local += cnt[lane * PER + u];
+    int incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    int run = incl - local;
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int c = cnt[lane * PER + u];
+      cnt[lane * PER + u] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < it.z; q += blockDim.x) {
+    const int pos = atomicAdd(&cnt[key[q]], 1);
+    sorted[it.y + pos] = idx[q];
+  }
+}
+
+// Fused type 2 -> weight -> type 1 over bin-sorted points.  A CTA takes one
+// work item (up to 2,048 points of one 8^3-cell bin, ordered by footprint
+// cell), stages the bin's footprint box of the type-2 grid in shared memory,
+// and accumulates the spread into a second box that is added to the type-1
+// accumulator at the end.  A warp serves one point at a time.  Lane
+// (g, c) = (lane / 8, lane % 8) owns the two footprint rows b = g and b = g + 4
+// (second axis) at offset c along the fastest axis over the W planes of the
+// slowest axis.  Consecutive points with the same footprint cell touch the
+// same 2W cells per lane, so a lane keeps their box values and their pending
+// spread in registers for the whole run: it reads the box, and adds to the
+// spread box (shared atomics), only when the cell changes.  The separable
+// weights are shuffled in once per point (w1 for the plane, w2 * w3 for the
+// lane's two rows).  With a row stride of 24 floats the 32 lanes of either
+// row set fall on 32 distinct banks.  Each point's coordinates are computed
+// once by one lane and broadcast; lanes 0-7 / 8-15 / 16-23 evaluate the
+// kernel on axes 1 / 2 / 3.
+constexpr int SORTED_ROW_STRIDE = 24;
+constexpr int SORTED_THREADS = 256;
+
+template <int W>
+__global__ void __launch_bounds__(SORTED_THREADS, 5)
     k_interp_spread_sorted(const float *__restrict__ re_pad, float *__restrict__ acc_pad,
                            GridGeom g, BinDims bd, const int4 *__restrict__ items,
                            const int32_t *__restrict__ sorted, const float *__restrict__ quats,
                            const float *__restrict__ ppr, int64_t n_pix, float s1, float s2,
                            float s3, const float *__restrict__ weights,
                            unsigned int *__restrict__ err) {
-  static_assert(W <= 8, "eight lanes per footprint row");
+  static_assert(W <= 8, "eight lanes per footprint row, two rows per lane");
   constexpr int D = BIN + W - 1;
   constexpr int SR = SORTED_ROW_STRIDE;
-  constexpr int SP = sorted_plane_stride(D, W);
-  constexpr int ROWS = W * W;
-  constexpr int STEPS = (ROWS + 3) / 4;
+  constexpr int SP = D * SR;
   static_assert(D <= SR, "row stride holds a footprint row");
   __shared__ float tbox[D * SP];
   __shared__ float abox[D * SP];
+  __shared__ float4 pt_tw[SORTED_THREADS];  // per warp: 32 prepared points
+  __shared__ int pt_key[SORTED_THREADS];
   const int4 it = items[blockIdx.x];
   const int b = it.x;
   const int bi = b / (bd.nb[1] * bd.nb[2]), bj = (b / bd.nb[2]) % bd.nb[1], bk = b % bd.nb[2];
@@ -839,78 +910,101 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const int grp = lane >> 3;  // footprint row within a step; kernel axis for the weights
+  const int grp = lane >> 3;  // row set of the lane; kernel axis for the weights
   const int c = lane & 7;     // offset along the fastest axis
+  const int r0 = grp, r1 = grp + 4;
+  const bool ok0 = c < W && r0 < W, ok1 = c < W && r1 < W;
+  const int lane_off0 = r0 * SR + c, lane_off1 = r1 * SR + c;
   const int warp = threadIdx.x >> 5;
-  const int nwarps = blockDim.x >> 5;
+  const int nwarps = SORTED_THREADS / 32;
+  // the run: footprint cell (packed li, lj, lk) held in registers, its box
+  // values and its spread not yet added
+  int cur = -1, cur_base = 0;
+  float p0[W], p1[W];
+  auto flush = [&]() {
+#pragma unroll
+    for (int a = 0; a < W; ++a) {
+      if (ok0) atomicAdd(&abox[cur_base + lane_off0 + a * SP], p0[a]);
+      if (ok1) atomicAdd(&abox[cur_base + lane_off1 + a * SP], p1[a]);
+    }
+  };
   const float fn1 = (float)g.n1, fn2 = (float)g.n2, fn3 = (float)g.n3;
+  float4 *my_tw = pt_tw + warp * 32;
+  int *my_key = pt_key + warp * 32;
   for (int q0 = warp * 32; q0 < it.z; q0 += nwarps * 32) {
     const int cnt = min(32, it.z - q0);
     // lane L prepares point q0 + L (same arithmetic as axis_setup / the bin sort)
-    int32_t my_pi = 0;
-    float t1 = 0.f, t2 = 0.f, t3 = 0.f, l1 = 0.f, l2 = 0.f, l3 = 0.f;
+    // into the warp's slots: (t1, t2, t3, weight) and the packed first cell
+    // in the box, or -1 for a point outside the box
     if (lane < cnt) {
-      my_pi = sorted[it.y + q0 + lane];
-      const int64_t o = my_pi / n_pix, p = my_pi % n_pix;
+      const int32_t pi = sorted[it.y + q0 + lane];
+      const float pw = weights ? weights[pi] : 1.0f;
+      const int64_t o = pi / n_pix, p = pi % n_pix;
       float h, k, l;
       rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
-      t1 = __fmul_rn(h, s1);
-      t2 = __fmul_rn(k, s2);
-      t3 = __fmul_rn(l, s3);
+      float t1 = __fmul_rn(h, s1), t2 = __fmul_rn(k, s2), t3 = __fmul_rn(l, s3);
       t1 = __fsub_rn(t1, __fmul_rn(fn1, floorf(__fadd_rn(__fdiv_rn(t1, fn1), 0.5f))));
       t2 = __fsub_rn(t2, __fmul_rn(fn2, floorf(__fadd_rn(__fdiv_rn(t2, fn2), 0.5f))));
       t3 = __fsub_rn(t3, __fmul_rn(fn3, floorf(__fadd_rn(__fdiv_rn(t3, fn3), 0.5f))));
-      l1 = ceilf(__fsub_rn(t1, 0.5f * W));
-      l2 = ceilf(__fsub_rn(t2, 0.5f * W));
-      l3 = ceilf(__fsub_rn(t3, 0.5f * W));
-    }
-    for (int j = 0; j < cnt; ++j) {
-      const int32_t pi = __shfl_sync(FULL, my_pi, j);
-      const float T1 = __shfl_sync(FULL, t1, j), T2 = __shfl_sync(FULL, t2, j),
-                  T3 = __shfl_sync(FULL, t3, j);
-      const float L1 = __shfl_sync(FULL, l1, j), L2 = __shfl_sync(FULL, l2, j),
-                  L3 = __shfl_sync(FULL, l3, j);
-      const int li = (int)L1 + g.off1 - i0b, lj = (int)L2 + g.off2 - j0b,
-                lk = (int)L3 + g.off3 - k0b;
+      const int li = (int)ceilf(__fsub_rn(t1, 0.5f * W)) + g.off1 - i0b;
+      const int lj = (int)ceilf(__fsub_rn(t2, 0.5f * W)) + g.off2 - j0b;
+      const int lk = (int)ceilf(__fsub_rn(t3, 0.5f * W)) + g.off3 - k0b;
       const bool inside =
           li >= 0 && lj >= 0 && lk >= 0 && li + W <= di && lj + W <= dj && lk + W <= dk;
-      if (!inside) {  // cannot happen for a correctly binned point; never read outside
-        if (lane == 0 && err) atomicExch(err, (unsigned int)(-SPF_ERR_CUDA));
-        continue;
-      }
-      const float tt = grp == 0 ? T1 : (grp == 1 ? T2 : T3);
-      const float ll = grp == 0 ? L1 : (grp == 1 ? L2 : L3);
-      const float kw = (c < W && grp < 3) ? es_eval((ll + (float)c - tt) * g.inv_half_w, g.beta)
-                                          : 0.0f;
-      const float w3c = __shfl_sync(FULL, kw, 16 + c);  // 0 for c >= W
-      // interpolate: step t covers footprint rows 4t .. 4t+3 (row r = a*W + b)
-      float w12[STEPS];
-      float part = 0.0f;
+      if (!inside && err)  // cannot happen for a correctly binned point; never read outside
+        atomicExch(err, (unsigned int)(-SPF_ERR_CUDA));
+      my_tw[lane] = make_float4(t1, t2, t3, pw);
+      my_key[lane] = inside ? (li << 10) | (lj << 5) | lk : -1;  // li, lj, lk < 32
+    }
+    __syncwarp();
+    for (int j = 0; j < cnt; ++j) {
+      const int key = my_key[j];
+      if (key < 0) continue;
+      const float4 tw = my_tw[j];
+      const int li = key >> 10, lj = (key >> 5) & 31, lk = key & 31;
+      // first footprint index along the lane's kernel axis, as a float (exact)
+      const int la = grp == 0 ? li + i0b - g.off1 : (grp == 1 ? lj + j0b - g.off2 : lk + k0b - g.off3);
+      const float tt = grp == 0 ? tw.x : (grp == 1 ? tw.y : tw.z);
+      const float kw = (c < W && grp < 3)
+                           ? es_eval(((float)la + (float)c - tt) * g.inv_half_w, g.beta)
+                           : 0.0f;
+      const float w3c = __shfl_sync(FULL, kw, 16 + c);
+      const float u0 = __shfl_sync(FULL, kw, 8 + r0) * w3c;
+      const float u1 = __shfl_sync(FULL, kw, 8 + (r1 & 7)) * w3c;
+      float w1[W];
 #pragma unroll
-      for (int t = 0; t < STEPS; ++t) {
-        const int r = 4 * t + grp;
-        const int a = r / W, bb = r - a * W;
-        w12[t] = __shfl_sync(FULL, kw, a & 7) * __shfl_sync(FULL, kw, 8 + bb);
-        if (r < ROWS && c < W)
-          part = fmaf(w12[t], tbox[(li + a) * SP + (lj + bb) * SR + lk + c], part);
-      }
-      part *= w3c;
+      for (int a = 0; a < W; ++a) w1[a] = __shfl_sync(FULL, kw, a);
+      if (key != cur) {  // warp-uniform
+        if (cur >= 0) flush();
+        cur = key;
+        cur_base = li * SP + lj * SR + lk;
 #pragma unroll
-      for (int m = 16; m >= 1; m >>= 1) part += __shfl_xor_sync(FULL, part, m);
-      float v = part;
-      if (weights) v *= weights[pi];
-      if (v != 0.0f) {
-        const float wv = w3c * v;
-#pragma unroll
-        for (int t = 0; t < STEPS; ++t) {
-          const int r = 4 * t + grp;
-          const int a = r / W, bb = r - a * W;
-          if (r < ROWS && c < W) atomicAdd(&abox[(li + a) * SP + (lj + bb) * SR + lk + c],
-                                           w12[t] * wv);
+        for (int a = 0; a < W; ++a) {
+          p0[a] = 0.0f;
+          p1[a] = 0.0f;
         }
       }
+      // interpolate: plane a, the lane's two rows
+      float part = 0.0f;
+#pragma unroll
+      for (int a = 0; a < W; ++a) {
+        const float xa = ok0 ? tbox[cur_base + lane_off0 + a * SP] : 0.0f;
+        const float xb = ok1 ? tbox[cur_base + lane_off1 + a * SP] : 0.0f;
+        part = fmaf(w1[a], fmaf(u1, xb, u0 * xa), part);
+      }
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) part += __shfl_xor_sync(FULL, part, m);
+      const float v = part * tw.w;  // weight 1 without weights
+      const float v0 = u0 * v, v1 = u1 * v;
+#pragma unroll
+      for (int a = 0; a < W; ++a) {
+        p0[a] = fmaf(w1[a], v0, p0[a]);
+        p1[a] = fmaf(w1[a], v1, p1[a]);
+      }
     }
+    __syncwarp();  // the slots are rewritten by the next chunk
   }
+  if (cur >= 0) flush();
   __syncthreads();
   box_flush(abox, acc_pad, g, shape);
 }
@@ -1360,6 +1454,11 @@ int spf_nufft_sort_orient(spf_nufft_plan P, const float *d_quats, int64_t n_orie
                                   cudaMemcpyHostToDevice), "sort_orient"));
   P->n_items = (int64_t)h_items.size();
   P->n_sorted = n;
+  if (P->n_items > 0) {  // points sharing a footprint cell become consecutive
+    SPF_W_DISPATCH(P->w, (k_item_cellsort<W><<<(unsigned)P->n_items, 256, 0, s>>>(
+                             g, bd, P->items, P->sorted, d_quats, d_ppr, n_pix, s1, s2, s3)));
+    SPF_TRY(check_launch("k_item_cellsort"));
+  }
   P->s_quats = d_quats;
   P->s_ppr = d_ppr;
   P->s_n_orient = n_orient;
@@ -1381,7 +1480,7 @@ int spf_nufft_interp_spread_sorted(spf_nufft_plan P, const float *d_weights, voi
   float s2 = (float)(P->s_scale * P->n[1] / (2.0 * M_PI));
   float s3 = (float)(P->s_scale * P->n[2] / (2.0 * M_PI));
   SPF_REQUIRE(P->n_items < (1LL << 31), "spf_nufft_interp_spread_sorted: too many items");
-  SPF_W_DISPATCH(P->w, (k_interp_spread_sorted<W><<<(unsigned)P->n_items, 256, 0, s>>>(
+  SPF_W_DISPATCH(P->w, (k_interp_spread_sorted<W><<<(unsigned)P->n_items, SORTED_THREADS, 0, s>>>(
                            P->re_pad, P->acc_pad, g, bd, P->items, P->sorted, P->s_quats,
                            P->s_ppr, P->s_n_pix, s1, s2, s3, d_weights, device_error_word())));
   return check_launch("k_interp_spread_sorted");
