@@ -882,6 +882,30 @@ __global__ void __launch_bounds__(256)
 constexpr int SORTED_ROW_STRIDE = 24;
 constexpr int SORTED_THREADS = 256;
 
+// d = a * b + c on two FP32 lanes in one instruction (fma.rn.f32x2)
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+
+// ES kernel exp(beta (sqrt(1 - z^2) - 1)) from the hardware approximations
+// (sqrt.approx, ex2.approx: relative errors near 2^-22, far below the
+// kernel's own approximation error at any eps >= 1e-7); beta_log2e = beta log2(e)
+__device__ __forceinline__ float es_eval_approx(float z, float beta_log2e) {
+  const float s = fmaxf(fmaf(-z, z, 1.0f), 0.0f);
+  float r, e;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
+  const float x = beta_log2e * (r - 1.0f);
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(x));
+  return e;
+}
+
+
 template <int W>
 __global__ void __launch_bounds__(SORTED_THREADS, 5)
     k_interp_spread_sorted(const float *__restrict__ re_pad, float *__restrict__ acc_pad,
@@ -920,14 +944,20 @@ __global__ void __launch_bounds__(SORTED_THREADS, 5)
   // the run: footprint cell (packed li, lj, lk) held in registers, its box
   // values and its spread not yet added
   int cur = -1, cur_base = 0;
-  float p0[W], p1[W];
+  float2 pend[W];  // spread not yet added at the lane's two cells of plane a
   auto flush = [&]() {
 #pragma unroll
     for (int a = 0; a < W; ++a) {
-      if (ok0) atomicAdd(&abox[cur_base + lane_off0 + a * SP], p0[a]);
-      if (ok1) atomicAdd(&abox[cur_base + lane_off1 + a * SP], p1[a]);
+      if (ok0) atomicAdd(&abox[cur_base + lane_off0 + a * SP], pend[a].x);
+      if (ok1) atomicAdd(&abox[cur_base + lane_off1 + a * SP], pend[a].y);
     }
   };
+  // the lane's kernel axis: position of its first footprint index in the
+  // packed cell key, and the offset from box to grid index
+  const int ax = grp < 3 ? grp : 2;
+  const int ax_shift = 10 - 5 * ax;
+  const int ax_base = ax == 0 ? i0b - g.off1 : (ax == 1 ? j0b - g.off2 : k0b - g.off3);
+  const float beta_log2e = g.beta * 1.4426950408889634f;
   const float fn1 = (float)g.n1, fn2 = (float)g.n2, fn3 = (float)g.n3;
   float4 *my_tw = pt_tw + warp * 32;
   int *my_key = pt_key + warp * 32;
@@ -957,16 +987,15 @@ __global__ void __launch_bounds__(SORTED_THREADS, 5)
       my_key[lane] = inside ? (li << 10) | (lj << 5) | lk : -1;  // li, lj, lk < 32
     }
     __syncwarp();
+    const float *my_twf = reinterpret_cast<const float *>(my_tw);
     for (int j = 0; j < cnt; ++j) {
       const int key = my_key[j];
       if (key < 0) continue;
-      const float4 tw = my_tw[j];
-      const int li = key >> 10, lj = (key >> 5) & 31, lk = key & 31;
       // first footprint index along the lane's kernel axis, as a float (exact)
-      const int la = grp == 0 ? li + i0b - g.off1 : (grp == 1 ? lj + j0b - g.off2 : lk + k0b - g.off3);
-      const float tt = grp == 0 ? tw.x : (grp == 1 ? tw.y : tw.z);
+      const int la = ((key >> ax_shift) & 31) + ax_base;
+      const float tt = my_twf[4 * j + ax];
       const float kw = (c < W && grp < 3)
-                           ? es_eval(((float)la + (float)c - tt) * g.inv_half_w, g.beta)
+                           ? es_eval_approx(((float)la + (float)c - tt) * g.inv_half_w, beta_log2e)
                            : 0.0f;
       const float w3c = __shfl_sync(FULL, kw, 16 + c);
       const float u0 = __shfl_sync(FULL, kw, 8 + r0) * w3c;
@@ -977,30 +1006,25 @@ __global__ void __launch_bounds__(SORTED_THREADS, 5)
       if (key != cur) {  // warp-uniform
         if (cur >= 0) flush();
         cur = key;
-        cur_base = li * SP + lj * SR + lk;
+        cur_base = (key >> 10) * SP + ((key >> 5) & 31) * SR + (key & 31);
 #pragma unroll
-        for (int a = 0; a < W; ++a) {
-          p0[a] = 0.0f;
-          p1[a] = 0.0f;
-        }
+        for (int a = 0; a < W; ++a) pend[a] = make_float2(0.0f, 0.0f);
       }
-      // interpolate: plane a, the lane's two rows
-      float part = 0.0f;
+      // interpolate: plane a, the lane's two rows (one packed FMA per plane)
+      float2 sx = make_float2(0.0f, 0.0f);
 #pragma unroll
       for (int a = 0; a < W; ++a) {
-        const float xa = ok0 ? tbox[cur_base + lane_off0 + a * SP] : 0.0f;
-        const float xb = ok1 ? tbox[cur_base + lane_off1 + a * SP] : 0.0f;
-        part = fmaf(w1[a], fmaf(u1, xb, u0 * xa), part);
+        const float2 xa = make_float2(ok0 ? tbox[cur_base + lane_off0 + a * SP] : 0.0f,
+                                      ok1 ? tbox[cur_base + lane_off1 + a * SP] : 0.0f);
+        sx = ffma2(make_float2(w1[a], w1[a]), xa, sx);
       }
+      float part = fmaf(u1, sx.y, u0 * sx.x);
 #pragma unroll
       for (int m = 16; m >= 1; m >>= 1) part += __shfl_xor_sync(FULL, part, m);
-      const float v = part * tw.w;  // weight 1 without weights
-      const float v0 = u0 * v, v1 = u1 * v;
+      const float v = part * my_twf[4 * j + 3];  // weight 1 without weights
+      const float2 vv = make_float2(u0 * v, u1 * v);
 #pragma unroll
-      for (int a = 0; a < W; ++a) {
-        p0[a] = fmaf(w1[a], v0, p0[a]);
-        p1[a] = fmaf(w1[a], v1, p1[a]);
-      }
+      for (int a = 0; a < W; ++a) pend[a] = ffma2(make_float2(w1[a], w1[a]), vv, pend[a]);
     }
     __syncwarp();  // the slots are rewritten by the next chunk
   }
