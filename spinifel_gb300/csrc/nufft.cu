@@ -907,7 +907,7 @@ __device__ __forceinline__ float es_eval_approx(float z, float beta_log2e) {
 
 
 template <int W>
-__global__ void __launch_bounds__(SORTED_THREADS, 5)
+__global__ void __launch_bounds__(SORTED_THREADS, 4)
     k_interp_spread_sorted(const float *__restrict__ re_pad, float *__restrict__ acc_pad,
                            GridGeom g, BinDims bd, const int4 *__restrict__ items,
                            const int32_t *__restrict__ sorted, const float *__restrict__ quats,
@@ -945,6 +945,7 @@ __global__ void __launch_bounds__(SORTED_THREADS, 5)
   // values and its spread not yet added
   int cur = -1, cur_base = 0;
   float2 pend[W];  // spread not yet added at the lane's two cells of plane a
+  float2 xc[W];    // box values at the lane's two cells of plane a
   auto flush = [&]() {
 #pragma unroll
     for (int a = 0; a < W; ++a) {
@@ -1008,15 +1009,17 @@ __global__ void __launch_bounds__(SORTED_THREADS, 5)
         cur = key;
         cur_base = (key >> 10) * SP + ((key >> 5) & 31) * SR + (key & 31);
 #pragma unroll
-        for (int a = 0; a < W; ++a) pend[a] = make_float2(0.0f, 0.0f);
+        for (int a = 0; a < W; ++a) {
+          pend[a] = make_float2(0.0f, 0.0f);
+          xc[a] = make_float2(ok0 ? tbox[cur_base + lane_off0 + a * SP] : 0.0f,
+                              ok1 ? tbox[cur_base + lane_off1 + a * SP] : 0.0f);
+        }
       }
       // interpolate: plane a, the lane's two rows (one packed FMA per plane)
       float2 sx = make_float2(0.0f, 0.0f);
 #pragma unroll
       for (int a = 0; a < W; ++a) {
-        const float2 xa = make_float2(ok0 ? tbox[cur_base + lane_off0 + a * SP] : 0.0f,
-                                      ok1 ? tbox[cur_base + lane_off1 + a * SP] : 0.0f);
-        sx = ffma2(make_float2(w1[a], w1[a]), xa, sx);
+        sx = ffma2(make_float2(w1[a], w1[a]), xc[a], sx);
       }
       float part = fmaf(u1, sx.y, u0 * sx.x);
 #pragma unroll
