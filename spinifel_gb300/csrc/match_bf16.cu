@@ -577,10 +577,13 @@ __global__ void __launch_bounds__(RR_THREADS)
 // for p = 0 .. n_pix-1 in order, then (x2 + s2) - 2 acc, so the re-ranked
 // values are bit-identical to the plain path's.  A CTA takes 4 frames (32
 // (frame, candidate) chains, one per lane of warp 0); all its warps stream the
-// 4 frame rows and 32 candidate rows through shared memory in coalesced
-// 256-pixel chunks (double-buffered, rows padded to 257 floats so the 32
-// chains read 32 different banks).  Lane 0 of each group of 8 keeps the
-// lexicographic minimum and evaluates the certificate.
+// 4 frame rows and 32 candidate rows through shared memory in 64-pixel
+// chunks, RXE_STAGES - 1 chunks in flight (cp.async groups issued by warps
+// 1-3 while warp 0 runs the chains), rows padded to 68 floats so that the
+// chains' 16-byte reads of 8 consecutive rows fall on distinct banks.  Small
+// stages keep 29 KB of shared memory per CTA, so many CTAs (and their loads)
+// are resident per SM.  Lane 0 of each group of 8 keeps the lexicographic
+// minimum and evaluates the certificate.
 // The certificate's band: a bound on |approximate - exact| distance for any
 // reference (CERT_SIGMAS sigma of the bf16 rounding, per-pixel bound, plus
 // the FP32 accumulation error of both paths).
@@ -604,6 +607,9 @@ constexpr int RX_ROWS = RX_FRAMES * (TOPK + 1);  // 4 frame rows + 32 candidate 
 constexpr int RX_CHUNK = 256;
 constexpr int RX_STRIDE = RX_CHUNK + 4;          // 16-byte aligned rows, 4-way banks
 constexpr int RX_THREADS = 128;
+constexpr int RXE_CHUNK = 64;                    // k_rerank_exact: pixels per stage
+constexpr int RXE_STRIDE = RXE_CHUNK + 4;
+constexpr int RXE_STAGES = 3;
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem)
@@ -618,7 +624,7 @@ __global__ void __launch_bounds__(RX_THREADS)
                    float *__restrict__ work, int32_t *__restrict__ out_idx,
                    float *__restrict__ out_dist, int32_t *__restrict__ uncertified,
                    int32_t *__restrict__ out_top) {
-  extern __shared__ __align__(16) float rx[];  // [2][RX_ROWS][RX_STRIDE]
+  extern __shared__ __align__(16) float rx[];  // [RXE_STAGES][RX_ROWS][RXE_STRIDE]
   __shared__ const float *rows[RX_ROWS];
   const int tid = threadIdx.x;
   const int64_t f0 = (int64_t)blockIdx.x * RX_FRAMES;
@@ -641,21 +647,25 @@ __global__ void __launch_bounds__(RX_THREADS)
     rows[tid] = ptr;
   }
   __syncthreads();
-  const int64_t nchunks = (n_pix + RX_CHUNK - 1) / RX_CHUNK;
+  const int64_t nchunks = (n_pix + RXE_CHUNK - 1) / RXE_CHUNK;
   const bool vec = (n_pix % 4) == 0 && aligned(img, 16) && aligned(ref, 16);
   // asynchronous 16-byte copies of one chunk of every row (ragged ends by
   // plain loads)
+  // (a chunk past the end issues nothing; its group is still committed so
+  // that the group count stays one per chunk)
   auto stage = [&](int buf, int64_t chunk) {
-    float *dst = rx + (size_t)buf * RX_ROWS * RX_STRIDE;
-    const int64_t base = chunk * RX_CHUNK;
-    for (int e = tid; e < RX_ROWS * (RX_CHUNK / 4); e += RX_THREADS) {
-      int r = e / (RX_CHUNK / 4), q4 = (e % (RX_CHUNK / 4)) * 4;
+    float *dst = rx + (size_t)buf * RX_ROWS * RXE_STRIDE;
+    const int64_t base = chunk * RXE_CHUNK;
+    if (tid < 32) return;  // warp 0 runs the chains; warps 1.. stage
+    for (int e = tid - 32; chunk < nchunks && e < RX_ROWS * (RXE_CHUNK / 4);
+         e += RX_THREADS - 32) {
+      int r = e / (RXE_CHUNK / 4), q4 = (e % (RXE_CHUNK / 4)) * 4;
       const float *src = rows[r];
       // a row without source (a skipped candidate, a list slot past the end,
       // a frame past the last) is not staged: its chain's result is discarded
       if (!src) continue;
       int64_t p = base + q4;
-      float *d = dst + r * RX_STRIDE + q4;
+      float *d = dst + r * RXE_STRIDE + q4;
       if (vec && p + 3 < n_pix) {
         cp_async16(d, src + p);
       } else {
@@ -670,20 +680,33 @@ __global__ void __launch_bounds__(RX_THREADS)
   const int fr = lane / TOPK;
   const int crow = RX_FRAMES + lane;
   float acc = 0.0f;
-  stage(0, 0);
+#pragma unroll
+  for (int st = 0; st < RXE_STAGES - 1; ++st) stage(st, st);
   for (int64_t ch = 0; ch < nchunks; ++ch) {
-    int cur = (int)(ch & 1);
-    // chunk ch has landed (and is visible to every thread) before use
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    const int cur = (int)(ch % RXE_STAGES);
+    // chunk ch has landed (groups complete in order; RXE_STAGES - 2 younger
+    // ones may still be in flight) and is visible to every thread; every
+    // thread is also done with the buffer the next stage overwrites
+    asm volatile("cp.async.wait_group %0;" ::"n"(RXE_STAGES - 2) : "memory");
     __syncthreads();
-    if (ch + 1 < nchunks) stage(cur ^ 1, ch + 1);
+    stage((int)((ch + RXE_STAGES - 1) % RXE_STAGES), ch + RXE_STAGES - 1);
     if (tid < 32) {
-      const float *xb = rx + (size_t)cur * RX_ROWS * RX_STRIDE + fr * RX_STRIDE;
-      const float *sb = rx + (size_t)cur * RX_ROWS * RX_STRIDE + crow * RX_STRIDE;
-      int64_t lim = n_pix - ch * RX_CHUNK;
-      int kmax = lim < RX_CHUNK ? (int)lim : RX_CHUNK;
-#pragma unroll 8
-      for (int k = 0; k < kmax; ++k) acc = fmaf(xb[k], sb[k], acc);
+      const float *xb = rx + (size_t)cur * RX_ROWS * RXE_STRIDE + fr * RXE_STRIDE;
+      const float *sb = rx + (size_t)cur * RX_ROWS * RXE_STRIDE + crow * RXE_STRIDE;
+      const int64_t lim = n_pix - ch * RXE_CHUNK;
+      if (lim >= RXE_CHUNK) {
+#pragma unroll 4
+        for (int k = 0; k < RXE_CHUNK; k += 4) {  // 16-byte reads, same FMA order
+          const float4 xv = *reinterpret_cast<const float4 *>(xb + k);
+          const float4 sv = *reinterpret_cast<const float4 *>(sb + k);
+          acc = fmaf(xv.x, sv.x, acc);
+          acc = fmaf(xv.y, sv.y, acc);
+          acc = fmaf(xv.z, sv.z, acc);
+          acc = fmaf(xv.w, sv.w, acc);
+        }
+      } else {
+        for (int k = 0; k < (int)lim; ++k) acc = fmaf(xb[k], sb[k], acc);
+      }
     }
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -731,7 +754,7 @@ __global__ void __launch_bounds__(RX_THREADS)
   work[im] = (dist - x2) + band;
 }
 
-constexpr size_t RX_SMEM = 2 * RX_ROWS * RX_STRIDE * sizeof(float);
+constexpr size_t RX_SMEM = (size_t)RXE_STAGES * RX_ROWS * RXE_STRIDE * sizeof(float);
 
 // Exact FP32 distances (plain-path arithmetic) for every listed candidate of
 // every frame; the per-frame lexicographic minimum is folded into best[]
@@ -871,7 +894,7 @@ __global__ void k_row_norms(const float *__restrict__ x, int64_t n_rows, int64_t
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-// k_rerank_exact uses RX_SMEM (74 KB) of dynamic shared memory
+// k_rerank_exact uses RX_SMEM (29 KB) of dynamic shared memory
 static int rerank_smem_attr() {
   static bool done[64] = {false};
   int dev = 0;
