@@ -604,10 +604,8 @@ __device__ __forceinline__ bool rerank_skip(const float *cand_d, int64_t im, int
 
 constexpr int RX_FRAMES = 4;
 constexpr int RX_ROWS = RX_FRAMES * (TOPK + 1);  // 4 frame rows + 32 candidate rows
-constexpr int RX_CHUNK = 256;
-constexpr int RX_STRIDE = RX_CHUNK + 4;          // 16-byte aligned rows, 4-way banks
 constexpr int RX_THREADS = 128;
-constexpr int RXE_CHUNK = 64;                    // k_rerank_exact: pixels per stage
+constexpr int RXE_CHUNK = 64;                    // re-rank kernels: pixels per stage
 constexpr int RXE_STRIDE = RXE_CHUNK + 4;
 constexpr int RXE_STAGES = 3;
 
@@ -759,10 +757,10 @@ constexpr size_t RX_SMEM = (size_t)RXE_STAGES * RX_ROWS * RXE_STRIDE * sizeof(fl
 // Exact FP32 distances (plain-path arithmetic) for every listed candidate of
 // every frame; the per-frame lexicographic minimum is folded into best[]
 // (packed order key << 32 | index, as spf_dist_argmin_f32 keeps it).  A CTA
-// takes one frame and walks its list 32 candidates at a time: all warps
+// takes one frame and walks its list 32 candidates at a time: warps 1-3
 // stream the frame row and the 32 candidate rows through shared memory in
-// 256-pixel chunks (cp.async, double-buffered) while warp 0 runs the 32
-// sequential FMA chains.
+// 64-pixel chunks (cp.async, the stages of k_rerank_exact) while warp 0 runs
+// the 32 sequential FMA chains.
 constexpr int RL_ROWS = 33;
 
 __global__ void __launch_bounds__(RX_THREADS)
@@ -770,7 +768,7 @@ __global__ void __launch_bounds__(RX_THREADS)
                   const float *__restrict__ img, const float *__restrict__ img_sq, int64_t n_img,
                   const float *__restrict__ ref, const float *__restrict__ ref_sq, int64_t n_pix,
                   int64_t ref_offset, unsigned long long *__restrict__ best) {
-  extern __shared__ __align__(16) float rx[];  // [2][RL_ROWS][RX_STRIDE]
+  extern __shared__ __align__(16) float rx[];  // [RXE_STAGES][RL_ROWS][RXE_STRIDE]
   __shared__ const float *rows[RL_ROWS];
   const int64_t im = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31;
@@ -780,7 +778,7 @@ __global__ void __launch_bounds__(RX_THREADS)
   // saturated tile list that may hide references, with fewer than cap entries
   // written): the caller settles that frame another way, so nothing is read
   if (cnt > cap) cnt = 0;
-  const int64_t nchunks = (n_pix + RX_CHUNK - 1) / RX_CHUNK;
+  const int64_t nchunks = (n_pix + RXE_CHUNK - 1) / RXE_CHUNK;
   const bool vec = (n_pix % 4) == 0 && aligned(img, 16) && aligned(ref, 16);
   unsigned long long kbest = ~0ULL;
   for (int g0 = 0; g0 < cnt; g0 += 32) {
@@ -795,15 +793,19 @@ __global__ void __launch_bounds__(RX_THREADS)
       rows[tid] = ptr;
     }
     __syncthreads();
+    // warps 1.. stage the chunks (an empty group past the end keeps one
+    // group per chunk); warp 0 runs the chains
     auto stage = [&](int buf, int64_t chunk) {
-      float *dst = rx + (size_t)buf * RL_ROWS * RX_STRIDE;
-      const int64_t base = chunk * RX_CHUNK;
-      for (int e = tid; e < RL_ROWS * (RX_CHUNK / 4); e += RX_THREADS) {
-        int r = e / (RX_CHUNK / 4), q4 = (e % (RX_CHUNK / 4)) * 4;
+      if (tid < 32) return;
+      float *dst = rx + (size_t)buf * RL_ROWS * RXE_STRIDE;
+      const int64_t base = chunk * RXE_CHUNK;
+      for (int e = tid - 32; chunk < nchunks && e < RL_ROWS * (RXE_CHUNK / 4);
+           e += RX_THREADS - 32) {
+        int r = e / (RXE_CHUNK / 4), q4 = (e % (RXE_CHUNK / 4)) * 4;
         const float *src = rows[r];
         if (!src) continue;  // a slot past the list's end: its chain is discarded
         int64_t p = base + q4;
-        float *d = dst + r * RX_STRIDE + q4;
+        float *d = dst + r * RXE_STRIDE + q4;
         if (vec && p + 3 < n_pix) {
           cp_async16(d, src + p);
         } else {
@@ -814,19 +816,30 @@ __global__ void __launch_bounds__(RX_THREADS)
       asm volatile("cp.async.commit_group;" ::: "memory");
     };
     float acc = 0.0f;
-    stage(0, 0);
+#pragma unroll
+    for (int st = 0; st < RXE_STAGES - 1; ++st) stage(st, st);
     for (int64_t ch = 0; ch < nchunks; ++ch) {
-      int cur = (int)(ch & 1);
-      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      const int cur = (int)(ch % RXE_STAGES);
+      asm volatile("cp.async.wait_group %0;" ::"n"(RXE_STAGES - 2) : "memory");
       __syncthreads();
-      if (ch + 1 < nchunks) stage(cur ^ 1, ch + 1);
+      stage((int)((ch + RXE_STAGES - 1) % RXE_STAGES), ch + RXE_STAGES - 1);
       if (tid < 32) {
-        const float *xb = rx + (size_t)cur * RL_ROWS * RX_STRIDE;
-        const float *sb = xb + (1 + lane) * RX_STRIDE;
-        int64_t lim = n_pix - ch * RX_CHUNK;
-        int kmax = lim < RX_CHUNK ? (int)lim : RX_CHUNK;
-#pragma unroll 8
-        for (int k = 0; k < kmax; ++k) acc = fmaf(xb[k], sb[k], acc);
+        const float *xb = rx + (size_t)cur * RL_ROWS * RXE_STRIDE;
+        const float *sb = xb + (1 + lane) * RXE_STRIDE;
+        const int64_t lim = n_pix - ch * RXE_CHUNK;
+        if (lim >= RXE_CHUNK) {
+#pragma unroll 4
+          for (int k = 0; k < RXE_CHUNK; k += 4) {  // 16-byte reads, same FMA order
+            const float4 xv = *reinterpret_cast<const float4 *>(xb + k);
+            const float4 sv = *reinterpret_cast<const float4 *>(sb + k);
+            acc = fmaf(xv.x, sv.x, acc);
+            acc = fmaf(xv.y, sv.y, acc);
+            acc = fmaf(xv.z, sv.z, acc);
+            acc = fmaf(xv.w, sv.w, acc);
+          }
+        } else {
+          for (int k = 0; k < (int)lim; ++k) acc = fmaf(xb[k], sb[k], acc);
+        }
       }
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -848,7 +861,7 @@ __global__ void __launch_bounds__(RX_THREADS)
   }
 }
 
-constexpr size_t RL_SMEM = 2 * RL_ROWS * RX_STRIDE * sizeof(float);
+constexpr size_t RL_SMEM = (size_t)RXE_STAGES * RL_ROWS * RXE_STRIDE * sizeof(float);
 
 // column maxima of squares: out[p] = max_r x[r, p]^2
 __global__ void k_col_maxsq(const float *__restrict__ x, int64_t n_rows, int64_t n_pix,
