@@ -56,10 +56,15 @@ int spf_selftest_bounded_wait(int64_t timeout_ms, int *d_result, void *stream);
  *                           tensor-core kernels (default 16)
  *   SPF_TUNE_FP32_GROUP_M : the same for the plain FP32 kernels (default 8)
  *   SPF_TUNE_BF16_GRID    : persistent CTAs of the tensor-core kernels
- *                           (default: one per SM) */
+ *                           (default: one per SM)
+ *   SPF_TUNE_PRIME_DFT    : the merge regulariser on a prime grid size M
+ *                           (read by spf_merge_create): 1 = Rader DFT
+ *                           (default, when M - 1 is 2,3,5,7-smooth),
+ *                           2 = cuFFT D2Z / Z2D */
 #define SPF_TUNE_BF16_GROUP_M 1
 #define SPF_TUNE_FP32_GROUP_M 2
 #define SPF_TUNE_BF16_GRID 3
+#define SPF_TUNE_PRIME_DFT 4
 int spf_tune_set(int param, int64_t value);
 int spf_tune_get(int param, int64_t *value);
 

@@ -28,6 +28,7 @@ SPF_ERR_UNSUPPORTED = -6
 SPF_TUNE_BF16_GROUP_M = 1
 SPF_TUNE_FP32_GROUP_M = 2
 SPF_TUNE_BF16_GRID = 3
+SPF_TUNE_PRIME_DFT = 4
 
 
 class SpfError(RuntimeError):

@@ -12,6 +12,9 @@
 // the kernel's transform is real because ugrid_conv is real and even).  The
 // regulariser is a size-M circular operation and uses exactly M; it runs in
 // FP64 because flambda = 1e3 scales its FP32 rounding above the data term.
+// For a prime M with smooth M - 1 (41, 151, ...) it runs as the Rader DFT
+// of prime_dft.cu (the reference's complex fftn / ifftn, real part taken);
+// otherwise as a cuFFT D2Z / Z2D pair on the half spectrum.
 //
 // CG follows scipy.sparse.linalg.cg (the solver the reference calls, :217)
 // step for step: stop when ||r|| < rtol ||b||, at most maxiter iterations.
@@ -24,6 +27,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "prime_dft.cuh"
 
 #include "../../include/spinifel_gb300.h"
 
@@ -56,7 +60,12 @@ struct spf_merge_s {
   double *scal = nullptr;      // device scalars
   int *flags = nullptr;        // [0] done, [1] iterations
   cufftHandle r2c_L = 0, c2r_L = 0, r2c_M = 0, c2r_M = 0;
-  bool plans_ok = false;
+  bool plans_ok = false;    // the L-grid pair
+  bool m_plans_ok = false;  // the M-grid D2Z / Z2D pair (regulariser without Rader)
+  // regulariser of a prime M with smooth M - 1: Rader DFT and the full
+  // real multiplier ifftshift(F_anti) on M^3
+  spf::PrimeDft *pd = nullptr;
+  double *mask_full = nullptr;
   // direct form
   spf_nufft_plan_s *nufft = nullptr;
   const float *quats = nullptr, *ppr = nullptr, *weights = nullptr;
@@ -311,7 +320,12 @@ __global__ void k_real_part(const float2 *__restrict__ z, float *__restrict__ ou
     out[i] = z[i].x;
 }
 
-// mask_hat[m] = F_anti[(m + M/2) mod M] on the R2C half spectrum
+// mask_hat on the R2C half spectrum: the even part (H(m) + H(-m)) / 2 of
+// H(m) = F_anti[(m + M/2) mod M].  For real input, Re(ifftn(fftn(y) . H))
+// (the reference's regulariser) equals the C2R transform of
+// rfftn(y) . (even part of H); F_anti from linspace is not always exactly
+// centrosymmetric (rounding at |q| = pi/ovs flips boundary cells, 28 of them
+// at M = 31), so H itself would differ there.
 __global__ void k_mask_half(const float *__restrict__ F, int M, double *__restrict__ out) {
   const int Mh = M / 2 + 1;
   const int64_t n = (int64_t)M * M * Mh;
@@ -319,6 +333,20 @@ __global__ void k_mask_half(const float *__restrict__ F, int M, double *__restri
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     int m3 = (int)(i % Mh), m2 = (int)((i / Mh) % M), m1 = (int)(i / ((int64_t)M * Mh));
+    int a = (m1 + h) % M, b = (m2 + h) % M, c = (m3 + h) % M;
+    int na = (M - m1 + h) % M, nb = (M - m2 + h) % M, nc = (M - m3 + h) % M;
+    out[i] = 0.5 * ((double)F[((int64_t)a * M + b) * M + c] +
+                    (double)F[((int64_t)na * M + nb) * M + nc]);
+  }
+}
+
+// mask_full[m] = F_anti[(m + M/2) mod M] on the whole M^3 spectrum
+__global__ void k_mask_full(const float *__restrict__ F, int M, double *__restrict__ out) {
+  const int64_t n = (int64_t)M * M * M;
+  const int h = M / 2;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int m3 = (int)(i % M), m2 = (int)((i / M) % M), m1 = (int)(i / ((int64_t)M * M));
     int a = (m1 + h) % M, b = (m2 + h) % M, c = (m3 + h) % M;
     out[i] = F[((int64_t)a * M + b) * M + c];
   }
@@ -337,8 +365,6 @@ static int grid1(int64_t n) { return grid_for(n, 256, (int64_t)sm_count() * 8); 
 
 // conv part of the operator from conv_in / reg_in / modes already loaded
 static int apply_operator_core(spf_merge_s *G, bool direct, cudaStream_t s) {
-  cufftSetStream(G->r2c_M, s);
-  cufftSetStream(G->c2r_M, s);
   if (!direct) {
     cufftSetStream(G->r2c_L, s);
     cufftSetStream(G->c2r_L, s);
@@ -361,6 +387,9 @@ static int apply_operator_core(spf_merge_s *G, bool direct, cudaStream_t s) {
                                              G->coord_scale, G->weights, s));
     SPF_TRY(spf_nufft_t1_finish(G->nufft, +1, G->t1_out, nullptr, s));
   }
+  if (G->pd) return prime_dft_filter(G->pd, G->reg_in, G->mask_full, G->reg_out, s);
+  cufftSetStream(G->r2c_M, s);
+  cufftSetStream(G->c2r_M, s);
   SPF_TRY(cufft_ok(cufftExecD2Z(G->r2c_M, G->reg_in,
                                 reinterpret_cast<cufftDoubleComplex *>(G->reg_freq)),
                    "reg D2Z"));
@@ -405,12 +434,18 @@ int spf_merge_create(int M, int M_ups, double rlambda, double flambda, const flo
   };
   alloc((void **)&G->support, G->n * sizeof(float));
   alloc((void **)&G->kernel_hat, G->nLh * sizeof(float));
-  alloc((void **)&G->mask_hat, G->nMh * sizeof(double));
+  const bool rader = prime_dft_applies(M) && tune_get(SPF_TUNE_PRIME_DFT, 1) == 1;
+  if (rader) {
+    alloc((void **)&G->mask_full, G->n * sizeof(double));
+    if (st == SPF_OK) st = prime_dft_create(M, 1, &G->pd);
+  } else {
+    alloc((void **)&G->mask_hat, G->nMh * sizeof(double));
+    alloc((void **)&G->reg_freq, G->nMh * sizeof(double2));
+  }
   alloc((void **)&G->conv_in, G->nL * sizeof(float));
   alloc((void **)&G->conv_freq, G->nLh * sizeof(float2));
   alloc((void **)&G->conv_out, G->nL * sizeof(float));
   alloc((void **)&G->reg_in, G->n * sizeof(double));
-  alloc((void **)&G->reg_freq, G->nMh * sizeof(double2));
   alloc((void **)&G->reg_out, G->n * sizeof(double));
   alloc((void **)&G->modes, G->n * sizeof(float));
   alloc((void **)&G->t1_out, G->n * sizeof(float));
@@ -422,10 +457,13 @@ int spf_merge_create(int M, int M_ups, double rlambda, double flambda, const flo
   alloc((void **)&G->flags, 2 * sizeof(int));
   if (st == SPF_OK) {
     bool ok = cufftPlan3d(&G->r2c_L, G->L, G->L, G->L, CUFFT_R2C) == CUFFT_SUCCESS &&
-              cufftPlan3d(&G->c2r_L, G->L, G->L, G->L, CUFFT_C2R) == CUFFT_SUCCESS &&
-              cufftPlan3d(&G->r2c_M, M, M, M, CUFFT_D2Z) == CUFFT_SUCCESS &&
-              cufftPlan3d(&G->c2r_M, M, M, M, CUFFT_Z2D) == CUFFT_SUCCESS;
+              cufftPlan3d(&G->c2r_L, G->L, G->L, G->L, CUFFT_C2R) == CUFFT_SUCCESS;
     G->plans_ok = ok;
+    if (ok && !G->pd) {
+      ok = cufftPlan3d(&G->r2c_M, M, M, M, CUFFT_D2Z) == CUFFT_SUCCESS &&
+           cufftPlan3d(&G->c2r_M, M, M, M, CUFFT_Z2D) == CUFFT_SUCCESS;
+      G->m_plans_ok = ok;
+    }
     if (!ok) {
       set_error("spf_merge_create: cufftPlan3d failed (L = %d, M = %d)", G->L, M);
       st = SPF_ERR_CUDA;
@@ -438,8 +476,13 @@ int spf_merge_create(int M, int M_ups, double rlambda, double flambda, const flo
   if (st == SPF_OK) {
     cudaMemset(G->conv_in, 0, G->nL * sizeof(float));
     cudaMemset(G->kernel_hat, 0, G->nLh * sizeof(float));
-    k_mask_half<<<grid1(G->nMh), 256>>>(d_antisupport, M, G->mask_hat);
-    st = check_launch("k_mask_half");
+    if (G->pd) {
+      k_mask_full<<<grid1(G->n), 256>>>(d_antisupport, M, G->mask_full);
+      st = check_launch("k_mask_full");
+    } else {
+      k_mask_half<<<grid1(G->nMh), 256>>>(d_antisupport, M, G->mask_hat);
+      st = check_launch("k_mask_half");
+    }
   }
   if (st == SPF_OK) st = check_cuda(cudaDeviceSynchronize(), "spf_merge_create");
   if (st != SPF_OK) {
@@ -454,12 +497,15 @@ int spf_merge_destroy(spf_merge_s *G) {
   if (!G) return SPF_OK;
   void *bufs[] = {G->support, G->kernel_hat, G->mask_hat, G->conv_in, G->conv_freq,
                   G->conv_out, G->reg_in, G->reg_freq, G->reg_out, G->modes, G->t1_out,
-                  G->r, G->p, G->q, G->partial, G->scal, G->flags};
+                  G->r, G->p, G->q, G->partial, G->scal, G->flags, G->mask_full};
   for (void *b : bufs) cudaFree(b);
   free_sweep(G->sweep);
+  prime_dft_free(G->pd);
   if (G->plans_ok) {
     cufftDestroy(G->r2c_L);
     cufftDestroy(G->c2r_L);
+  }
+  if (G->m_plans_ok) {
     cufftDestroy(G->r2c_M);
     cufftDestroy(G->c2r_M);
   }
@@ -606,7 +652,8 @@ struct Sweep {
   double *partial = nullptr, *scal = nullptr;
   int *flags = nullptr;
   cufftHandle r2c = 0, c2r = 0, d2z = 0, z2d = 0;
-  bool plans = false;
+  bool plans = false, m_plans = false;
+  spf::PrimeDft *pd = nullptr;  // batched Rader regulariser (prime M)
 };
 
 void free_sweep(Sweep *w) {
@@ -619,9 +666,12 @@ void free_sweep(Sweep *w) {
   if (w->plans) {
     cufftDestroy(w->r2c);
     cufftDestroy(w->c2r);
+  }
+  if (w->m_plans) {
     cufftDestroy(w->d2z);
     cufftDestroy(w->z2d);
   }
+  spf::prime_dft_free(w->pd);
   delete w;
 }
 
@@ -649,7 +699,11 @@ static int make_sweep(spf_merge_s *G, int nl) {
   alloc((void **)&w->conv_freq, nl * G->nLh * sizeof(float2));
   alloc((void **)&w->reg_in, nl * n * sizeof(double));
   alloc((void **)&w->reg_out, nl * n * sizeof(double));
-  alloc((void **)&w->reg_freq, nl * G->nMh * sizeof(double2));
+  if (G->pd) {
+    if (st == SPF_OK) st = prime_dft_create(G->M, nl, &w->pd);
+  } else {
+    alloc((void **)&w->reg_freq, nl * G->nMh * sizeof(double2));
+  }
   alloc((void **)&w->partial, nl * RED_BLOCKS * sizeof(double));
   alloc((void **)&w->scal, nl * S_COUNT * sizeof(double));
   alloc((void **)&w->flags, nl * 2 * sizeof(int));
@@ -661,12 +715,15 @@ static int make_sweep(spf_merge_s *G, int nl) {
         cufftPlanMany(&w->r2c, 3, dl, dl, 1, (int)G->nL, el, 1, (int)G->nLh, CUFFT_R2C, nl) ==
             CUFFT_SUCCESS &&
         cufftPlanMany(&w->c2r, 3, dl, el, 1, (int)G->nLh, dl, 1, (int)G->nL, CUFFT_C2R, nl) ==
-            CUFFT_SUCCESS &&
-        cufftPlanMany(&w->d2z, 3, dm, dm, 1, (int)n, em, 1, (int)G->nMh, CUFFT_D2Z, nl) ==
-            CUFFT_SUCCESS &&
-        cufftPlanMany(&w->z2d, 3, dm, em, 1, (int)G->nMh, dm, 1, (int)n, CUFFT_Z2D, nl) ==
             CUFFT_SUCCESS;
     w->plans = ok;
+    if (ok && !w->pd) {
+      ok = cufftPlanMany(&w->d2z, 3, dm, dm, 1, (int)n, em, 1, (int)G->nMh, CUFFT_D2Z, nl) ==
+               CUFFT_SUCCESS &&
+           cufftPlanMany(&w->z2d, 3, dm, em, 1, (int)G->nMh, dm, 1, (int)n, CUFFT_Z2D, nl) ==
+               CUFFT_SUCCESS;
+      w->m_plans = ok;
+    }
     if (!ok) {
       set_error("spf_merge_cg_sweep: batched cuFFT plans failed (n = %d)", nl);
       st = SPF_ERR_CUDA;
@@ -870,20 +927,27 @@ static int sweep_operator(spf_merge_s *G, Sweep *w, const double *v, double conv
   const int nl = w->nl;
   cufftSetStream(w->r2c, s);
   cufftSetStream(w->c2r, s);
-  cufftSetStream(w->d2z, s);
-  cufftSetStream(w->z2d, s);
   SPF_TRY(cufft_ok(cufftExecR2C(w->r2c, w->conv_in, reinterpret_cast<cufftComplex *>(w->conv_freq)),
                    "sweep conv R2C"));
   k_sw_mul<<<grid1(nl * G->nLh), 256, 0, s>>>(w->conv_freq, G->kernel_hat, G->nLh, nl * G->nLh);
   SPF_TRY(check_launch("k_sw_mul"));
   SPF_TRY(cufft_ok(cufftExecC2R(w->c2r, reinterpret_cast<cufftComplex *>(w->conv_freq), w->conv_out),
                    "sweep conv C2R"));
-  SPF_TRY(cufft_ok(cufftExecD2Z(w->d2z, w->reg_in, reinterpret_cast<cufftDoubleComplex *>(w->reg_freq)),
-                   "sweep reg D2Z"));
-  k_sw_mul_d<<<grid1(nl * G->nMh), 256, 0, s>>>(w->reg_freq, G->mask_hat, G->nMh, nl * G->nMh);
-  SPF_TRY(check_launch("k_sw_mul_d"));
-  SPF_TRY(cufft_ok(cufftExecZ2D(w->z2d, reinterpret_cast<cufftDoubleComplex *>(w->reg_freq), w->reg_out),
-                   "sweep reg Z2D"));
+  if (w->pd) {
+    SPF_TRY(prime_dft_filter(w->pd, w->reg_in, G->mask_full, w->reg_out, s));
+  } else {
+    cufftSetStream(w->d2z, s);
+    cufftSetStream(w->z2d, s);
+    SPF_TRY(cufft_ok(cufftExecD2Z(w->d2z, w->reg_in,
+                                  reinterpret_cast<cufftDoubleComplex *>(w->reg_freq)),
+                     "sweep reg D2Z"));
+    k_sw_mul_d<<<grid1(nl * G->nMh), 256, 0, s>>>(w->reg_freq, G->mask_hat, G->nMh,
+                                                  nl * G->nMh);
+    SPF_TRY(check_launch("k_sw_mul_d"));
+    SPF_TRY(cufft_ok(cufftExecZ2D(w->z2d, reinterpret_cast<cufftDoubleComplex *>(w->reg_freq),
+                                  w->reg_out),
+                     "sweep reg Z2D"));
+  }
   k_sw_assemble<<<dim3(RED_BLOCKS, nl), RED_THREADS, 0, s>>>(
       v, G->support, G->M, G->L, w->conv_out, G->conv_scale * conv_factor, w->reg_out, w->lam,
       w->q, w->partial);

@@ -167,3 +167,48 @@ def test_cg_solve_captured_in_a_cuda_graph(setup):
     torch.cuda.synchronize()
     assert int(iters.item()) == 12
     assert torch.equal(x, eager)
+
+
+def _reg_only(M, S, v, prime_dft):
+    """flambda * S.reg(S.v) of the Toeplitz operator (zero convolution kernel,
+    rlambda 0), with the regulariser's DFT chosen by SPF_TUNE_PRIME_DFT."""
+    from spinifel_gb300 import _lib
+    from spinifel_gb300.merge import MergeOperator, antisupport
+
+    dev = torch.device("cuda", 0)
+    _lib.call("spf_tune_set", _lib.SPF_TUNE_PRIME_DFT, prime_dft)
+    try:
+        op = MergeOperator(M, 2 * M, 0.0, 1.0, torch.as_tensor(S, dtype=torch.float32, device=dev),
+                           antisupport(M, 1))
+    finally:
+        _lib.call("spf_tune_set", _lib.SPF_TUNE_PRIME_DFT, 0)
+    op.set_kernel(torch.zeros((2 * M,) * 3, dtype=torch.float32, device=dev))
+    out = op.apply(torch.as_tensor(v.reshape(-1), device=dev)).cpu().numpy()
+    op.close()
+    return out
+
+
+@pytest.mark.parametrize("M", [31, 41])
+def test_prime_grid_regulariser_matches_fp64_oracle(lib, M):
+    """A prime model grid (M - 1 smooth) runs the regulariser as Rader DFTs:
+    S.Re(ifftn(fftn(S.x) . ifftshift(F_anti))) equals the oracle's numpy FP64
+    result to 1e-12, and the cuFFT path to 1e-12."""
+    rng = np.random.default_rng(M)
+    S = (rng.random((M,) * 3) > 0.2).astype(np.float64)
+    v = rng.standard_normal((M,) * 3)
+    mo = omerge.MergeOracle(M, 2 * M, 1000, oversampling=1)
+    want = mo.reg(v.reshape(-1), S)
+    rader = _reg_only(M, S, v, 1)
+    cufft = _reg_only(M, S, v, 2)
+    assert rel(rader, want) < 1e-12
+    assert rel(cufft, want) < 1e-12
+    assert rel(rader, cufft) < 1e-12
+
+
+def test_prime_grid_regulariser_151(lib):
+    """At the 151^3 merge grid the Rader path equals cuFFT's Bluestein path."""
+    M = 151
+    rng = np.random.default_rng(151)
+    S = np.ones((M,) * 3)
+    v = rng.standard_normal((M,) * 3)
+    assert rel(_reg_only(M, S, v, 1), _reg_only(M, S, v, 2)) < 1e-12
