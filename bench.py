@@ -310,9 +310,50 @@ def run_nufft(args):
 
     def spr():
         P.spread_zero()
-        P.spread_orient(q, ppr_t, mult, c, det_shape=det)
+        P.spread_orient(q, ppr_t, mult, c, det_shape=det, sort=False)
 
     t_spr = timed(spr)
+
+    def spr_orient_sorted():  # what spread_orient picks at this size: sort + sorted pass
+        P.spread_zero()
+        P.spread_orient(q, ppr_t, mult, c, det_shape=det, sort=True)
+
+    t_spr_s = timed(spr_orient_sorted)
+    # explicit points (the reference's adjoint call: H, K, L arrays): one
+    # thread per point with global atomics, and bin sort + sorted spreading
+    del out
+    H, K, L = (torch.empty(npts, dtype=torch.float32, device=dev) for _ in range(3))
+    for st in range(0, n_or, 250):
+        qq = q[st:st + 250].double()
+        w_, x_, y_, z_ = qq[:, 0:1], qq[:, 1:2], qq[:, 2:3], qq[:, 3:4]
+        R = torch.stack([torch.cat([1 - 2 * (y_ ** 2 + z_ ** 2), 2 * (x_ * y_ - z_ * w_),
+                                    2 * (x_ * z_ + y_ * w_)], 1),
+                         torch.cat([2 * (x_ * y_ + z_ * w_), 1 - 2 * (x_ ** 2 + z_ ** 2),
+                                    2 * (y_ * z_ - x_ * w_)], 1),
+                         torch.cat([2 * (x_ * z_ - y_ * w_), 2 * (y_ * z_ + x_ * w_),
+                                    1 - 2 * (x_ ** 2 + y_ ** 2)], 1)], 1)
+        hkl = torch.einsum("oji,jp->oip", R, ppr_t.double()) * mult  # R^-1 = R^T
+        sl = slice(st * n_pix, (st + qq.shape[0]) * n_pix)
+        H[sl], K[sl], L[sl] = (hkl[:, d].reshape(-1).float() for d in range(3))
+    cv = c.reshape(-1)
+
+    def spr_points():
+        P.spread_zero()
+        P.spread(H, K, L, cv)
+
+    t_pts = timed(spr_points, reps=1)
+    torch.cuda.synchronize()
+    e0.record()
+    P.sort_points(H, K, L)
+    e1.record()
+    torch.cuda.synchronize()
+    t_sort = e0.elapsed_time(e1)
+
+    def spr_sorted():
+        P.spread_zero()
+        P.spread_sorted(cv)
+
+    t_srt = timed(spr_sorted)
     w = P.width
     peaks, src = load_peaks()
     fp32_peak = 152 * 128 * 2 * 2070.0 * 1e6 / 1e12
@@ -326,7 +367,13 @@ def run_nufft(args):
         "interp_spread_sorted": {"ms": t_isp, "points_per_s": npts / (t_isp / 1e3)},
         "spread_t1_patch": {"ms": t_spr, "points_per_s": npts / (t_spr / 1e3),
                             "gbs_points": npts * 16 / (t_spr / 1e3) / 1e9,
-                            "hbm_peak_gbs": float(peaks.get("hbm_gbs", 6800.0))}}
+                            "hbm_peak_gbs": float(peaks.get("hbm_gbs", 6800.0))},
+        "spread_t1_orient_sort_and_spread": {"ms": t_spr_s, "points_per_s": npts / (t_spr_s / 1e3)},
+        "spread_t1_points": {"ms": t_pts, "points_per_s": npts / (t_pts / 1e3)},
+        "spread_t1_points_sorted": {"sort_ms": t_sort, "ms": t_srt,
+                                    "points_per_s": npts / (t_srt / 1e3),
+                                    "points_per_s_with_sort": npts / ((t_srt + t_sort) / 1e3),
+                                    "gbs_points": npts * 16 / (t_srt / 1e3) / 1e9}}
     print(json.dumps(rec), flush=True)
 
 
@@ -523,6 +570,7 @@ def run_merge(args):
     ev[2].record()
     torch.cuda.synchronize()
     spread_ms = ev[1].elapsed_time(ev[2])
+    ones_ms = ev[0].elapsed_time(ev[1])
     ugrid_conv = ugrid_conv / float(Mu) ** 3
     del Pu
     S = torch.ones((M,) * 3, dtype=torch.float32, device=dev)
@@ -594,6 +642,7 @@ def run_merge(args):
            "operator_direct_vs_toeplitz_rel_l2": op_rel,
            "data_term_direct_vs_toeplitz_rel_l2": conv_rel,
            "setup_type1_spread_ms": spread_ms,
+           "setup_type1_ones_302_ms": ones_ms,
            "interp_spread_pass": {"ms": isp_ms, "patch_kernel_ms": passes["patch"],
                                   "points_per_s": npts / (isp_ms / 1e3),
                                   "achieved_gbs": alg_bytes / (isp_ms / 1e3) / 1e9,

@@ -151,7 +151,19 @@ int spf_nufft_interp_spread_det(spf_nufft_plan plan, const float *d_quats, int64
  * shared memory.  The points' geometry pointers must stay valid. */
 int spf_nufft_sort_orient(spf_nufft_plan plan, const float *d_quats, int64_t n_orient,
                           const float *d_ppr, int64_t n_pix, double scale, void *stream);
+/* The same bin sort for n explicit points (coordinates in radians, as
+ * spf_nufft_t1_spread takes them); the sorted passes then read the points
+ * from d_x, d_y, d_z, which must stay valid. */
+int spf_nufft_sort_points(spf_nufft_plan plan, const float *d_x, const float *d_y,
+                          const float *d_z, int64_t n, void *stream);
 int spf_nufft_interp_spread_sorted(spf_nufft_plan plan, const float *d_weights, void *stream);
+/* Type-1 spreading of real values (d_values[o*n_pix + p], or 1 for every
+ * point when NULL) over the points sorted by spf_nufft_sort_orient, into the
+ * plan's type-1 accumulator (spf_nufft_t1_zero before, spf_nufft_t1_finish
+ * after), the adjoint's spreading stage (nufft_ext.py:287-327 NUFFT.adjoint;
+ * autocorrelation.py:152-166, the type 1 of ones).  Points sharing a
+ * footprint cell are summed in registers before the shared-memory adds. */
+int spf_nufft_spread_sorted(spf_nufft_plan plan, const float *d_values, void *stream);
 
 /* Fused type 2 -> type 1 at orientation points (the direct A^H D A product):
  * every point interpolates Re of the type-2 fine grid set by

@@ -78,7 +78,9 @@ SIGNATURES = {
     "spf_merge_set_direct": [_c_void_p, _c_void_p, _c_void_p, _i64, _c_void_p, _i64, _int, _int,
                              _int, _dbl, _c_void_p],
     "spf_nufft_sort_orient": [_c_void_p, _c_void_p, _i64, _c_void_p, _i64, _dbl, _c_void_p],
+    "spf_nufft_sort_points": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _i64, _c_void_p],
     "spf_nufft_interp_spread_sorted": [_c_void_p, _c_void_p, _c_void_p],
+    "spf_nufft_spread_sorted": [_c_void_p, _c_void_p, _c_void_p],
     "spf_nufft_t1_spread_det": [_c_void_p, _c_void_p, _i64, _c_void_p, _int, _int, _int, _dbl,
                                 _c_void_p, _c_void_p],
     "spf_nufft_interp_spread_det": [_c_void_p, _c_void_p, _i64, _c_void_p, _int, _int, _int, _dbl,

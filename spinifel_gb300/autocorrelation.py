@@ -63,9 +63,17 @@ def forward(ugrid, H_, K_, L_, support, use_recip_sym, N, eps=DEFAULT_EPS):
     return _arrays.like_input(out, ugrid)
 
 
+# from this many points on, the adjoint bin-sorts them once and spreads with
+# the sorted kernel (points sharing a footprint cell summed in registers)
+# instead of one thread per point with global atomics
+SORTED_SPREAD_MIN_POINTS = 1 << 21
+
+
 def adjoint(nuvect, H_, K_, L_, M, use_recip_sym=True, support=None, eps=DEFAULT_EPS,
-            isign=+1, plan=None):
-    """Type 1 onto M^3 (isign +1), times support, real part, divided by M^3."""
+            isign=+1, plan=None, sort=None):
+    """Type 1 onto M^3 (isign +1), times support, real part, divided by M^3.
+    sort: None picks the sorted spreading for large point sets; True / False
+    forces it on or off."""
     if _numel(H_):
         assert _max_abs(H_, K_, L_) < 3 * np.pi
     P = plan if plan is not None else plan_for(M, eps)
@@ -75,13 +83,23 @@ def adjoint(nuvect, H_, K_, L_, M, use_recip_sym=True, support=None, eps=DEFAULT
     c = c.to(_arrays.device()).reshape(-1)
     cre = (c.real if torch.is_complex(c) else c).to(torch.float32).contiguous()
     cim = c.imag.to(torch.float32).contiguous() if torch.is_complex(c) else None
+    use_sorted = (x.numel() >= SORTED_SPREAD_MIN_POINTS) if sort is None else bool(sort)
+    if use_sorted:
+        P.sort_points(x, y, z)
+
+    def spread(values):
+        if use_sorted:
+            P.spread_sorted(values)
+        else:
+            P.spread(x, y, z, values)
+
     P.spread_zero()
-    P.spread(x, y, z, cre)
+    spread(cre)
     fr_re, fr_im = P.finish(isign, want_imag=True)
     re, im = fr_re, fr_im
     if cim is not None and bool((cim != 0).any()):
         P.spread_zero()
-        P.spread(x, y, z, cim)
+        spread(cim)
         fi_re, fi_im = P.finish(isign, want_imag=True)
         re = fr_re - fi_im
         im = fr_im + fi_re

@@ -40,6 +40,7 @@ struct spf_nufft_plan_s {
   int64_t n_items = 0, n_sorted = 0, sorted_cap = 0, items_cap = 0;
   int nb[3] = {0, 0, 0};
   const float *s_quats = nullptr, *s_ppr = nullptr;
+  const float *s_x = nullptr, *s_y = nullptr, *s_z = nullptr;  // explicit points instead
   int64_t s_n_orient = 0, s_n_pix = 0;
   double s_scale = 0;
 };
@@ -726,6 +727,25 @@ __global__ void k_interp_spread_orient(const float *__restrict__ re_pad,
 constexpr int BIN = 8;
 constexpr int BIN_CHUNK = 2048;  // points per work item (big bins are split)
 
+// The points of the sorted passes: orientation points (point o * n_pix + p
+// is pixel p of the detector rotated by quaternion o, coordinates made in the
+// kernel) or explicit coordinates x, y, z.
+struct PointSrc {
+  const float *quats, *ppr;
+  int64_t n_pix;
+  const float *x, *y, *z;
+  __device__ __forceinline__ void coords(int64_t i, float &h, float &k, float &l) const {
+    if (x) {
+      h = x[i];
+      k = y[i];
+      l = z[i];
+      return;
+    }
+    const int64_t o = i / n_pix, p = i % n_pix;
+    rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
+  }
+};
+
 template <int W>
 __device__ __forceinline__ int point_bin(const GridGeom &g, const int *nb, float h, float k, float l,
                                          float s1, float s2, float s3) {
@@ -741,16 +761,12 @@ struct BinDims {
 };
 
 template <int W>
-__global__ void k_bin_count(GridGeom g, BinDims bd, const float *__restrict__ quats,
-                            const float *__restrict__ ppr, int64_t n_orient, int64_t n_pix,
-                            float s1, float s2, float s3, int32_t *__restrict__ bin_of,
-                            int32_t *__restrict__ counts) {
-  const int64_t n = n_orient * n_pix;
+__global__ void k_bin_count(GridGeom g, BinDims bd, PointSrc src, int64_t n, float s1, float s2,
+                            float s3, int32_t *__restrict__ bin_of, int32_t *__restrict__ counts) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    int64_t o = i / n_pix, p = i % n_pix;
     float h, k, l;
-    rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
+    src.coords(i, h, k, l);
     int b = point_bin<W>(g, bd.nb, h, k, l, s1, s2, s3);
     bin_of[i] = b;
     atomicAdd(counts + b, 1);
@@ -810,8 +826,7 @@ __device__ __forceinline__ int axis_cell(float x, float s, int n, int off) {
 template <int W>
 __global__ void __launch_bounds__(256)
     k_item_cellsort(GridGeom g, BinDims bd, const int4 *__restrict__ items,
-                    int32_t *__restrict__ sorted, const float *__restrict__ quats,
-                    const float *__restrict__ ppr, int64_t n_pix, float s1, float s2, float s3) {
+                    int32_t *__restrict__ sorted, PointSrc src, float s1, float s2, float s3) {
   constexpr int NC = BIN * BIN * BIN;
   __shared__ int32_t idx[BIN_CHUNK];
   __shared__ int16_t key[BIN_CHUNK];
@@ -824,9 +839,8 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   for (int q = threadIdx.x; q < it.z; q += blockDim.x) {
     const int32_t pi = sorted[it.y + q];
-    const int64_t o = pi / n_pix, p = pi % n_pix;
     float h, k, l;
-    rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
+    src.coords(pi, h, k, l);
     const int ci = min(max(axis_cell<W>(h, s1, g.n1, g.off1) - i0b, 0), BIN - 1);
     const int cj = min(max(axis_cell<W>(k, s2, g.n2, g.off2) - j0b, 0), BIN - 1);
     const int ck = min(max(axis_cell<W>(l, s3, g.n3, g.off3) - k0b, 0), BIN - 1);
@@ -906,12 +920,11 @@ __device__ __forceinline__ float es_eval_approx(float z, float beta_log2e) {
 }
 
 
-template <int W>
+template <int W, bool INTERP>
 __global__ void __launch_bounds__(SORTED_THREADS, 4)
     k_interp_spread_sorted(const float *__restrict__ re_pad, float *__restrict__ acc_pad,
                            GridGeom g, BinDims bd, const int4 *__restrict__ items,
-                           const int32_t *__restrict__ sorted, const float *__restrict__ quats,
-                           const float *__restrict__ ppr, int64_t n_pix, float s1, float s2,
+                           const int32_t *__restrict__ sorted, PointSrc src, float s1, float s2,
                            float s3, const float *__restrict__ weights,
                            unsigned int *__restrict__ err) {
   static_assert(W <= 8, "eight lanes per footprint row, two rows per lane");
@@ -919,7 +932,7 @@ __global__ void __launch_bounds__(SORTED_THREADS, 4)
   constexpr int SR = SORTED_ROW_STRIDE;
   constexpr int SP = D * SR;
   static_assert(D <= SR, "row stride holds a footprint row");
-  __shared__ float tbox[D * SP];
+  __shared__ float tbox[INTERP ? D * SP : 1];
   __shared__ float abox[D * SP];
   __shared__ float4 pt_tw[SORTED_THREADS];  // per warp: 32 prepared points
   __shared__ int pt_key[SORTED_THREADS];
@@ -929,7 +942,7 @@ __global__ void __launch_bounds__(SORTED_THREADS, 4)
   const int i0b = bi * BIN, j0b = bj * BIN, k0b = bk * BIN;
   const int di = min(D, g.p1 - i0b), dj = min(D, g.p2 - j0b), dk = min(D, g.p3 - k0b);
   const BoxShape shape{i0b, j0b, k0b, di, dj, dk, SP, SR};
-  box_load(tbox, re_pad, g, shape);
+  if (INTERP) box_load(tbox, re_pad, g, shape);
   box_rows(shape, [&](int, int, int, int s) { abox[s] = 0.0f; });
   __syncthreads();
   const unsigned FULL = 0xffffffffu;
@@ -970,9 +983,8 @@ __global__ void __launch_bounds__(SORTED_THREADS, 4)
     if (lane < cnt) {
       const int32_t pi = sorted[it.y + q0 + lane];
       const float pw = weights ? weights[pi] : 1.0f;
-      const int64_t o = pi / n_pix, p = pi % n_pix;
       float h, k, l;
-      rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
+      src.coords(pi, h, k, l);
       float t1 = __fmul_rn(h, s1), t2 = __fmul_rn(k, s2), t3 = __fmul_rn(l, s3);
       t1 = __fsub_rn(t1, __fmul_rn(fn1, floorf(__fadd_rn(__fdiv_rn(t1, fn1), 0.5f))));
       t2 = __fsub_rn(t2, __fmul_rn(fn2, floorf(__fadd_rn(__fdiv_rn(t2, fn2), 0.5f))));
@@ -1011,20 +1023,22 @@ __global__ void __launch_bounds__(SORTED_THREADS, 4)
 #pragma unroll
         for (int a = 0; a < W; ++a) {
           pend[a] = make_float2(0.0f, 0.0f);
-          xc[a] = make_float2(ok0 ? tbox[cur_base + lane_off0 + a * SP] : 0.0f,
-                              ok1 ? tbox[cur_base + lane_off1 + a * SP] : 0.0f);
+          if (INTERP)
+            xc[a] = make_float2(ok0 ? tbox[cur_base + lane_off0 + a * SP] : 0.0f,
+                                ok1 ? tbox[cur_base + lane_off1 + a * SP] : 0.0f);
         }
       }
-      // interpolate: plane a, the lane's two rows (one packed FMA per plane)
-      float2 sx = make_float2(0.0f, 0.0f);
+      float v = my_twf[4 * j + 3];  // the point's weight (1 without weights)
+      if (INTERP) {
+        // interpolate: plane a, the lane's two rows (one packed FMA per plane)
+        float2 sx = make_float2(0.0f, 0.0f);
 #pragma unroll
-      for (int a = 0; a < W; ++a) {
-        sx = ffma2(make_float2(w1[a], w1[a]), xc[a], sx);
+        for (int a = 0; a < W; ++a) sx = ffma2(make_float2(w1[a], w1[a]), xc[a], sx);
+        float part = fmaf(u1, sx.y, u0 * sx.x);
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) part += __shfl_xor_sync(FULL, part, m);
+        v *= part;
       }
-      float part = fmaf(u1, sx.y, u0 * sx.x);
-#pragma unroll
-      for (int m = 16; m >= 1; m >>= 1) part += __shfl_xor_sync(FULL, part, m);
-      const float v = part * my_twf[4 * j + 3];  // weight 1 without weights
       const float2 vv = make_float2(u0 * v, u1 * v);
 #pragma unroll
       for (int a = 0; a < W; ++a) pend[a] = ffma2(make_float2(w1[a], w1[a]), vv, pend[a]);
@@ -1406,13 +1420,9 @@ int spf_nufft_interp_spread_det(spf_nufft_plan P, const float *d_quats, int64_t 
                     "spf_nufft_interp_spread_det");
 }
 
-int spf_nufft_sort_orient(spf_nufft_plan P, const float *d_quats, int64_t n_orient,
-                          const float *d_ppr, int64_t n_pix, double scale, void *stream) {
-  SPF_TRY(check_plan(P, "spf_nufft_sort_orient"));
-  SPF_REQUIRE(n_orient >= 0 && n_pix >= 0, "spf_nufft_sort_orient: negative size");
-  SPF_REQUIRE(d_quats && d_ppr, "spf_nufft_sort_orient: NULL pointer");
-  const int64_t n = n_orient * n_pix;
-  SPF_REQUIRE(n < (1LL << 31), "spf_nufft_sort_orient: more than 2^31 points");
+// bin sort of n points (orientation or explicit) for the sorted passes
+static int sort_points(spf_nufft_plan P, PointSrc src, int64_t n, double scale, void *stream) {
+  SPF_REQUIRE(n < (1LL << 31), "spf_nufft_sort: more than 2^31 points");
   cudaStream_t s = as_stream(stream);
   GridGeom g = geom_of(P);
   BinDims bd;
@@ -1436,8 +1446,7 @@ int spf_nufft_sort_orient(spf_nufft_plan P, const float *d_quats, int64_t n_orie
     cursor = counts + 2 * n_bins;
     cudaMemsetAsync(counts, 0, n_bins * 3 * sizeof(int32_t), s);
     int grid = grid_for(n, 256, (int64_t)sm_count() * 16);
-    SPF_W_DISPATCH(P->w, (k_bin_count<W><<<grid, 256, 0, s>>>(g, bd, d_quats, d_ppr, n_orient,
-                                                                 n_pix, s1, s2, s3, bin_of,
+    SPF_W_DISPATCH(P->w, (k_bin_count<W><<<grid, 256, 0, s>>>(g, bd, src, n, s1, s2, s3, bin_of,
                                                                  counts)));
     st = check_launch("k_bin_count");
   }
@@ -1483,21 +1492,46 @@ int spf_nufft_sort_orient(spf_nufft_plan P, const float *d_quats, int64_t n_orie
   P->n_sorted = n;
   if (P->n_items > 0) {  // points sharing a footprint cell become consecutive
     SPF_W_DISPATCH(P->w, (k_item_cellsort<W><<<(unsigned)P->n_items, 256, 0, s>>>(
-                             g, bd, P->items, P->sorted, d_quats, d_ppr, n_pix, s1, s2, s3)));
+                             g, bd, P->items, P->sorted, src, s1, s2, s3)));
     SPF_TRY(check_launch("k_item_cellsort"));
   }
-  P->s_quats = d_quats;
-  P->s_ppr = d_ppr;
-  P->s_n_orient = n_orient;
-  P->s_n_pix = n_pix;
+  P->s_quats = src.quats;
+  P->s_ppr = src.ppr;
+  P->s_n_pix = src.n_pix;
+  P->s_x = src.x;
+  P->s_y = src.y;
+  P->s_z = src.z;
   P->s_scale = scale;
   return SPF_OK;
 }
 
-int spf_nufft_interp_spread_sorted(spf_nufft_plan P, const float *d_weights, void *stream) {
-  SPF_TRY(check_plan(P, "spf_nufft_interp_spread_sorted"));
+int spf_nufft_sort_orient(spf_nufft_plan P, const float *d_quats, int64_t n_orient,
+                          const float *d_ppr, int64_t n_pix, double scale, void *stream) {
+  SPF_TRY(check_plan(P, "spf_nufft_sort_orient"));
+  SPF_REQUIRE(n_orient >= 0 && n_pix >= 0, "spf_nufft_sort_orient: negative size");
+  SPF_REQUIRE(d_quats && d_ppr, "spf_nufft_sort_orient: NULL pointer");
+  SPF_REQUIRE(n_pix > 0 || n_orient == 0, "spf_nufft_sort_orient: n_pix = 0");
+  SPF_TRY(sort_points(P, PointSrc{d_quats, d_ppr, n_pix > 0 ? n_pix : 1, nullptr, nullptr, nullptr},
+                      n_orient * n_pix, scale, stream));
+  P->s_n_orient = n_orient;
+  return SPF_OK;
+}
+
+int spf_nufft_sort_points(spf_nufft_plan P, const float *d_x, const float *d_y,
+                          const float *d_z, int64_t n, void *stream) {
+  SPF_TRY(check_plan(P, "spf_nufft_sort_points"));
+  SPF_REQUIRE(n >= 0, "spf_nufft_sort_points: negative size");
+  SPF_REQUIRE(n == 0 || (d_x && d_y && d_z), "spf_nufft_sort_points: NULL pointer");
+  SPF_TRY(sort_points(P, PointSrc{nullptr, nullptr, 1, d_x, d_y, d_z}, n, 1.0, stream));
+  P->s_n_orient = 0;
+  return SPF_OK;
+}
+
+static int sorted_pass(spf_nufft_plan P, const float *d_weights, bool interp, const char *what,
+                       void *stream) {
+  SPF_TRY(check_plan(P, what));
   SPF_REQUIRE(P->sorted != nullptr && P->n_sorted > 0 || P->n_items == 0,
-              "spf_nufft_interp_spread_sorted: call spf_nufft_sort_orient first");
+              "%s: call spf_nufft_sort_orient first", what);
   if (P->n_items == 0) return SPF_OK;
   cudaStream_t s = as_stream(stream);
   GridGeom g = geom_of(P);
@@ -1506,11 +1540,30 @@ int spf_nufft_interp_spread_sorted(spf_nufft_plan P, const float *d_weights, voi
   float s1 = (float)(P->s_scale * P->n[0] / (2.0 * M_PI));
   float s2 = (float)(P->s_scale * P->n[1] / (2.0 * M_PI));
   float s3 = (float)(P->s_scale * P->n[2] / (2.0 * M_PI));
-  SPF_REQUIRE(P->n_items < (1LL << 31), "spf_nufft_interp_spread_sorted: too many items");
-  SPF_W_DISPATCH(P->w, (k_interp_spread_sorted<W><<<(unsigned)P->n_items, SORTED_THREADS, 0, s>>>(
-                           P->re_pad, P->acc_pad, g, bd, P->items, P->sorted, P->s_quats,
-                           P->s_ppr, P->s_n_pix, s1, s2, s3, d_weights, device_error_word())));
-  return check_launch("k_interp_spread_sorted");
+  SPF_REQUIRE(P->n_items < (1LL << 31), "%s: too many items", what);
+  const PointSrc src{P->s_quats, P->s_ppr, P->s_n_pix, P->s_x, P->s_y, P->s_z};
+  if (interp) {
+    SPF_W_DISPATCH(P->w, (k_interp_spread_sorted<W, true>
+                          <<<(unsigned)P->n_items, SORTED_THREADS, 0, s>>>(
+                              P->re_pad, P->acc_pad, g, bd, P->items, P->sorted, src, s1, s2,
+                              s3, d_weights,
+                              device_error_word())));
+  } else {
+    SPF_W_DISPATCH(P->w, (k_interp_spread_sorted<W, false>
+                          <<<(unsigned)P->n_items, SORTED_THREADS, 0, s>>>(
+                              P->re_pad, P->acc_pad, g, bd, P->items, P->sorted, src, s1, s2,
+                              s3, d_weights,
+                              device_error_word())));
+  }
+  return check_launch(what);
+}
+
+int spf_nufft_interp_spread_sorted(spf_nufft_plan P, const float *d_weights, void *stream) {
+  return sorted_pass(P, d_weights, true, "spf_nufft_interp_spread_sorted", stream);
+}
+
+int spf_nufft_spread_sorted(spf_nufft_plan P, const float *d_values, void *stream) {
+  return sorted_pass(P, d_values, false, "spf_nufft_spread_sorted", stream);
 }
 
 int spf_nufft_t1_finish(spf_nufft_plan P, int isign, float *d_out_re, float *d_out_im,

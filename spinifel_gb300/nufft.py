@@ -118,7 +118,13 @@ class NufftPlan:
         _lib.call("spf_nufft_t1_spread", self._h, _lib.ptr(x), _lib.ptr(y), _lib.ptr(z),
                   _lib.ptr(c), x.numel(), _lib.stream_handle())
 
-    def spread_orient(self, quats, ppr, scale, c, det_shape: tuple | None = None):
+    # from this many points on, spread_orient bin-sorts the points and uses
+    # the sorted spreading (points sharing a footprint cell summed in
+    # registers); below it, the patch or thread-per-point kernels
+    SORTED_MIN_POINTS = 1 << 21
+
+    def spread_orient(self, quats, ppr, scale, c, det_shape: tuple | None = None,
+                      sort: bool | None = None):
         quats = quats.to(device=self.device, dtype=torch.float32).contiguous()
         if det_shape is None and ppr.dim() == 4:
             det_shape = tuple(ppr.shape[1:])
@@ -126,7 +132,14 @@ class NufftPlan:
         c = c.to(device=self.device, dtype=torch.float32).contiguous()
         if c.numel() != quats.shape[0] * ppr.shape[1]:
             raise ValueError("strengths must be n_orient * n_pix")
-        if det_shape is not None and len(det_shape) == 3 and \
+        if sort is None:
+            sort = c.numel() >= self.SORTED_MIN_POINTS
+        if sort:
+            self._sorted_points = (quats, ppr)
+            _lib.call("spf_nufft_sort_orient", self._h, _lib.ptr(quats), quats.shape[0],
+                      _lib.ptr(ppr), ppr.shape[1], float(scale), _lib.stream_handle())
+            _lib.call("spf_nufft_spread_sorted", self._h, _lib.ptr(c), _lib.stream_handle())
+        elif det_shape is not None and len(det_shape) == 3 and \
                 int(np.prod(det_shape)) == ppr.shape[1]:
             _lib.call("spf_nufft_t1_spread_det", self._h, _lib.ptr(quats), quats.shape[0],
                       _lib.ptr(ppr), int(det_shape[0]), int(det_shape[1]), int(det_shape[2]),
@@ -135,6 +148,23 @@ class NufftPlan:
             _lib.call("spf_nufft_t1_spread_orient", self._h, _lib.ptr(quats), quats.shape[0],
                       _lib.ptr(ppr), ppr.shape[1], float(scale), _lib.ptr(c),
                       _lib.stream_handle())
+
+    def sort_points(self, x, y, z):
+        """Bin-sort explicit points (radians) once for spread_sorted; the
+        coordinate tensors are kept alive by the plan."""
+        x, y, z = (t.to(device=self.device, dtype=torch.float32).contiguous().reshape(-1)
+                   for t in (x, y, z))
+        self._sorted_points = (x, y, z)
+        _lib.call("spf_nufft_sort_points", self._h, _lib.ptr(x), _lib.ptr(y), _lib.ptr(z),
+                  x.numel(), _lib.stream_handle())
+
+    def spread_sorted(self, c=None):
+        """Type-1 spreading of c (or ones) over the points of the last sort
+        (sort_points or the orientation sort), into the type-1 accumulator."""
+        if c is not None:
+            c = c.to(device=self.device, dtype=torch.float32).contiguous().reshape(-1)
+        _lib.call("spf_nufft_spread_sorted", self._h, _lib.ptr(c) if c is not None else None,
+                  _lib.stream_handle())
 
     def finish(self, isign: int = 1, want_imag=False):
         re = torch.empty(self.m, device=self.device, dtype=torch.float32)

@@ -68,7 +68,11 @@ class Merge:
         op.set_kernel(ugrid_conv)
         if self.form == "direct":
             assert orientations is not None
-            plan = self.nufft.plan(self.M)
+            # a plan of its own: the operator keeps its bin-sorted points for
+            # the whole solve, while the adjoints below sort on the shared one
+            from ..nufft import NufftPlan
+
+            plan = NufftPlan(self.M, self.nufft.eps)
             det = tuple(self.pixel_position_reciprocal.shape[1:])
             op.set_direct(plan, torch.as_tensor(orientations, dtype=torch.float32, device=dev),
                           torch.as_tensor(self.pixel_position_reciprocal.reshape(3, -1),

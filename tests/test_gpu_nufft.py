@@ -296,3 +296,47 @@ def test_operator_glue_matches_reference_golden(dev):
     assert rel(fwd, g["forward"]) < TOL
     assert rel(adj, g["adjoint"]) < TOL
     assert adj.dtype in (np.float32, np.float64) and adj.shape == (15, 15, 15)
+
+
+@pytest.mark.parametrize("with_values", [True, False])
+def test_sorted_spread_of_explicit_points_equals_unsorted(dev, with_values):
+    """spf_nufft_sort_points + spf_nufft_spread_sorted (bin-sorted, runs of
+    points with the same footprint cell summed in registers) equals the
+    thread-per-point type-1 spreading, with values and with ones (NULL)."""
+    from spinifel_gb300 import geom
+    from spinifel_gb300.nufft import NufftPlan
+
+    model, ppr, pdr, quats = _slice_case(31, (4, 32, 32), 60, 41)
+    mult = np.pi / pdr.max()
+    H, K, L = geom.hkl(quats.astype(np.float64), ppr)
+    x, y, z = (t(v.reshape(-1) * mult, dev) for v in (H, K, L))
+    rng = np.random.default_rng(42)
+    c = t(rng.poisson(2.0, x.numel()).astype(np.float32), dev) if with_values else \
+        torch.ones(x.numel(), dtype=torch.float32, device=dev)
+    P = NufftPlan(31, 1e-6)
+    P.spread_zero()
+    P.spread(x, y, z, c)
+    a, _ = P.finish(+1)
+    P.sort_points(x, y, z)
+    P.spread_zero()
+    P.spread_sorted(c if with_values else None)
+    b, _ = P.finish(+1)
+    from spinifel_gb300 import matching
+
+    matching.check_device_error()  # no point fell outside its bin's box
+    assert rel(b.cpu().numpy(), a.cpu().numpy()) < 1e-6
+
+
+def test_adjoint_sorted_matches_oracle(dev):
+    """autocorrelation.adjoint with the sorted spreading forced on equals the
+    FP64 oracle's adjoint (the reference's glue) at the NUFFT tolerance."""
+    from spinifel_gb300 import autocorrelation as ac
+    from spinifel_gb300 import geom
+
+    model, ppr, pdr, quats = _slice_case(21, (4, 16, 16), 30, 43)
+    mult = np.pi / pdr.max()
+    H, K, L = (v.reshape(-1) * mult for v in geom.hkl(quats.astype(np.float64), ppr))
+    nuv = np.random.default_rng(44).standard_normal(H.size)
+    got = ac.adjoint(nuv, H, K, L, 21, True, None, sort=True)
+    want = onufft.adjoint(nuv, H, K, L, 21, True, None)
+    assert rel(np.asarray(got), np.asarray(want)) < TOL
