@@ -468,6 +468,56 @@ def run_phasing(args):
     print(json.dumps(out), flush=True)
 
 
+INGEST = dict(name="bin-frames-pnccd", n_img=1000, panels=4, sa=512, sb=512, n_clip=0, n_bin=2,
+              photons=0.5, seed=20261203)
+
+
+def run_ingest(args):
+    """Frame clipping + 2^n x 2^n binning on the device (prep.py:37-125):
+    raw uint16 PnCCD frames (4 panels of 512 x 512) binned 4 x 4 to the
+    4 x 128 x 128 matching detector, summed.  HBM-bound: 2 B read per raw
+    pixel, 4 B written per binned pixel."""
+    import torch
+
+    from spinifel_gb300 import prep
+
+    W = INGEST
+    n = args.n_img or W["n_img"]
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(W["seed"])
+    lam = torch.full((n, W["panels"], W["sa"], W["sb"]), W["photons"], device=dev)
+    raw = torch.poisson(lam, generator=g).to(torch.int16)
+    del lam
+    out = prep.bin_frames(raw, W["n_clip"], W["n_bin"])
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        prep.bin_frames(raw, W["n_clip"], W["n_bin"], out=out)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    bytes_moved = raw.numel() * 2 + out.numel() * 4
+    peaks, src = load_peaks()
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    # exactness on a sample: the binned sums equal the reference's repeated 2 x 2 sums
+    samp = raw[:4].to(torch.int64).cpu().numpy() & 0xFFFF
+    st_ = type("S", (), {"N_clipping": W["n_clip"], "N_binning": W["n_bin"]})()
+    want = prep.binning_sum(samp.astype(np.float64), st_)
+    exact = bool(np.array_equal(out[:4].cpu().numpy().astype(np.float64), want))
+    rec = {"metric": "frames binned/s (4 x 512 x 512 uint16 -> 4 x 128 x 128)",
+           "value": n / (ms / 1e3), "unit": "frames/s", "ms": ms, "n_img": n,
+           "config": {"workload": W["name"], "n_clip": W["n_clip"], "n_bin": W["n_bin"]},
+           "roofline": {"bound": "hbm", "achieved": bytes_moved / (ms / 1e3) / 1e9, "peak": peak,
+                        "unit": "GB/s", "frac": bytes_moved / (ms / 1e3) / 1e9 / peak,
+                        "peak_source": f"hbm_gbs ({src})"},
+           "exact_vs_reference_binning": exact}
+    print(json.dumps(rec), flush=True)
+
+
 def run_eval(args):
     """Reconstruction-quality tools at M = 81: scoring 420 candidate
     rotations (the coarse alignment search; trilinear rotation + Pearson
@@ -630,6 +680,74 @@ def run_merge(args):
         torch.cuda.synchronize()
         passes[name] = e0.elapsed_time(e1)
     isp_ms = passes["sorted"]
+    # the MPI merge's lambda sweep (mpi/autocorrelation.py:64-68): 8 ranks'
+    # (rlambda_r, flambda_r) as one batched CG, against the same 8 systems
+    # solved one after another with the single-system CG
+    from spinifel_gb300.mpi.autocorrelation import lambdas
+
+    n_sys = 8
+    rls, fls = lambdas(M, N, n_sys)
+    opm = MergeOperator(M, Mu, 1.0, 1.0, S, antisupport(M, 1))
+    opm.set_kernel(ugrid_conv)
+    opm.cg_sweep(rls, fls, d, x0, 2, rtol=1e-30, conv_factor=float(M) ** 3)  # warm-up
+    torch.cuda.synchronize()
+    ev[5].record()
+    xs, norms, its, _ = opm.cg_sweep(rls, fls, d, x0, W["iters"], rtol=1e-30,
+                                     conv_factor=float(M) ** 3)
+    ev[6].record()
+    torch.cuda.synchronize()
+    sweep_ms = ev[5].elapsed_time(ev[6])
+    seq_ms = 0.0
+    for r in range(n_sys):
+        ops = MergeOperator(M, Mu, float(rls[r]), float(fls[r]), S, antisupport(M, 1))
+        ops.set_kernel(ugrid_conv * float(M) ** 3)
+        ops.cg(d, x0, 2, rtol=1e-30)  # warm-up
+        torch.cuda.synchronize()
+        ev[5].record()
+        ops.cg(d, x0, W["iters"], rtol=1e-30)
+        ev[6].record()
+        torch.cuda.synchronize()
+        seq_ms += ev[5].elapsed_time(ev[6])
+        ops.close()
+    opm.close()
+    sweep = {"systems": n_sys, "iterations": W["iters"], "ms_total": sweep_ms,
+             "ms_per_iteration_all_systems": sweep_ms / W["iters"],
+             "sequential_single_solves_ms": seq_ms,
+             "speedup_vs_sequential": seq_ms / sweep_ms}
+    # the same comparison on the 41^3 grid of the reference's 41^3 example
+    # (a Gaussian stand-in for the Toeplitz kernel: timing only)
+    m_s = 41
+    g_ = torch.arange(2 * m_s, device=dev, dtype=torch.float32) - m_s
+    blob = torch.exp(-(g_[:, None, None] ** 2 + g_[None, :, None] ** 2 + g_[None, None, :] ** 2)
+                     / 50.0).contiguous()
+    S_s = torch.ones((m_s,) * 3, dtype=torch.float32, device=dev)
+    d_s = torch.randn(m_s ** 3, dtype=torch.float64, device=dev)
+    x0_s = torch.zeros_like(d_s)
+    rls_s, fls_s = lambdas(m_s, N, n_sys)
+    ops_ = MergeOperator(m_s, 2 * m_s, 1.0, 1.0, S_s, antisupport(m_s, 1))
+    ops_.set_kernel(blob)
+    ops_.cg_sweep(rls_s, fls_s, d_s, x0_s, 2, rtol=1e-30)
+    torch.cuda.synchronize()
+    ev[5].record()
+    ops_.cg_sweep(rls_s, fls_s, d_s, x0_s, W["iters"], rtol=1e-30)
+    ev[6].record()
+    torch.cuda.synchronize()
+    sw_s = ev[5].elapsed_time(ev[6])
+    ops_.close()
+    seq_s = 0.0
+    for r in range(n_sys):
+        o1 = MergeOperator(m_s, 2 * m_s, float(rls_s[r]), float(fls_s[r]), S_s, antisupport(m_s, 1))
+        o1.set_kernel(blob)
+        o1.cg(d_s, x0_s, 2, rtol=1e-30)
+        torch.cuda.synchronize()
+        ev[5].record()
+        o1.cg(d_s, x0_s, W["iters"], rtol=1e-30)
+        ev[6].record()
+        torch.cuda.synchronize()
+        seq_s += ev[5].elapsed_time(ev[6])
+        o1.close()
+    sweep["grid_41"] = {"ms_total": sw_s, "sequential_single_solves_ms": seq_s,
+                        "speedup_vs_sequential": seq_s / sw_s}
     peaks, src = load_peaks()
     alg_bytes = npts * 20.0 * 2  # coords + value per point, interpolation and spreading pass
     out = {"metric": "merge CG: ms per iteration (151^3, 1.31e8 points)",
@@ -643,6 +761,7 @@ def run_merge(args):
            "data_term_direct_vs_toeplitz_rel_l2": conv_rel,
            "setup_type1_spread_ms": spread_ms,
            "setup_type1_ones_302_ms": ones_ms,
+           "lambda_sweep": sweep,
            "interp_spread_pass": {"ms": isp_ms, "patch_kernel_ms": passes["patch"],
                                   "points_per_s": npts / (isp_ms / 1e3),
                                   "achieved_gbs": alg_bytes / (isp_ms / 1e3) / 1e9,
@@ -663,7 +782,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--workload", default="match",
-                    choices=["match", "merge", "serving", "nufft", "phasing", "eval"])
+                    choices=["match", "merge", "serving", "nufft", "phasing", "eval",
+                             "ingest"])
     args = ap.parse_args()
     if args.workload == "merge":
         run_merge(args)
@@ -676,6 +796,9 @@ def main():
         return
     if args.workload == "eval":
         run_eval(args)
+        return
+    if args.workload == "ingest":
+        run_ingest(args)
         return
     if args.workload == "serving":
         WORKLOAD.update(name="om-serving-200k", n_ref=200_000, n_img=20_000)

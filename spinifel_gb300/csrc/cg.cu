@@ -637,11 +637,20 @@ int spf_cg_solve(spf_merge_s *G, int form, const double *d_b, double *d_x, int x
 //   W_l x = c conv(x) + rlambda_l x + flambda_l reg(x) = ADb + rlambda_l x0
 // (c = 1 for the sequential merge's scaling, M^3 for the MPI merge, whose
 // kernel transform is not divided by M^3: mpi/autocorrelation.py:95-104)
-// run as one batched CG on one GPU: every vector is [n][M^3], the FFTs are
-// batched cuFFT plans, and each launch covers all systems (blockIdx.y, or one
-// block per system for the scalar stages), so an iteration costs the same
-// number of launches for any n.  Each system keeps its own CG scalars and
+// run as one batched CG on one GPU: every vector is [n][M^3], each pointwise
+// and CG launch covers all systems (blockIdx.y, or one block per system for
+// the scalar stages), and the transforms run system by system with the
+// single-system plans; the regulariser runs batched (Rader over all systems
+// while their buffers fit in L2 together, else system by system; batched
+// D2Z / Z2D for a non-prime M).  Each system keeps its own CG scalars and
 // stops on scipy's rule independently.
+// per-system stride of the sweep's L-grid arrays: L^3 rounded up to 64
+// floats, so that every system's array starts on a 256-byte boundary (cuFFT
+// rejects an R2C input at an odd float offset)
+__host__ __device__ __forceinline__ int64_t sweep_stride(int L) {
+  return ((int64_t)L * L * L + 63) / 64 * 64;
+}
+
 struct Sweep {
   int nl = 0;
   double *r = nullptr, *p = nullptr, *q = nullptr, *d = nullptr, *lam = nullptr;
@@ -651,9 +660,12 @@ struct Sweep {
   double2 *reg_freq = nullptr;
   double *partial = nullptr, *scal = nullptr;
   int *flags = nullptr;
-  cufftHandle r2c = 0, c2r = 0, d2z = 0, z2d = 0;
-  bool plans = false, m_plans = false;
-  spf::PrimeDft *pd = nullptr;  // batched Rader regulariser (prime M)
+  // regulariser of a non-prime M: batched D2Z / Z2D over the systems (their
+  // strides handled by cuFFT; per-system offsets of an odd M^3 doubles are
+  // not aligned for single-system transforms)
+  cufftHandle d2z = 0, z2d = 0;
+  bool m_plans = false;
+  spf::PrimeDft *pd = nullptr;  // prime M: the Rader regulariser over all systems at once
 };
 
 void free_sweep(Sweep *w) {
@@ -663,10 +675,6 @@ void free_sweep(Sweep *w) {
                   w->reg_freq, w->partial, w->scal,      w->flags};
   for (void *b : bufs)
     if (b) cudaFree(b);
-  if (w->plans) {
-    cufftDestroy(w->r2c);
-    cufftDestroy(w->c2r);
-  }
   if (w->m_plans) {
     cufftDestroy(w->d2z);
     cufftDestroy(w->z2d);
@@ -694,43 +702,37 @@ static int make_sweep(spf_merge_s *G, int nl) {
   alloc((void **)&w->q, nl * n * sizeof(double));
   alloc((void **)&w->d, nl * n * sizeof(double));
   alloc((void **)&w->lam, 2 * nl * sizeof(double));
-  alloc((void **)&w->conv_in, nl * G->nL * sizeof(float));
-  alloc((void **)&w->conv_out, nl * G->nL * sizeof(float));
+  const int64_t sL = sweep_stride(G->L);
+  alloc((void **)&w->conv_in, nl * sL * sizeof(float));
+  alloc((void **)&w->conv_out, nl * sL * sizeof(float));
   alloc((void **)&w->conv_freq, nl * G->nLh * sizeof(float2));
   alloc((void **)&w->reg_in, nl * n * sizeof(double));
   alloc((void **)&w->reg_out, nl * n * sizeof(double));
-  if (G->pd) {
-    if (st == SPF_OK) st = prime_dft_create(G->M, nl, &w->pd);
-  } else {
-    alloc((void **)&w->reg_freq, nl * G->nMh * sizeof(double2));
-  }
-  alloc((void **)&w->partial, nl * RED_BLOCKS * sizeof(double));
-  alloc((void **)&w->scal, nl * S_COUNT * sizeof(double));
-  alloc((void **)&w->flags, nl * 2 * sizeof(int));
-  if (st == SPF_OK) {
-    int dl[3] = {G->L, G->L, G->L}, dm[3] = {G->M, G->M, G->M};
-    const int Lh = G->L / 2 + 1, Mh = G->M / 2 + 1;
-    int el[3] = {G->L, G->L, Lh}, em[3] = {G->M, G->M, Mh};
+  // the Rader buffers (two complex M^3 arrays per system) of all systems
+  // together in L2: one batched regulariser; otherwise system by system with
+  // the operator's own (one system's buffers stay in L2: 110 MB at M = 151)
+  const bool batched_rader = (double)nl * 2.0 * (double)n * 16.0 <= 96.0 * (1 << 20);
+  if (G->pd && batched_rader && st == SPF_OK) st = prime_dft_create(G->M, nl, &w->pd);
+  if (!G->pd) alloc((void **)&w->reg_freq, nl * G->nMh * sizeof(double2));
+  if (st == SPF_OK && !G->pd) {
+    int dm[3] = {G->M, G->M, G->M};
+    int em[3] = {G->M, G->M, G->M / 2 + 1};
     bool ok =
-        cufftPlanMany(&w->r2c, 3, dl, dl, 1, (int)G->nL, el, 1, (int)G->nLh, CUFFT_R2C, nl) ==
+        cufftPlanMany(&w->d2z, 3, dm, dm, 1, (int)n, em, 1, (int)G->nMh, CUFFT_D2Z, nl) ==
             CUFFT_SUCCESS &&
-        cufftPlanMany(&w->c2r, 3, dl, el, 1, (int)G->nLh, dl, 1, (int)G->nL, CUFFT_C2R, nl) ==
+        cufftPlanMany(&w->z2d, 3, dm, em, 1, (int)G->nMh, dm, 1, (int)n, CUFFT_Z2D, nl) ==
             CUFFT_SUCCESS;
-    w->plans = ok;
-    if (ok && !w->pd) {
-      ok = cufftPlanMany(&w->d2z, 3, dm, dm, 1, (int)n, em, 1, (int)G->nMh, CUFFT_D2Z, nl) ==
-               CUFFT_SUCCESS &&
-           cufftPlanMany(&w->z2d, 3, dm, em, 1, (int)G->nMh, dm, 1, (int)n, CUFFT_Z2D, nl) ==
-               CUFFT_SUCCESS;
-      w->m_plans = ok;
-    }
+    w->m_plans = ok;
     if (!ok) {
       set_error("spf_merge_cg_sweep: batched cuFFT plans failed (n = %d)", nl);
       st = SPF_ERR_CUDA;
     }
   }
+  alloc((void **)&w->partial, nl * RED_BLOCKS * sizeof(double));
+  alloc((void **)&w->scal, nl * S_COUNT * sizeof(double));
+  alloc((void **)&w->flags, nl * 2 * sizeof(int));
   if (st == SPF_OK)
-    st = check_cuda(cudaMemset(w->conv_in, 0, nl * G->nL * sizeof(float)), "spf_merge_cg_sweep");
+    st = check_cuda(cudaMemset(w->conv_in, 0, nl * sL * sizeof(float)), "spf_merge_cg_sweep");
   if (st != SPF_OK) {
     free_sweep(w);
     return st;
@@ -761,7 +763,7 @@ __global__ void k_sw_load(double *__restrict__ v, const double *__restrict__ r,
                           const float *__restrict__ S, int M, int L, float *__restrict__ conv_in,
                           double *__restrict__ reg_in) {
   const int l = blockIdx.y;
-  const int64_t n = (int64_t)M * M * M, nL = (int64_t)L * L * L;
+  const int64_t n = (int64_t)M * M * M, sL = sweep_stride(L);
   const bool update = r != nullptr && !flags[2 * l];
   const double beta = r ? scal[l * S_COUNT + S_BETA] : 0.0;
   const int h = M / 2;
@@ -774,7 +776,7 @@ __global__ void k_sw_load(double *__restrict__ v, const double *__restrict__ r,
     }
     const double vd = pv * (double)S[i];
     const int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
-    conv_in[l * nL + ((int64_t)a * L + b) * L + c] = (float)vd;
+    conv_in[l * sL + ((int64_t)a * L + b) * L + c] = (float)vd;
     const int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
     reg_in[l * n + ((int64_t)ja * M + jb) * M + jc] = vd;
   }
@@ -807,7 +809,7 @@ __global__ void __launch_bounds__(RED_THREADS)
                   const double *__restrict__ reg_out, const double *__restrict__ lam,
                   double *__restrict__ q, double *__restrict__ partial) {
   const int l = blockIdx.y;
-  const int64_t n = (int64_t)M * M * M, nL = (int64_t)L * L * L;
+  const int64_t n = (int64_t)M * M * M, sL = sweep_stride(L);
   const int h = M / 2;
   const double reg_scale = 1.0 / ((double)M * M * M);
   const double rl = lam[2 * l], fl = lam[2 * l + 1];
@@ -816,7 +818,7 @@ __global__ void __launch_bounds__(RED_THREADS)
        i += (int64_t)gridDim.x * RED_THREADS) {
     const int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
     const double sv = S[i];
-    const double cv = (double)conv_out[l * nL + ((int64_t)a * L + b) * L + c];
+    const double cv = (double)conv_out[l * sL + ((int64_t)a * L + b) * L + c];
     const int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
     const double rv = reg_out[l * n + ((int64_t)ja * M + jb) * M + jc];
     const double xv = v[l * n + i];
@@ -924,17 +926,30 @@ __global__ void k_sw_iters(const int *flags, int *iters, int nl) {
 // the partials of v . q
 static int sweep_operator(spf_merge_s *G, Sweep *w, const double *v, double conv_factor,
                           cudaStream_t s) {
+  // the convolution transforms run system by system with the single-system
+  // plans (batched 3-D cuFFT plans measured slower); the regulariser runs
+  // batched when the systems' buffers fit in L2 together; the pointwise and
+  // CG kernels cover all systems per launch
   const int nl = w->nl;
-  cufftSetStream(w->r2c, s);
-  cufftSetStream(w->c2r, s);
-  SPF_TRY(cufft_ok(cufftExecR2C(w->r2c, w->conv_in, reinterpret_cast<cufftComplex *>(w->conv_freq)),
-                   "sweep conv R2C"));
+  cufftSetStream(G->r2c_L, s);
+  cufftSetStream(G->c2r_L, s);
+  for (int l = 0; l < nl; ++l)
+    SPF_TRY(cufft_ok(cufftExecR2C(G->r2c_L, w->conv_in + l * sweep_stride(G->L),
+                                  reinterpret_cast<cufftComplex *>(w->conv_freq + l * G->nLh)),
+                     "sweep conv R2C"));
   k_sw_mul<<<grid1(nl * G->nLh), 256, 0, s>>>(w->conv_freq, G->kernel_hat, G->nLh, nl * G->nLh);
   SPF_TRY(check_launch("k_sw_mul"));
-  SPF_TRY(cufft_ok(cufftExecC2R(w->c2r, reinterpret_cast<cufftComplex *>(w->conv_freq), w->conv_out),
-                   "sweep conv C2R"));
+  for (int l = 0; l < nl; ++l)
+    SPF_TRY(cufft_ok(cufftExecC2R(G->c2r_L,
+                                  reinterpret_cast<cufftComplex *>(w->conv_freq + l * G->nLh),
+                                  w->conv_out + l * sweep_stride(G->L)),
+                     "sweep conv C2R"));
   if (w->pd) {
     SPF_TRY(prime_dft_filter(w->pd, w->reg_in, G->mask_full, w->reg_out, s));
+  } else if (G->pd) {
+    for (int l = 0; l < nl; ++l)
+      SPF_TRY(prime_dft_filter(G->pd, w->reg_in + l * G->n, G->mask_full, w->reg_out + l * G->n,
+                               s));
   } else {
     cufftSetStream(w->d2z, s);
     cufftSetStream(w->z2d, s);

@@ -26,7 +26,8 @@ __device__ __forceinline__ void clip_map(int n_panels, int panel, int sa, int sb
 }
 
 __global__ void k_bin_frames(const uint16_t *__restrict__ raw, int64_t n_img, int n_panels, int sa,
-                             int sb, int ca, int cb, int nb, int mean, float *__restrict__ out) {
+                             int sb, int ca, int cb, int nb, int mean, bool vec4,
+                             float *__restrict__ out) {
   const int f = 1 << nb;
   const int oa = ca >> nb, ob = cb >> nb;
   const int64_t per_img = (int64_t)n_panels * oa * ob;
@@ -44,7 +45,12 @@ __global__ void k_bin_frames(const uint16_t *__restrict__ raw, int64_t n_img, in
       int rr, rc;
       clip_map(n_panels, panel, sa, sb, ca, cb, pr * f + dr, pc * f, &rr, &rc);
       const uint16_t *row = src + (int64_t)rr * sb + rc;
-      for (int dc = 0; dc < f; ++dc) s += row[dc];
+      if (vec4 && f == 4) {  // the block row as one 8-byte load (4 counts)
+        const uint2 q = *reinterpret_cast<const uint2 *>(row);
+        s += (q.x & 0xFFFFu) + (q.x >> 16) + (q.y & 0xFFFFu) + (q.y >> 16);
+      } else {
+        for (int dc = 0; dc < f; ++dc) s += row[dc];
+      }
     }
     out[i] = mean ? (float)((double)s * inv) : (float)s;
   }
@@ -74,8 +80,13 @@ extern "C" int spf_bin_frames_u16(const uint16_t *d_raw, int64_t n_img, int n_pa
   if (n_img == 0) return SPF_OK;
   SPF_REQUIRE(d_raw && d_out, "spf_bin_frames_u16: NULL pointer");
   const int64_t total = n_img * n_panels * (int64_t)(ca >> n_bin) * (cb >> n_bin);
+  // 4 x 4 blocks as 8-byte row loads when every block row starts on an
+  // 8-byte boundary: an aligned base, row length and clipped column offsets
+  // multiples of 4 pixels
+  const int col0 = n_panels == 1 ? sb / 2 - cb / 2 : sb - cb;
+  const bool vec4 = n_bin == 2 && ((uintptr_t)d_raw % 8) == 0 && sb % 4 == 0 && col0 % 4 == 0;
   k_bin_frames<<<spf::grid_for(total, 256, (int64_t)spf::sm_count() * 16), 256, 0,
                  spf::as_stream(stream)>>>(d_raw, n_img, n_panels, sa, sb, ca, cb, n_bin, mean,
-                                           d_out);
+                                           vec4, d_out);
   return spf::check_launch("k_bin_frames");
 }
