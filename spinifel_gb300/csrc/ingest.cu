@@ -9,6 +9,8 @@
 // prep.py:88-112), and sums the block in int64 (exact for uint16 counts), so
 // the result is exactly the reference's repeated 2 x 2 sums; the mean is the
 // sum / 4^N_binning (exact: a power of two).
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace {
@@ -25,34 +27,36 @@ __device__ __forceinline__ void clip_map(int n_panels, int panel, int sa, int sb
   }
 }
 
+// one CTA per (frame, panel) plane at a time (grid-stride over planes);
+// 32-bit index arithmetic within a plane
 __global__ void k_bin_frames(const uint16_t *__restrict__ raw, int64_t n_img, int n_panels, int sa,
                              int sb, int ca, int cb, int nb, int mean, bool vec4,
                              float *__restrict__ out) {
   const int f = 1 << nb;
   const int oa = ca >> nb, ob = cb >> nb;
-  const int64_t per_img = (int64_t)n_panels * oa * ob;
-  const int64_t total = n_img * per_img;
+  const int per_plane = oa * ob;
+  const int64_t planes = n_img * n_panels;
   const double inv = 1.0 / (double)((int64_t)f * f);
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t img = i / per_img;
-    const int64_t rem = i - img * per_img;
-    const int panel = (int)(rem / ((int64_t)oa * ob));
-    const int pr = (int)((rem / ob) % oa), pc = (int)(rem % ob);
-    const uint16_t *src = raw + (img * n_panels + panel) * (int64_t)sa * sb;
-    int64_t s = 0;
-    for (int dr = 0; dr < f; ++dr) {
-      int rr, rc;
-      clip_map(n_panels, panel, sa, sb, ca, cb, pr * f + dr, pc * f, &rr, &rc);
-      const uint16_t *row = src + (int64_t)rr * sb + rc;
-      if (vec4 && f == 4) {  // the block row as one 8-byte load (4 counts)
-        const uint2 q = *reinterpret_cast<const uint2 *>(row);
-        s += (q.x & 0xFFFFu) + (q.x >> 16) + (q.y & 0xFFFFu) + (q.y >> 16);
-      } else {
-        for (int dc = 0; dc < f; ++dc) s += row[dc];
+  for (int64_t pl = blockIdx.x; pl < planes; pl += gridDim.x) {
+    const int panel = (int)(pl % n_panels);
+    const uint16_t *src = raw + pl * (int64_t)sa * sb;
+    float *dst = out + pl * (int64_t)per_plane;
+    for (int q = threadIdx.x; q < per_plane; q += blockDim.x) {
+      const int pr = q / ob, pc = q - pr * ob;
+      int64_t s = 0;
+      for (int dr = 0; dr < f; ++dr) {
+        int rr, rc;
+        clip_map(n_panels, panel, sa, sb, ca, cb, pr * f + dr, pc * f, &rr, &rc);
+        const uint16_t *row = src + (int64_t)rr * sb + rc;
+        if (vec4 && f == 4) {  // the block row as one 8-byte load (4 counts)
+          const uint2 v = *reinterpret_cast<const uint2 *>(row);
+          s += (v.x & 0xFFFFu) + (v.x >> 16) + (v.y & 0xFFFFu) + (v.y >> 16);
+        } else {
+          for (int dc = 0; dc < f; ++dc) s += row[dc];
+        }
       }
+      dst[q] = mean ? (float)((double)s * inv) : (float)s;
     }
-    out[i] = mean ? (float)((double)s * inv) : (float)s;
   }
 }
 
@@ -79,13 +83,13 @@ extern "C" int spf_bin_frames_u16(const uint16_t *d_raw, int64_t n_img, int n_pa
               "spf_bin_frames_u16: clipped panel %d x %d not divisible by 2^%d", ca, cb, n_bin);
   if (n_img == 0) return SPF_OK;
   SPF_REQUIRE(d_raw && d_out, "spf_bin_frames_u16: NULL pointer");
-  const int64_t total = n_img * n_panels * (int64_t)(ca >> n_bin) * (cb >> n_bin);
   // 4 x 4 blocks as 8-byte row loads when every block row starts on an
   // 8-byte boundary: an aligned base, row length and clipped column offsets
   // multiples of 4 pixels
   const int col0 = n_panels == 1 ? sb / 2 - cb / 2 : sb - cb;
   const bool vec4 = n_bin == 2 && ((uintptr_t)d_raw % 8) == 0 && sb % 4 == 0 && col0 % 4 == 0;
-  k_bin_frames<<<spf::grid_for(total, 256, (int64_t)spf::sm_count() * 16), 256, 0,
+  const int64_t planes = n_img * n_panels;
+  k_bin_frames<<<(unsigned)std::min<int64_t>(planes, (int64_t)spf::sm_count() * 16), 256, 0,
                  spf::as_stream(stream)>>>(d_raw, n_img, n_panels, sa, sb, ca, cb, n_bin, mean,
                                            vec4, d_out);
   return spf::check_launch("k_bin_frames");
