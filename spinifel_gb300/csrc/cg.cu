@@ -198,7 +198,8 @@ __global__ void k_cg_update_p(double *__restrict__ p, const double *__restrict__
     }
     double vd = pv * (double)S[i];
     float v = (float)vd;
-    int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
+    const unsigned iu = (unsigned)i;  // M^3 < 2^31 (M <= 1024)
+    int c = (int)(iu % M), b = (int)((iu / M) % M), a = (int)(iu / (unsigned)(M * M));
     if (conv_in) conv_in[((int64_t)a * L + b) * L + c] = v;
     if (modes) modes[i] = v;
     // ifftshift: reg_in[j] = in[(j + M/2) mod M]  <=>  in[i] lands at j = (i - M/2) mod M
@@ -217,7 +218,8 @@ __global__ void k_load_input(const double *__restrict__ x, const float *__restri
        i += (int64_t)gridDim.x * blockDim.x) {
     double vd = x[i] * (double)S[i];
     float v = (float)vd;
-    int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
+    const unsigned iu = (unsigned)i;  // M^3 < 2^31 (M <= 1024)
+    int c = (int)(iu % M), b = (int)((iu / M) % M), a = (int)(iu / (unsigned)(M * M));
     if (conv_in) conv_in[((int64_t)a * L + b) * L + c] = v;
     if (modes) modes[i] = v;
     int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
@@ -257,7 +259,8 @@ __global__ void __launch_bounds__(RED_THREADS)
   double s = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * RED_THREADS) {
-    int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
+    const unsigned iu = (unsigned)i;  // M^3 < 2^31 (M <= 1024)
+    int c = (int)(iu % M), b = (int)((iu / M) % M), a = (int)(iu / (unsigned)(M * M));
     double sv = S[i];
     double cv = conv_out ? (double)conv_out[((int64_t)a * L + b) * L + c] : (double)t1_out[i];
     // fftshift: out[i] = reg_out[(i - M/2) mod M]
@@ -775,7 +778,8 @@ __global__ void k_sw_load(double *__restrict__ v, const double *__restrict__ r,
       v[l * n + i] = pv;
     }
     const double vd = pv * (double)S[i];
-    const int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
+    const unsigned iu = (unsigned)i;  // M^3 < 2^31 (M <= 1024)
+    const int c = (int)(iu % M), b = (int)((iu / M) % M), a = (int)(iu / (unsigned)(M * M));
     conv_in[l * sL + ((int64_t)a * L + b) * L + c] = (float)vd;
     const int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
     reg_in[l * n + ((int64_t)ja * M + jb) * M + jc] = vd;
@@ -816,7 +820,8 @@ __global__ void __launch_bounds__(RED_THREADS)
   double s = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * RED_THREADS) {
-    const int c = (int)(i % M), b = (int)((i / M) % M), a = (int)(i / ((int64_t)M * M));
+    const unsigned iu = (unsigned)i;  // M^3 < 2^31 (M <= 1024)
+    const int c = (int)(iu % M), b = (int)((iu / M) % M), a = (int)(iu / (unsigned)(M * M));
     const double sv = S[i];
     const double cv = (double)conv_out[l * sL + ((int64_t)a * L + b) * L + c];
     const int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;

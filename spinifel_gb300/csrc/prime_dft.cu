@@ -71,21 +71,24 @@ static int primitive_root(int p) {
   return -1;
 }
 
-// element idx of the [nb][p][p][p] array -> (line, position along axis ax)
-__device__ __forceinline__ void line_of(int64_t idx, int p, int ax, int64_t &line, int &n) {
-  const int64_t p3 = (int64_t)p * p * p;
-  const int64_t sys = idx / p3;
-  const int64_t r = idx - sys * p3;
-  const int i2 = (int)(r % p), i1 = (int)((r / p) % p), i0 = (int)(r / ((int64_t)p * p));
-  int u, v;
+// element idx of the [nb][p][p][p] array -> (line, position along axis ax);
+// 32-bit arithmetic (nb p^3 < 2^31, checked at creation)
+__device__ __forceinline__ void line_of(unsigned idx, unsigned p, int ax, unsigned &line,
+                                        int &n) {
+  const unsigned p2 = p * p, p3 = p2 * p;
+  const unsigned sys = idx / p3;
+  const unsigned r = idx - sys * p3;
+  const unsigned i0 = r / p2, r2 = r - i0 * p2;
+  const unsigned i1 = r2 / p, i2 = r2 - i1 * p;
+  unsigned u, v;
   if (ax == 2) {
-    n = i2; u = i0; v = i1;
+    n = (int)i2; u = i0; v = i1;
   } else if (ax == 1) {
-    n = i1; u = i0; v = i2;
+    n = (int)i1; u = i0; v = i2;
   } else {
-    n = i0; u = i1; v = i2;
+    n = (int)i0; u = i1; v = i2;
   }
-  line = sys * p * p + (int64_t)u * p + v;
+  line = sys * p2 + u * p + v;
 }
 
 // a[line][pinv[n]] = x[line, n] (n >= 1), x0[line] = x[line, 0]; the input
@@ -95,14 +98,14 @@ __global__ void k_pd_gather(const double *__restrict__ xr, const double2 *__rest
                             double2 *__restrict__ a, double2 *__restrict__ x0) {
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t line;
+    unsigned line;
     int n;
-    line_of(idx, p, ax, line, n);
+    line_of((unsigned)idx, (unsigned)p, ax, line, n);
     const double2 v = xr ? make_double2(xr[idx], 0.0) : z[idx];
     if (n == 0)
       x0[line] = v;
     else
-      a[line * (p - 1) + pinv[n]] = v;
+      a[(int64_t)line * (p - 1) + pinv[n]] = v;
   }
 }
 
@@ -111,9 +114,10 @@ __global__ void k_pd_mul(double2 *__restrict__ a, const double2 *__restrict__ bh
                          int64_t total, double2 *__restrict__ dc) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int m = (int)(i % pm1);
+    const unsigned iu = (unsigned)i;  // lines (p - 1) < 2^31
+    const int m = (int)(iu % (unsigned)pm1);
     const double2 v = a[i];
-    if (m == 0) dc[i / pm1] = v;
+    if (m == 0) dc[iu / (unsigned)pm1] = v;
     const double2 b = bh[m];
     a[i] = make_double2(v.x * b.x - v.y * b.y, v.x * b.y + v.y * b.x);
   }
@@ -129,14 +133,14 @@ __global__ void k_pd_scatter(const double2 *__restrict__ a, const double2 *__res
   const int64_t p3 = (int64_t)p * p * p;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t line;
+    unsigned line;
     int n;
-    line_of(idx, p, ax, line, n);
+    line_of((unsigned)idx, (unsigned)p, ax, line, n);
     const double2 b = x0[line];
-    const double2 c = n == 0 ? dc[line] : a[line * (p - 1) + qinv[n]];
+    const double2 c = n == 0 ? dc[line] : a[(int64_t)line * (p - 1) + qinv[n]];
     double2 X = make_double2(b.x + c.x, b.y + c.y);
     if (h) {
-      const double s = h[idx % p3];
+      const double s = h[(unsigned)idx % (unsigned)p3];
       X = make_double2(X.x * s, X.y * s);
     }
     if (re_out)
@@ -165,6 +169,8 @@ int prime_dft_create(int p, int nb, PrimeDft **out) {
   using namespace pdft;
   *out = nullptr;
   SPF_REQUIRE(prime_dft_applies(p) && nb >= 1, "prime_dft_create: size %d not supported", p);
+  SPF_REQUIRE((int64_t)nb * p * p * p < (1LL << 31), "prime_dft_create: %d x %d^3 too large", nb,
+              p);
   const int g = primitive_root(p);
   SPF_REQUIRE(g > 0, "prime_dft_create: no primitive root of %d", p);
   auto *d = new PrimeDft();
