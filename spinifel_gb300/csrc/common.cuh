@@ -96,4 +96,16 @@ int sm_count();
 // Runtime tunables (set by the autotuner through spf_tune_set).
 int64_t tune_get(int param, int64_t dflt);
 
+// d = a * b + c on two FP32 lanes in one instruction (fma.rn.f32x2, sm_100
+// family): each lane is an IEEE round-to-nearest fma, bit-identical to fmaf
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+
 }  // namespace spf

@@ -117,17 +117,31 @@ __device__ __forceinline__ void tile_mainloop(const T *__restrict__ A, int64_t n
         b[i] = Bs[cur][k][tx * 4 + i];
         b[i + 4] = Bs[cur][k][64 + tx * 4 + i];
       }
+      if constexpr (MODE == Mode::DOT && sizeof(T) == 4) {
+        // two outputs per instruction (packed fma, each lane the same IEEE
+        // fma as below, so every output's chain is unchanged)
 #pragma unroll
-      for (int i = 0; i < 8; ++i)
+        for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          if constexpr (MODE == Mode::DIFF) {
-            T d = a[i] - b[j];
-            acc[i][j] = fma(d, d, acc[i][j]);
-          } else {
-            acc[i][j] = fma(a[i], b[j], acc[i][j]);
+          for (int j = 0; j < 8; j += 2) {
+            const float2 r = ffma2(make_float2(a[i], a[i]), make_float2(b[j], b[j + 1]),
+                                   make_float2(acc[i][j], acc[i][j + 1]));
+            acc[i][j] = r.x;
+            acc[i][j + 1] = r.y;
           }
-        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            if constexpr (MODE == Mode::DIFF) {
+              T d = a[i] - b[j];
+              acc[i][j] = fma(d, d, acc[i][j]);
+            } else {
+              acc[i][j] = fma(a[i], b[j], acc[i][j]);
+            }
+          }
+      }
     }
     if (more) {
       la.store(As[cur ^ 1]);

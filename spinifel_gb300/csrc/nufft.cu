@@ -896,16 +896,6 @@ __global__ void __launch_bounds__(256)
 constexpr int SORTED_ROW_STRIDE = 24;
 constexpr int SORTED_THREADS = 256;
 
-// d = a * b + c on two FP32 lanes in one instruction (fma.rn.f32x2)
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
-  float2 d;
-  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
-      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
-      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-      : "=f"(d.x), "=f"(d.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-  return d;
-}
 
 // ES kernel exp(beta (sqrt(1 - z^2) - 1)) from the hardware approximations
 // (sqrt.approx, ex2.approx: relative errors near 2^-22, far below the
