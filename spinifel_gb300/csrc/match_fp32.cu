@@ -117,15 +117,22 @@ __device__ __forceinline__ void tile_mainloop(const T *__restrict__ A, int64_t n
         b[i] = Bs[cur][k][tx * 4 + i];
         b[i + 4] = Bs[cur][k][64 + tx * 4 + i];
       }
-      if constexpr (MODE == Mode::DOT && sizeof(T) == 4) {
-        // two outputs per instruction (packed fma, each lane the same IEEE
-        // fma as below, so every output's chain is unchanged)
+      if constexpr (sizeof(T) == 4) {
+        // two outputs per instruction (packed sub / fma, each lane the same
+        // IEEE operation as below, so every output's chain is unchanged)
 #pragma unroll
         for (int i = 0; i < 8; ++i)
 #pragma unroll
           for (int j = 0; j < 8; j += 2) {
-            const float2 r = ffma2(make_float2(a[i], a[i]), make_float2(b[j], b[j + 1]),
-                                   make_float2(acc[i][j], acc[i][j + 1]));
+            const float2 ai = make_float2(a[i], a[i]), bj = make_float2(b[j], b[j + 1]);
+            const float2 c = make_float2(acc[i][j], acc[i][j + 1]);
+            float2 r;
+            if constexpr (MODE == Mode::DIFF) {
+              const float2 d = fsub2(ai, bj);
+              r = ffma2(d, d, c);
+            } else {
+              r = ffma2(ai, bj, c);
+            }
             acc[i][j] = r.x;
             acc[i][j + 1] = r.y;
           }
