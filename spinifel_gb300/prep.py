@@ -5,9 +5,9 @@ pass from uint16 counts; the per-detector geometry (pixel positions, index
 maps; binned once) uses the numpy functions, which restate prep.py.
 
 HDF5 input (prep.py:131-183: intensities, pixel_position_reciprocal,
-pixel_index_map, orientations, volume) needs h5py, which neither this build
-nor its GPU machines provide; load_* read the same datasets from any mapping
-of dataset name -> array (an h5py.File where h5py exists)."""
+pixel_index_map, orientations, volume) needs h5py, which is not a dependency
+of this package; load_* read the same datasets from any mapping of dataset
+name -> array (an h5py.File where h5py exists)."""
 from __future__ import annotations
 
 import numpy as np
