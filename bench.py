@@ -748,6 +748,29 @@ def run_merge(args):
         o1.close()
     sweep["grid_41"] = {"ms_total": sw_s, "sequential_single_solves_ms": seq_s,
                         "speedup_vs_sequential": seq_s / sw_s}
+    # CPU baseline: one application of the reference's own W (numpy FP64
+    # fftn / ifftn of the Toeplitz product on 302^3 and the regulariser on
+    # 151^3, oracle/merge.py restating sequential/autocorrelation.py:116-149)
+    # on the host cores, i.e. the cost of one of its CG iterations
+    cpu_baseline = None
+    if not args.no_cpu_baseline:
+        import time
+
+        from oracle import merge as omerge
+
+        mo = omerge.MergeOracle(M, Mu, N, oversampling=1)
+        F_conv = np.fft.fftn(np.fft.ifftshift(ugrid_conv.double().cpu().numpy())) / M ** 3
+        S_h = S.double().cpu().numpy()
+        v_h = np.random.default_rng(3).standard_normal(M ** 3)
+        t0c = time.perf_counter()
+        mo.conv(v_h, F_conv, S_h) + mo.rlambda * v_h + mo.flambda * mo.reg(v_h, S_h)
+        cpu_ms = (time.perf_counter() - t0c) * 1e3
+        del F_conv
+        cpu_baseline = {"value": cpu_ms, "unit": "ms/iteration", "cores": 1,
+                        "kind": "port",
+                        "sample": "one W application of the numpy FP64 restatement "
+                                  "(Toeplitz product on 302^3 + regulariser on 151^3); "
+                                  "numpy's FFT (the reference's np.fft) runs on one core"}
     peaks, src = load_peaks()
     alg_bytes = npts * 20.0 * 2  # coords + value per point, interpolation and spreading pass
     out = {"metric": "merge CG: ms per iteration (151^3, 1.31e8 points)",
@@ -762,6 +785,7 @@ def run_merge(args):
            "setup_type1_spread_ms": spread_ms,
            "setup_type1_ones_302_ms": ones_ms,
            "lambda_sweep": sweep,
+           "cpu_baseline": cpu_baseline,
            "interp_spread_pass": {"ms": isp_ms, "patch_kernel_ms": passes["patch"],
                                   "points_per_s": npts / (isp_ms / 1e3),
                                   "achieved_gbs": alg_bytes / (isp_ms / 1e3) / 1e9,
