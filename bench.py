@@ -354,6 +354,25 @@ def run_nufft(args):
         P.spread_sorted(cv)
 
     t_srt = timed(spr_sorted)
+    # CPU baseline: the oracle's FP64 ES type 2 (fine-grid FFT in numpy, the
+    # interpolation in C with OpenMP on the host cores) on 4 orientations
+    cpu_baseline = None
+    if not args.no_cpu_baseline:
+        import time
+
+        from oracle import nufft as onufft
+
+        n_s = 4
+        qs = q[:n_s].double()
+        hs = [hh[:n_s * n_pix].double().cpu().numpy() for hh in (H, K, L)]
+        t0c = time.perf_counter()
+        onufft.nufft3d2(hs[0], hs[1], hs[2], model.astype(np.float64), -1, W["eps"])
+        cpu_s = time.perf_counter() - t0c
+        del qs
+        cpu_baseline = {"value": n_s * n_pix / cpu_s, "unit": "points/s", "cores": cpu_threads(),
+                        "kind": "port",
+                        "sample": f"{n_s} orientations x {n_pix} pixels, type 2 at eps "
+                                  f"{W['eps']} incl. the fine-grid FFT ({cpu_s:.2f} s)"}
     w = P.width
     peaks, src = load_peaks()
     fp32_peak = 152 * 128 * 2 * 2070.0 * 1e6 / 1e12
@@ -370,6 +389,7 @@ def run_nufft(args):
                             "hbm_peak_gbs": float(peaks.get("hbm_gbs", 6800.0))},
         "spread_t1_orient_sort_and_spread": {"ms": t_spr_s, "points_per_s": npts / (t_spr_s / 1e3)},
         "spread_t1_points": {"ms": t_pts, "points_per_s": npts / (t_pts / 1e3)},
+        "cpu_baseline": cpu_baseline,
         "spread_t1_points_sorted": {"sort_ms": t_sort, "ms": t_srt,
                                     "points_per_s": npts / (t_srt / 1e3),
                                     "points_per_s_with_sort": npts / ((t_srt + t_sort) / 1e3),
