@@ -153,6 +153,18 @@ __device__ __forceinline__ float es_eval(float z, float beta) {
   return expf(beta * (sqrtf(s) - 1.0f));
 }
 
+// ES kernel exp(beta (sqrt(1 - z^2) - 1)) from the hardware approximations
+// (sqrt.approx, ex2.approx: relative errors near 2^-22, far below the
+// kernel's own approximation error at any eps >= 1e-7); beta_log2e = beta log2(e)
+__device__ __forceinline__ float es_eval_approx(float z, float beta_log2e) {
+  const float s = fmaxf(fmaf(-z, z, 1.0f), 0.0f);
+  float r, e;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
+  const float x = beta_log2e * (r - 1.0f);
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(x));
+  return e;
+}
+
 // Padded first index and the W weights along one axis for the point at
 // x (in units of the coordinate scale) with grid scale s: t = x s in grid
 // units, wrapped into [-n/2, n/2).  The index arithmetic uses explicitly
@@ -173,14 +185,29 @@ __device__ __forceinline__ int axis_setup(float x, float s, int n, int off, floa
   return (int)l0 + off;
 }
 
+// axis_setup with the kernel values from es_eval_approx (the type-2 slicing
+// kernels: every kernel that slices through here gives the same bits)
+template <int W>
+__device__ __forceinline__ int axis_setup_approx(float x, float s, int n, int off,
+                                                 float beta_log2e, float inv_half_w, float *wt) {
+  float fn = (float)n;
+  float t = __fmul_rn(x, s);
+  t = __fsub_rn(t, __fmul_rn(fn, floorf(__fadd_rn(__fdiv_rn(t, fn), 0.5f))));
+  float l0 = ceilf(__fsub_rn(t, 0.5f * W));
+#pragma unroll
+  for (int a = 0; a < W; ++a) wt[a] = es_eval_approx((l0 + (float)a - t) * inv_half_w, beta_log2e);
+  return (int)l0 + off;
+}
+
 template <int W>
 __device__ __forceinline__ float interp_point(const float *__restrict__ grid, const GridGeom &g,
                                               float x1, float s1, float x2, float s2, float x3,
                                               float s3) {
   float w1[W], w2[W], w3[W];
-  int i0 = axis_setup<W>(x1, s1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
-  int j0 = axis_setup<W>(x2, s2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
-  int k0 = axis_setup<W>(x3, s3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
+  const float bl2 = g.beta * 1.4426950408889634f;
+  int i0 = axis_setup_approx<W>(x1, s1, g.n1, g.off1, bl2, g.inv_half_w, w1);
+  int j0 = axis_setup_approx<W>(x2, s2, g.n2, g.off2, bl2, g.inv_half_w, w2);
+  int k0 = axis_setup_approx<W>(x3, s3, g.n3, g.off3, bl2, g.inv_half_w, w3);
   float acc = 0.0f;
 #pragma unroll
   for (int a = 0; a < W; ++a) {
@@ -429,9 +456,10 @@ __global__ void __launch_bounds__(256)
   float h, k, l;
   rotate_inv(quats + 4 * o, ppr[p], ppr[n_pix + p], ppr[2 * n_pix + p], 1.0f, h, k, l);
   float w1[W], w2[W], w3[W];
-  int i0 = axis_setup<W>(h, scale1, g.n1, g.off1, g.beta, g.inv_half_w, w1);
-  int j0 = axis_setup<W>(k, scale2, g.n2, g.off2, g.beta, g.inv_half_w, w2);
-  int k0 = axis_setup<W>(l, scale3, g.n3, g.off3, g.beta, g.inv_half_w, w3);
+  const float bl2 = g.beta * 1.4426950408889634f;
+  int i0 = axis_setup_approx<W>(h, scale1, g.n1, g.off1, bl2, g.inv_half_w, w1);
+  int j0 = axis_setup_approx<W>(k, scale2, g.n2, g.off2, bl2, g.inv_half_w, w2);
+  int k0 = axis_setup_approx<W>(l, scale3, g.n3, g.off3, bl2, g.inv_half_w, w3);
   {
     int mi = valid ? i0 : INT32_MAX, mj = valid ? j0 : INT32_MAX, mk = valid ? k0 : INT32_MAX;
     int xi = valid ? i0 : INT32_MIN, xj = valid ? j0 : INT32_MIN, xk = valid ? k0 : INT32_MIN;
@@ -897,17 +925,6 @@ constexpr int SORTED_ROW_STRIDE = 24;
 constexpr int SORTED_THREADS = 256;
 
 
-// ES kernel exp(beta (sqrt(1 - z^2) - 1)) from the hardware approximations
-// (sqrt.approx, ex2.approx: relative errors near 2^-22, far below the
-// kernel's own approximation error at any eps >= 1e-7); beta_log2e = beta log2(e)
-__device__ __forceinline__ float es_eval_approx(float z, float beta_log2e) {
-  const float s = fmaxf(fmaf(-z, z, 1.0f), 0.0f);
-  float r, e;
-  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
-  const float x = beta_log2e * (r - 1.0f);
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(x));
-  return e;
-}
 
 
 template <int W, bool INTERP>
