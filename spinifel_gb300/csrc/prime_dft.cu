@@ -225,13 +225,14 @@ int prime_dft_create(int p, int nb, PrimeDft **out) {
       st = SPF_ERR_CUDA;
     }
   }
-  if (st == SPF_OK) {
-    cudaMemcpy(d->pinv, pinv.data(), p * sizeof(int16_t), cudaMemcpyHostToDevice);
-    cudaMemcpy(d->qinv, qinv.data(), p * sizeof(int16_t), cudaMemcpyHostToDevice);
-    cudaMemcpy(d->bf, bf.data(), pm1 * sizeof(double2), cudaMemcpyHostToDevice);
-    st = check_cuda(cudaMemcpy(d->bi, bi.data(), pm1 * sizeof(double2), cudaMemcpyHostToDevice),
-                    "prime_dft_create");
-  }
+  auto upload = [&](void *dst, const void *src, size_t bytes) {
+    if (st == SPF_OK)
+      st = check_cuda(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), "prime_dft_create");
+  };
+  upload(d->pinv, pinv.data(), p * sizeof(int16_t));
+  upload(d->qinv, qinv.data(), p * sizeof(int16_t));
+  upload(d->bf, bf.data(), pm1 * sizeof(double2));
+  upload(d->bi, bi.data(), pm1 * sizeof(double2));
   if (st != SPF_OK) {
     prime_dft_free(d);
     return st;

@@ -81,6 +81,22 @@ def test_library_rejects_bad_arguments_without_a_device(lib):
     assert lib.spf_status_string(_lib.SPF_ERR_TIMEOUT) == b"device wait timed out"
 
 
+def test_tunables_validated_without_a_device(lib):
+    """spf_tune_set / spf_tune_get (host-side): the prime-grid regulariser
+    switch takes 0 (default), 1 (Rader) or 2 (cuFFT); unknown parameters and
+    out-of-range values are rejected; 0 restores the built-in default."""
+    from spinifel_gb300 import _lib
+
+    v = ctypes.c_int64(-1)
+    assert lib.spf_tune_set(_lib.SPF_TUNE_PRIME_DFT, 3) == _lib.SPF_ERR_ARG
+    assert lib.spf_tune_set(_lib.SPF_TUNE_PRIME_DFT, -1) == _lib.SPF_ERR_ARG
+    assert lib.spf_tune_set(5, 1) == _lib.SPF_ERR_ARG
+    assert lib.spf_tune_set(_lib.SPF_TUNE_PRIME_DFT, 2) == _lib.SPF_OK
+    assert lib.spf_tune_get(_lib.SPF_TUNE_PRIME_DFT, ctypes.byref(v)) == _lib.SPF_OK
+    assert v.value == 2
+    assert lib.spf_tune_set(_lib.SPF_TUNE_PRIME_DFT, 0) == _lib.SPF_OK
+
+
 def test_named_entry_points_and_server_reject_bad_arguments_without_a_device(lib):
     from spinifel_gb300 import _lib
 
