@@ -139,3 +139,51 @@ def test_product_path_has_no_cpu_fallback(tmp_path):
             _lib.load(str(tmp_path / "missing.so"))
         finally:
             _lib._lib = _lib._lib_backup
+
+
+def test_adjoint_dispatch_sorted_spreading_by_size(monkeypatch):
+    """autocorrelation.adjoint sorts the points once and spreads with the
+    sorted kernel from SORTED_SPREAD_MIN_POINTS points on (twice for complex
+    values, one sort), and spreads point by point below it; sort=True/False
+    overrides.  Host logic only: a recording stand-in replaces the plan."""
+    import torch
+
+    from spinifel_gb300 import _arrays
+    from spinifel_gb300 import autocorrelation as ac
+
+    monkeypatch.setattr(_arrays, "device", lambda: torch.device("cpu"))
+    M = 4
+
+    class Rec:
+        def __init__(self):
+            self.calls = []
+
+        def sort_points(self, x, y, z):
+            self.calls.append("sort")
+
+        def spread_sorted(self, c):
+            self.calls.append("spread_sorted")
+
+        def spread(self, x, y, z, c):
+            self.calls.append("spread")
+
+        def spread_zero(self):
+            self.calls.append("zero")
+
+        def finish(self, isign, want_imag=False):
+            return torch.zeros(M ** 3), torch.zeros(M ** 3)
+
+    def run(n, values, **kw):
+        P = Rec()
+        xyz = [np.zeros(n, dtype=np.float32) for _ in range(3)]
+        ac.adjoint(values(n), *xyz, M, plan=P, **kw)
+        return P.calls
+
+    big = ac.SORTED_SPREAD_MIN_POINTS
+    real = lambda n: np.ones(n, dtype=np.float32)  # noqa: E731
+    cplx = lambda n: np.ones(n, dtype=np.complex64) * (1 + 1j)  # noqa: E731
+    assert run(big, real) == ["sort", "zero", "spread_sorted"]
+    assert run(big - 1, real) == ["zero", "spread"]
+    assert run(big, cplx) == ["sort", "zero", "spread_sorted", "zero", "spread_sorted"]
+    assert run(10, real, sort=True) == ["sort", "zero", "spread_sorted"]
+    assert run(big, real, sort=False) == ["zero", "spread"]
