@@ -187,3 +187,36 @@ def test_adjoint_dispatch_sorted_spreading_by_size(monkeypatch):
     assert run(big, cplx) == ["sort", "zero", "spread_sorted", "zero", "spread_sorted"]
     assert run(10, real, sort=True) == ["sort", "zero", "spread_sorted"]
     assert run(big, real, sort=False) == ["zero", "spread"]
+
+
+def test_spread_orient_dispatch_by_size(monkeypatch):
+    """NufftPlan.spread_orient: bin sort + sorted spreading from
+    SORTED_MIN_POINTS points on, the patch kernel (panel detector) or the
+    per-point kernel below; the plan keeps the sorted points' tensors."""
+    import torch
+
+    from spinifel_gb300 import _lib
+    from spinifel_gb300.nufft import NufftPlan
+
+    calls = []
+    monkeypatch.setattr(_lib, "call", lambda name, *a: calls.append(name))
+    monkeypatch.setattr(_lib, "stream_handle", lambda *a: None)
+    P = object.__new__(NufftPlan)
+    P._h = None
+    P.device = torch.device("cpu")
+
+    def run(n_orient, n_pix, det=None, **kw):
+        calls.clear()
+        q = torch.zeros(n_orient, 4)
+        ppr = torch.zeros(3, n_pix)
+        c = torch.zeros(n_orient * n_pix)
+        P.spread_orient(q, ppr, 1.0, c, det_shape=det, **kw)
+        return list(calls)
+
+    n_pix = 4 * 32 * 32
+    big = -(-NufftPlan.SORTED_MIN_POINTS // n_pix)  # orientations reaching the threshold
+    assert run(big, n_pix, (4, 32, 32)) == ["spf_nufft_sort_orient", "spf_nufft_spread_sorted"]
+    assert len(P._sorted_points) == 2
+    assert run(2, n_pix, (4, 32, 32)) == ["spf_nufft_t1_spread_det"]
+    assert run(2, n_pix) == ["spf_nufft_t1_spread_orient"]
+    assert run(2, n_pix, sort=True) == ["spf_nufft_sort_orient", "spf_nufft_spread_sorted"]
