@@ -90,3 +90,36 @@ def test_merge_mpi_mirror_matches_reference_golden(setup, gen):
     np.testing.assert_allclose(got[:, 1], summ[:, 1], rtol=1e-12)  # lambdas
     np.testing.assert_allclose(got[:, 2], summ[:, 2], rtol=1e-4)   # ||x||
     assert rel(ac, g[f"ac_gen{gen}"]) < 1e-3
+
+
+@pytest.mark.parametrize("M,n_sys", [(31, 3), (151, 2)])
+def test_prime_grid_sweep_equals_single_solves(lib, M, n_sys):
+    """On a prime grid the sweep's regulariser is the Rader DFT: batched over
+    all systems while their buffers fit in L2 together (M = 31), system by
+    system otherwise (M = 151).  Either way every system's iterates equal
+    the single-system CG's."""
+    from spinifel_gb300.merge import MergeOperator, antisupport
+
+    dev = torch.device("cuda", 0)
+    g = torch.arange(2 * M, device=dev, dtype=torch.float32) - M
+    kern = torch.exp(-(g[:, None, None] ** 2 + g[None, :, None] ** 2 + g[None, None, :] ** 2)
+                     / (0.05 * M * M)).contiguous()
+    St = torch.ones((M,) * 3, dtype=torch.float32, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(M)
+    adb = torch.randn(M ** 3, dtype=torch.float64, device=dev, generator=gen)
+    x0 = torch.zeros_like(adb)
+    rls = np.array([1e-3, 1e-2, 1e-1])[:n_sys]
+    fls = np.array([10.0, 1e3, 1e2])[:n_sys]
+    iters_n = 6
+    op = MergeOperator(M, 2 * M, 0.0, 0.0, St, antisupport(M, 1))
+    op.set_kernel(kern)
+    x, norms, iters, _ = op.cg_sweep(rls, fls, adb, x0, iters_n, rtol=1e-30)
+    for l in range(n_sys):
+        single = MergeOperator(M, 2 * M, rls[l], fls[l], St, antisupport(M, 1))
+        single.set_kernel(kern)
+        xs, it, _ = single.cg(adb + rls[l] * x0, x0, iters_n, rtol=1e-30)
+        assert int(iters[l]) == int(it.item()) == iters_n
+        assert rel(x[l].cpu().numpy(), xs.cpu().numpy()) < 1e-7
+        single.close()
+    op.close()
