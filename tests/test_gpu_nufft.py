@@ -340,3 +340,25 @@ def test_adjoint_sorted_matches_oracle(dev):
     got = ac.adjoint(nuv, H, K, L, 21, True, None, sort=True)
     want = onufft.adjoint(nuv, H, K, L, 21, True, None)
     assert rel(np.asarray(got), np.asarray(want)) < TOL
+
+
+def test_spread_orient_sorted_equals_patch(dev):
+    """NufftPlan.spread_orient with the bin sort + sorted spreading (what it
+    picks for large point sets) equals the patch kernel on the same points."""
+    from spinifel_gb300.nufft import NufftPlan
+
+    model, ppr, pdr, quats = _slice_case(41, (4, 32, 32), 50, 45)
+    mult = np.pi / pdr.max()
+    ppr_t = t(ppr.reshape(3, -1), dev)
+    q_t = t(quats, dev)
+    c = t(np.random.default_rng(46).poisson(1.5, (50, ppr[0].size)).astype(np.float32), dev)
+    P = NufftPlan(41, 1e-6)
+    out = []
+    for sort in (False, True):
+        P.spread_zero()
+        P.spread_orient(q_t, ppr_t, mult, c.reshape(-1), det_shape=(4, 32, 32), sort=sort)
+        out.append(P.finish(+1)[0].cpu().numpy())
+    from spinifel_gb300 import matching
+
+    matching.check_device_error()
+    assert rel(out[1], out[0]) < 1e-6
