@@ -31,6 +31,7 @@ extern "C" {
 #define SPF_ERR_UNSUPPORTED (-6) /* device or shape not supported            */
 
 typedef struct spf_nufft_plan_s *spf_nufft_plan;
+typedef struct spf_nufft64_plan_s *spf_nufft64_plan;
 typedef struct spf_merge_s *spf_merge;
 typedef struct spf_server_s *spf_server;
 typedef struct spf_phaser_s *spf_phaser;
@@ -197,6 +198,43 @@ int spf_fft_deconv(spf_nufft_plan plan, int type, int isign, const float *d_mode
                    const float *d_support, float *d_modes_out_re, float *d_modes_out_im,
                    void *stream);
 
+/* ---- FP64 NUFFT plan (the reference's tolerance) -----------------------
+ * The reference runs its NUFFTs at eps = 1e-12 in double
+ * (spinifel/extern/nufft_ext.py:62; finufft_ext.py:70-89 for type 2,
+ * finufft_ext.py:41-60 for type 1); an FP32 grid cannot reach that, so these
+ * entry points repeat the FP32 plan's type 2 and type 1 in FP64 with kernel
+ * widths up to 16 (w = 13 at eps 1e-12).  Same mode ordering, axis
+ * convention and isign meaning as spf_nufft_plan_create.  eps in [1e-15, 1). */
+int spf_nufft64_plan_create(int m1, int m2, int m3, double eps, double upsampfac,
+                            spf_nufft64_plan *out);
+int spf_nufft64_plan_destroy(spf_nufft64_plan plan);
+int spf_nufft64_plan_info(spf_nufft64_plan plan, int *n_fine, int *width, double *beta,
+                          int *n_padded);
+/* spf_nufft_t2_set_modes in FP64 (d_modes, d_support: m1*m2*m3 doubles). */
+int spf_nufft64_t2_set_modes(spf_nufft64_plan plan, const double *d_modes,
+                             const double *d_support, int isign, int want_imag, void *stream);
+/* spf_nufft_t2_interp in FP64 (NUFFT.forward at explicit points,
+ * spinifel/autocorrelation.py:32-61). */
+int spf_nufft64_t2_interp(spf_nufft64_plan plan, const double *d_x, const double *d_y,
+                          const double *d_z, int64_t npts, double *d_out_re, double *d_out_im,
+                          void *stream);
+/* spf_slice_t2 in FP64: quaternions (4 per orientation) and pixel positions
+ * (3 x n_pix) in double, rotation by R(q)^-1 in double, d_out[o*n_pix + p]
+ * = Re c.  Replaces NUFFT.forward at the reference's eps
+ * (spinifel/extern/nufft_ext.py:420-446 with the HKL precompute :136-144). */
+int spf_slice_t2_f64(spf_nufft64_plan plan, const double *d_quats, int64_t n_orient,
+                     const double *d_ppr, int64_t n_pix, double scale, double *d_out,
+                     void *stream);
+/* Type 1 in FP64: zero (allocates the accumulator on first use), spread real
+ * strengths at explicit points, fold + FFT + deconvolve onto the modes
+ * (NUFFT.adjoint before the support multiply and 1/M^3,
+ * spinifel/extern/nufft_ext.py:450-487). */
+int spf_nufft64_t1_zero(spf_nufft64_plan plan, void *stream);
+int spf_nufft64_t1_spread(spf_nufft64_plan plan, const double *d_x, const double *d_y,
+                          const double *d_z, const double *d_c, int64_t npts, void *stream);
+int spf_nufft64_t1_finish(spf_nufft64_plan plan, int isign, double *d_out_re,
+                          double *d_out_im, void *stream);
+
 /* ---- orientation matching --------------------------------------------- */
 
 /* pyCudaKNearestNeighbors.cudaEuclideanDistance
@@ -254,6 +292,20 @@ int spf_dist_argmin_fp32(const float *d_img, const float *d_img_sq, int64_t n_im
                          const float *d_ref, const float *d_ref_sq, int64_t n_ref,
                          int64_t n_pix, uint64_t *d_best, int32_t *d_idx, float *d_dist,
                          void *stream);
+
+/* FP64 matching at the reference's double precision (use_single_prec =
+ * false: SNM.euclidean_dist in float64, orientation_matching.py:32-36,
+ * 98-109, and the sklearn branch of nearest_neighbor.py:134-135).
+ * spf_dist_f64: d_out[d*n_ref + r] = sum over ALL n_pix pixels of
+ * (data - ref)^2 in FP64.  spf_argmin_rows_f64 folds each row's minimum
+ * (index + ref_offset; ties to the lower index; the running best changes only
+ * on a strictly smaller distance) into d_best_dist / d_best_idx
+ * (initialise with spf_best64_init: +inf, -1). */
+int spf_dist_f64(const double *d_ref, const double *d_data, int64_t n_ref, int64_t n_data,
+                 int64_t n_pix, double *d_out, void *stream);
+int spf_best64_init(double *d_best_dist, int64_t *d_best_idx, int64_t n_img, void *stream);
+int spf_argmin_rows_f64(const double *d_dist, int64_t n_img, int64_t n_ref, int64_t ref_offset,
+                        double *d_best_dist, int64_t *d_best_idx, void *stream);
 
 /* ---- autocorrelation merge: operator and device-resident CG -----------
  * Replaces Merge.setup_linops / W_matvec / cg
@@ -411,21 +463,24 @@ int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img, const void *d_r
                         int64_t chunk_frames, int32_t *h_idx, float *h_dist, int64_t *h_stats,
                         void *stream);
 
-/* Matching for callers that cannot allocate device memory: code that records
- * its work inside a CUDA stream capture (an allocation breaks the capture)
- * and online data-acquisition processes that fix their GPU memory at start-up.
+/* Matching for callers that cannot allocate device memory: online
+ * data-acquisition processes that fix their GPU memory when they start and
+ * must not allocate while frames stream in, and plug-ins hosted by an
+ * application whose own allocator owns the device's memory.
  * No counterpart in the reference.  Same result as spf_dist_topk_bf16 +
  * spf_rerank_fp32 (best index, exact FP32 distance, uncertified flags; the
  * caller completes uncertified frames), but all scratch lives in a static
- * device array of the library: 16 MiB + 64 KiB held by every GPU that loads
- * the library until the process exits.  Limits per call: n_img <=
+ * device array of the library: 16 MiB + 16 KiB + 256 B held by every GPU
+ * that loads the library until the process exits.  Limits per call: n_img <=
  * SPF_STATIC_MAX_FRAMES and ceil(n_ref/256) * n_img <=
  * SPF_STATIC_MAX_TILE_FRAMES; larger calls are rejected with SPF_ERR_ARG.
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) and sets the kernel's shared-memory limit; make it
  * before any stream capture.  It calls no cudaMalloc or cudaFree.  All calls
  * on a device share the array: calls that overlap on the GPU race, so
- * serialise them. */
+ * serialise them.  If a bounded device wait of the tensor-core kernel gives
+ * up, every frame of the call comes back void (d_idx -1, d_dist NaN,
+ * d_uncertified 1) and spf_device_error reports the code. */
 #define SPF_STATIC_MAX_FRAMES 4096
 #define SPF_STATIC_MAX_TILE_FRAMES 262144
 int spf_match_bf16_static(const void *d_img_bf16, const float *d_img, const float *d_img_sq,

@@ -155,6 +155,22 @@ SIGNATURES = {
     "spf_match_bf16_host": [_c_void_p, _i64, _c_void_p, _c_void_p, _c_void_p, _c_void_p,
                             ctypes.c_float, _i64, _i64, _i64, _i64, _c_void_p, _c_void_p,
                             _c_void_p, _c_void_p],
+    "spf_nufft64_plan_create": [_int, _int, _int, _dbl, _dbl, ctypes.POINTER(_c_void_p)],
+    "spf_nufft64_plan_destroy": [_c_void_p],
+    "spf_nufft64_plan_info": [_c_void_p, ctypes.POINTER(_int), ctypes.POINTER(_int),
+                              ctypes.POINTER(_dbl), ctypes.POINTER(_int)],
+    "spf_nufft64_t2_set_modes": [_c_void_p, _c_void_p, _c_void_p, _int, _int, _c_void_p],
+    "spf_nufft64_t2_interp": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _i64, _c_void_p,
+                              _c_void_p, _c_void_p],
+    "spf_slice_t2_f64": [_c_void_p, _c_void_p, _i64, _c_void_p, _i64, _dbl, _c_void_p,
+                         _c_void_p],
+    "spf_nufft64_t1_zero": [_c_void_p, _c_void_p],
+    "spf_nufft64_t1_spread": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _i64,
+                              _c_void_p],
+    "spf_nufft64_t1_finish": [_c_void_p, _int, _c_void_p, _c_void_p, _c_void_p],
+    "spf_dist_f64": [_c_void_p, _c_void_p, _i64, _i64, _i64, _c_void_p, _c_void_p],
+    "spf_best64_init": [_c_void_p, _c_void_p, _i64, _c_void_p],
+    "spf_argmin_rows_f64": [_c_void_p, _i64, _i64, _i64, _c_void_p, _c_void_p, _c_void_p],
     "spf_phase_create": [_int, ctypes.POINTER(_c_void_p)],
     "spf_phase_destroy": [_c_void_p],
     "spf_phase_set_ac": [_c_void_p, _c_void_p, _c_void_p],

@@ -5,11 +5,11 @@ forward(ugrid, H_, K_, L_, support, use_recip_sym, N)      :32-61
 adjoint(nuvect, H_, K_, L_, M, use_recip_sym=True, support=None)  :97-128
 gen_nonuniform_positions / gen_nonuniform_normalized_positions   :290-323
 
-The NUFFT runs on the GPU (libspinifel_gb300) in FP32 at tolerance `eps`
-(the reference asks finufft for 1e-12 in double precision; the FP32 kernels
-resolve about 1e-7, and the default here is the 1e-6 the GB300 path is
-specified at).  Inputs may be numpy arrays (results come back as numpy) or
-CUDA tensors (results stay on the device).
+The NUFFT runs on the GPU (libspinifel_gb300) at tolerance `eps`: FP32
+kernels from the default 1e-6 (the GB300 path's specified tolerance) down to
+about 1e-7, FP64 kernels below that, down to the 1e-12 in double that the
+reference asks finufft for.  Inputs may be numpy arrays (results come back
+as numpy) or CUDA tensors (results stay on the device).
 """
 from __future__ import annotations
 
@@ -17,7 +17,7 @@ import numpy as np
 import torch
 
 from . import _arrays, geom
-from .nufft import NufftPlan
+from .nufft import NufftPlan, make_plan
 
 DEFAULT_EPS = 1e-6
 _plans: dict = {}
@@ -28,7 +28,7 @@ def plan_for(M, eps=DEFAULT_EPS) -> NufftPlan:
     key = (m, float(eps), torch.cuda.current_device())
     p = _plans.get(key)
     if p is None:
-        p = NufftPlan(m, eps)
+        p = make_plan(m, eps)
         _plans[key] = p
     return p
 
@@ -52,11 +52,12 @@ def forward(ugrid, H_, K_, L_, support, use_recip_sym, N, eps=DEFAULT_EPS):
         else:
             assert np.all(np.isreal(ugrid))
     g = _arrays.to_dev(ugrid.real if _arrays.is_torch(ugrid) and torch.is_complex(ugrid)
-                       else (np.real(ugrid) if not _arrays.is_torch(ugrid) else ugrid))
+                       else (np.real(ugrid) if not _arrays.is_torch(ugrid) else ugrid),
+                       torch.float64)
     P = plan_for(g.shape, eps)
     P.set_modes(g, support, isign=-1, want_imag=True)
-    x, y, z = (_arrays.to_dev(np.asarray(a).reshape(-1) if not _arrays.is_torch(a) else a)
-               for a in (H_, K_, L_))
+    x, y, z = (_arrays.to_dev(np.asarray(a).reshape(-1) if not _arrays.is_torch(a) else a,
+                              torch.float64) for a in (H_, K_, L_))
     re, im = P.interp(x, y, z, want_imag=True)
     out = torch.complex(re, im)
     assert out.numel() == N
@@ -77,13 +78,14 @@ def adjoint(nuvect, H_, K_, L_, M, use_recip_sym=True, support=None, eps=DEFAULT
     if _numel(H_):
         assert _max_abs(H_, K_, L_) < 3 * np.pi
     P = plan if plan is not None else plan_for(M, eps)
-    x, y, z = (_arrays.to_dev(np.asarray(a).reshape(-1) if not _arrays.is_torch(a) else a)
-               for a in (H_, K_, L_))
+    x, y, z = (_arrays.to_dev(np.asarray(a).reshape(-1) if not _arrays.is_torch(a) else a,
+                              P.dtype) for a in (H_, K_, L_))
     c = nuvect if _arrays.is_torch(nuvect) else torch.as_tensor(np.asarray(nuvect))
     c = c.to(_arrays.device()).reshape(-1)
-    cre = (c.real if torch.is_complex(c) else c).to(torch.float32).contiguous()
-    cim = c.imag.to(torch.float32).contiguous() if torch.is_complex(c) else None
+    cre = (c.real if torch.is_complex(c) else c).to(P.dtype).contiguous()
+    cim = c.imag.to(P.dtype).contiguous() if torch.is_complex(c) else None
     use_sorted = (x.numel() >= SORTED_SPREAD_MIN_POINTS) if sort is None else bool(sort)
+    use_sorted = use_sorted and P.supports_sort
     if use_sorted:
         P.sort_points(x, y, z)
 
@@ -104,7 +106,7 @@ def adjoint(nuvect, H_, K_, L_, M, use_recip_sym=True, support=None, eps=DEFAULT
         re = fr_re - fi_im
         im = fr_im + fi_re
     if support is not None:
-        s = _arrays.to_dev(support) if not isinstance(support, (int, float)) else support
+        s = _arrays.to_dev(support, P.dtype) if not isinstance(support, (int, float)) else support
         re = re * s
         im = im * s
     out = re if use_recip_sym else torch.complex(re, im)

@@ -111,13 +111,20 @@ int spf_device_error(void *stream, int *h_code) {
     spf::set_error("spf_device_error: no device error word");
     return SPF_ERR_CUDA;
   }
-  unsigned int v = 0;
+  unsigned int v = 0, sv = 0;
   cudaStream_t s = spf::as_stream(stream);
+  // the static matching path keeps its own word (it may not allocate)
+  unsigned int *ws = spf::static_match_error_word();
   SPF_TRY(spf::check_cuda(cudaMemcpyAsync(&v, w, sizeof(v), cudaMemcpyDeviceToHost, s),
                           "spf_device_error"));
+  if (ws)
+    SPF_TRY(spf::check_cuda(cudaMemcpyAsync(&sv, ws, sizeof(sv), cudaMemcpyDeviceToHost, s),
+                            "spf_device_error"));
   SPF_TRY(spf::check_cuda(cudaStreamSynchronize(s), "spf_device_error"));
   SPF_TRY(spf::check_cuda(cudaMemsetAsync(w, 0, sizeof(unsigned int), s), "spf_device_error"));
-  *h_code = (int)v;
+  if (ws)
+    SPF_TRY(spf::check_cuda(cudaMemsetAsync(ws, 0, sizeof(unsigned int), s), "spf_device_error"));
+  *h_code = (int)(v ? v : sv);
   return SPF_OK;
 }
 

@@ -25,6 +25,10 @@ inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_o
 
 // Device-side error word (per device; bounded waits write codes here).
 unsigned int *device_error_word();
+// The error word of the matching path without device allocation
+// (spf_match_bf16_static) on the current device; NULL until that path has
+// been set up on it.
+unsigned int *static_match_error_word();
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 

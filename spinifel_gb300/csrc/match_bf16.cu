@@ -618,7 +618,7 @@ __global__ void __launch_bounds__(RX_THREADS)
     k_rerank_exact(const float *__restrict__ cand_d, const int32_t *__restrict__ cand_i,
                    const float *__restrict__ img, const float *__restrict__ img_sq,
                    int64_t n_img, const float *__restrict__ ref, const float *__restrict__ ref_sq,
-                   float ref_sq_max, int64_t n_pix, int64_t ref_offset,
+                   int64_t n_ref, float ref_sq_max, int64_t n_pix, int64_t ref_offset,
                    float *__restrict__ work, int32_t *__restrict__ out_idx,
                    float *__restrict__ out_dist, int32_t *__restrict__ uncertified,
                    int32_t *__restrict__ out_top) {
@@ -638,7 +638,9 @@ __global__ void __launch_bounds__(RX_THREADS)
       if (im < n_img) {
         int32_t j = cand_i[(size_t)im * TOPK + (q % TOPK)];
         float band = cert_band(work[im], img_sq[im], ref_sq_max, n_pix);
-        if (j != INT32_MAX && !rerank_skip(cand_d, im, q % TOPK, band))
+        // an index outside [0, n_ref) (a candidate slot the GEMM did not
+        // write) is never read
+        if (j >= 0 && j < n_ref && !rerank_skip(cand_d, im, q % TOPK, band))
           ptr = ref + (int64_t)j * n_pix;
       }
     }
@@ -716,7 +718,7 @@ __global__ void __launch_bounds__(RX_THREADS)
   int32_t j = cand_i[(size_t)imc * TOPK + c];
   float x2 = live ? img_sq[imc] : 0.0f;
   const float band = live ? cert_band(work[imc], x2, ref_sq_max, n_pix) : 0.0f;
-  const bool valid = live && j != INT32_MAX && !rerank_skip(cand_d, imc, c, band);
+  const bool valid = live && j >= 0 && j < n_ref && !rerank_skip(cand_d, imc, c, band);
   float dist = valid ? __fsub_rn(__fadd_rn(x2, ref_sq[j]), __fmul_rn(2.0f, acc))
                      : __int_as_float(0x7f800000);
   int32_t jj = valid ? j : INT32_MAX;
@@ -1263,8 +1265,8 @@ static int rerank_impl(const char *name, float *d_cand_d, int32_t *d_cand_i, int
   SPF_TRY(check_launch("k_merge_top8"));
   SPF_TRY(rerank_smem_attr());
   k_rerank_exact<<<(unsigned)((n_img + RX_FRAMES - 1) / RX_FRAMES), RX_THREADS, RX_SMEM, s>>>(
-      d_mrg_d, d_mrg_i, d_img, d_img_sq, n_img, d_ref, d_ref_sq, ref_sq_max, n_pix, ref_offset,
-      d_work, d_idx, d_dist, d_uncertified, d_top8);
+      d_mrg_d, d_mrg_i, d_img, d_img_sq, n_img, d_ref, d_ref_sq, n_ref, ref_sq_max, n_pix,
+      ref_offset, d_work, d_idx, d_dist, d_uncertified, d_top8);
   return check_launch("k_rerank_exact");
 }
 
@@ -1334,11 +1336,15 @@ int spf_row_norms_f32(const float *d_x, int64_t n_rows, int64_t n_pix, float *d_
 // candidate buffer, the re-rank work area and the device error word) in the
 // file-scope array below instead of caller- or library-allocated memory.
 // The array is part of this library's device image: every GPU that loads the
-// library holds it (16 MiB + 64 KiB) until the process exits.  All calls on a
-// device share it and it keeps the last call's contents, so calls that overlap
-// on the GPU (different streams, or different host threads) race; serialise
-// them.  Every byte a call reads is written earlier in the same call except
-// the error word, which the call clears first.
+// library holds it (STATIC_SCRATCH_BYTES = 2 x 8 MiB of candidates + 16 KiB of
+// per-frame work + 256 B for the error word) until the process exits.  All
+// calls on a device share it and it keeps the last call's contents, so calls
+// that overlap on the GPU (different streams, or different host threads)
+// race; serialise them.  The call clears the error word first; the GEMM then
+// writes every candidate slot the re-rank reads, unless a bounded wait gives
+// up, in which case the re-rank skips indices outside [0, n_ref), the call's
+// outputs are marked void (idx -1, distance NaN, uncertified 1) and the error
+// word keeps the code for spf_device_error.
 // ---------------------------------------------------------------------------
 namespace spf {
 namespace bf16mm {
@@ -1350,6 +1356,20 @@ constexpr size_t STATIC_WORK_BYTES = (size_t)STATIC_MAX_FRAMES * 4;
 constexpr size_t STATIC_SCRATCH_BYTES = 2 * STATIC_CAND_BYTES + STATIC_WORK_BYTES + 256;
 
 static __device__ __align__(256) unsigned char g_match_scratch[STATIC_SCRATCH_BYTES];
+
+// After a GEMM that gave up a bounded wait (*err != 0): idx -1, distance
+// NaN and uncertified for every frame of the call.
+__global__ void k_static_abort_mark(const unsigned int *__restrict__ err, int64_t n_img,
+                                    int32_t *__restrict__ idx, float *__restrict__ dist,
+                                    int32_t *__restrict__ unc) {
+  if (*err == 0u) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_img;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    idx[i] = -1;
+    if (dist) dist[i] = __int_as_float(0x7fc00000);
+    if (unc) unc[i] = 1;
+  }
+}
 
 // Device address of g_match_scratch per device, looked up once with the
 // device current (host code cannot use the symbol itself as an address).
@@ -1380,6 +1400,19 @@ static int static_scratch(int dev, unsigned char **out) {
 }
 
 }  // namespace bf16mm
+
+// The static path's error word on the current device, or NULL while no
+// static call has set the path up on it (read by spf_device_error).
+unsigned int *static_match_error_word() {
+  using namespace bf16mm;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_ptr[dev]) return nullptr;
+  return reinterpret_cast<unsigned int *>(g_static_ptr[dev] + 2 * STATIC_CAND_BYTES +
+                                          STATIC_WORK_BYTES);
+}
+
 }  // namespace spf
 
 extern "C" int spf_match_bf16_static(const void *d_img_bf16, const float *d_img,
@@ -1443,7 +1476,12 @@ extern "C" int spf_match_bf16_static(const void *d_img_bf16, const float *d_img,
   SPF_TRY(check_launch("k_merge_top8 (static scratch)"));
   SPF_TRY(rerank_smem_attr());
   k_rerank_exact<<<(unsigned)((n_img + RX_FRAMES - 1) / RX_FRAMES), RX_THREADS, RX_SMEM, s>>>(
-      cand_d, cand_i, d_img, d_img_sq, n_img, d_ref, d_ref_sq, ref_sq_max, n_pix, 0, work, d_idx,
-      d_dist, d_uncertified, nullptr);
-  return check_launch("k_rerank_exact (static scratch)");
+      cand_d, cand_i, d_img, d_img_sq, n_img, d_ref, d_ref_sq, n_ref, ref_sq_max, n_pix, 0, work,
+      d_idx, d_dist, d_uncertified, nullptr);
+  SPF_TRY(check_launch("k_rerank_exact (static scratch)"));
+  // a GEMM that gave up a bounded wait left candidate slots unwritten: the
+  // call's answers are then void, and every frame says so
+  k_static_abort_mark<<<grid_for(n_img, 256, 1024), 256, 0, s>>>(err, n_img, d_idx, d_dist,
+                                                                d_uncertified);
+  return check_launch("k_static_abort_mark");
 }

@@ -251,6 +251,51 @@ __global__ void k_best_unpack(const unsigned long long *__restrict__ best, int64
   }
 }
 
+// FP64 running argmin over the rows of a distance block [n_img][n_ref]: one
+// warp per image; the lowest column wins ties within the block, and the
+// running best changes only on a strictly smaller distance (earlier blocks
+// hold lower reference indices), as argmin over the whole row would.
+__global__ void k_argmin_rows_f64(const double *__restrict__ dist, int64_t n_img, int64_t n_ref,
+                                  int64_t ref_offset, double *__restrict__ best_dist,
+                                  int64_t *__restrict__ best_idx) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n_img;
+       i += nwarps) {
+    const double *row = dist + i * n_ref;
+    double bd = INFINITY;
+    int64_t bi = -1;
+    for (int64_t r = lane; r < n_ref; r += 32) {
+      const double d = row[r];
+      if (d < bd) {  // lanes walk their columns in increasing order
+        bd = d;
+        bi = r;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+      const double od = __shfl_xor_sync(0xffffffffu, bd, o);
+      const int64_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (oi >= 0 && (bi < 0 || od < bd || (od == bd && oi < bi))) {
+        bd = od;
+        bi = oi;
+      }
+    }
+    if (lane == 0 && bi >= 0 && (best_idx[i] < 0 || bd < best_dist[i])) {
+      best_dist[i] = bd;
+      best_idx[i] = bi + ref_offset;
+    }
+  }
+}
+
+__global__ void k_best64_init(double *best_dist, int64_t *best_idx, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    best_dist[i] = INFINITY;
+    best_idx[i] = -1;
+  }
+}
+
 // sum of squares per row (FP64 accumulation, one warp per row)
 __global__ void k_row_sqnorm(const float *__restrict__ x, int64_t n_rows, int64_t n_pix,
                              float *__restrict__ out) {
@@ -624,6 +669,39 @@ int spf_dist_argmin_fp32(const float *d_img, const float *d_img_sq, int64_t n_im
   SPF_TRY(spf_dist_argmin_f32(d_img, d_img_sq, n_img, d_ref, d_ref_sq, n_ref, n_pix, 0, d_best,
                               stream));
   return spf_best_unpack(d_best, n_img, d_idx, d_dist, stream);
+}
+
+int spf_dist_f64(const double *d_ref, const double *d_data, int64_t n_ref, int64_t n_data,
+                 int64_t n_pix, double *d_out, void *stream) {
+  SPF_REQUIRE(n_ref >= 0 && n_data >= 0 && n_pix >= 0, "spf_dist_f64: negative size");
+  if (n_ref == 0 || n_data == 0) return SPF_OK;
+  SPF_REQUIRE(d_ref && d_data && d_out, "spf_dist_f64: NULL pointer");
+  const int64_t tiles = ((n_data + TB_M - 1) / TB_M) * ((n_ref + TB_N - 1) / TB_N);
+  SPF_REQUIRE(tiles < (1LL << 31), "spf_dist_f64: too many tiles");
+  const int group_m = (int)tune_get(SPF_TUNE_FP32_GROUP_M, GROUP_M);
+  k_knn_eudist<double><<<(unsigned)tiles, TB_THREADS, 0, as_stream(stream)>>>(
+      d_ref, d_data, n_ref, n_data, n_pix, n_pix, d_out, group_m);
+  return check_launch("spf_dist_f64");
+}
+
+int spf_best64_init(double *d_best_dist, int64_t *d_best_idx, int64_t n_img, void *stream) {
+  SPF_REQUIRE(n_img >= 0, "spf_best64_init: negative size");
+  if (n_img == 0) return SPF_OK;
+  SPF_REQUIRE(d_best_dist && d_best_idx, "spf_best64_init: NULL pointer");
+  k_best64_init<<<grid_for(n_img, 256, 4096), 256, 0, as_stream(stream)>>>(d_best_dist,
+                                                                           d_best_idx, n_img);
+  return check_launch("spf_best64_init");
+}
+
+int spf_argmin_rows_f64(const double *d_dist, int64_t n_img, int64_t n_ref, int64_t ref_offset,
+                        double *d_best_dist, int64_t *d_best_idx, void *stream) {
+  SPF_REQUIRE(n_img >= 0 && n_ref >= 0 && ref_offset >= 0, "spf_argmin_rows_f64: negative size");
+  if (n_img == 0 || n_ref == 0) return SPF_OK;
+  SPF_REQUIRE(d_dist && d_best_dist && d_best_idx, "spf_argmin_rows_f64: NULL pointer");
+  k_argmin_rows_f64<<<grid_for(n_img * 32, 256, (int64_t)sm_count() * 16), 256, 0,
+                      as_stream(stream)>>>(d_dist, n_img, n_ref, ref_offset, d_best_dist,
+                                           d_best_idx);
+  return check_launch("spf_argmin_rows_f64");
 }
 
 }  // extern "C"

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "es_params.cuh"
 
 struct spf_nufft_plan_s {
   int dev = 0;
@@ -47,79 +48,17 @@ struct spf_nufft_plan_s {
 
 namespace spf {
 
-static int next_smooth_even(int n) {
-  if (n < 2) n = 2;
-  if (n & 1) ++n;
-  for (;; n += 2) {
-    int m = n;
-    for (int p : {2, 3, 5})
-      while (m % p == 0) m /= p;
-    if (m == 1) return n;
-  }
-}
+static int next_smooth_even(int n) { return es_next_smooth_even(n); }
 
-// Gauss-Legendre nodes/weights on [-1, 1] by Newton iteration on P_q.
-static void gauss_legendre(int q, std::vector<double> &x, std::vector<double> &wt) {
-  x.assign(q, 0.0);
-  wt.assign(q, 0.0);
-  for (int i = 0; i < q; ++i) {
-    double z = cos(M_PI * (i + 0.75) / (q + 0.5));
-    double dp = 1.0;
-    for (int it = 0; it < 100; ++it) {
-      double p0 = 1.0, p1 = z;
-      for (int k = 2; k <= q; ++k) {
-        double pk = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
-        p0 = p1;
-        p1 = pk;
-      }
-      dp = q * (z * p1 - p0) / (z * z - 1.0);
-      double dz = p1 / dp;
-      z -= dz;
-      if (fabs(dz) < 1e-15) break;
-    }
-    x[i] = z;
-    wt[i] = 2.0 / ((1.0 - z * z) * dp * dp);
-  }
-}
+// FP32 cannot resolve tolerances finer than w = 8 (the FP64 plan of
+// nufft_f64.cu serves those)
+static int es_width(double eps, double sigma) { return es_width_for(eps, sigma, 3, 8); }
 
-static int es_width(double eps, double sigma) {
-  int w;
-  if (sigma == 2.0) {
-    w = (int)ceil(-log10(eps / 10.0));
-  } else {
-    w = (int)ceil(log(1.0 / eps) / (M_PI * sqrt(1.0 - 1.0 / sigma)));
-  }
-  if (w < 3) w = 3;
-  if (w > 8) w = 8;  // FP32 cannot resolve finer tolerances
-  return w;
-}
+static double es_beta(int w, double sigma) { return es_beta_for(w, sigma); }
 
-static double es_beta(int w, double sigma) {
-  if (sigma == 2.0) {
-    double bon = (w == 2) ? 2.20 : (w == 3) ? 2.26 : (w == 4) ? 2.38 : 2.30;
-    return bon * w;
-  }
-  return 0.97 * M_PI * w * (1.0 - 1.0 / (2.0 * sigma));
-}
-
-// 1 / p(k), p(k) = int_{-w/2}^{w/2} phi(2t/w) cos(k h t) dt, h = 2 pi / n.
 static std::vector<float> inverse_kernel_ft(int m, int n, int w, double beta) {
-  std::vector<double> xq, wq;
-  gauss_legendre(4 * w + 40, xq, wq);
-  std::vector<float> out(m);
-  double h = 2.0 * M_PI / n;
-  for (int i = 0; i < m; ++i) {
-    double k = (double)(i - m / 2);
-    double s = 0.0;
-    for (size_t q = 0; q < xq.size(); ++q) {
-      double t = 0.25 * w * (xq[q] + 1.0);
-      double z = 2.0 * t / w;
-      double phi = exp(beta * (sqrt(fmax(1.0 - z * z, 0.0)) - 1.0));
-      s += 0.25 * w * wq[q] * phi * cos(k * h * t);
-    }
-    out[i] = (float)(1.0 / (2.0 * s));
-  }
-  return out;
+  std::vector<double> d = es_inverse_kernel_ft(m, n, w, beta);
+  return std::vector<float>(d.begin(), d.end());
 }
 
 // ---------------------------------------------------------------------------

@@ -14,6 +14,13 @@ batch to the device per call; here the reference quaternions and the pixel
 positions live on the device and the kernel rotates each pixel itself.
 Reference orientations come from a seeded uniform sampler (skopi is not
 available), or are passed in.
+
+Precision follows the reference's settings: with use_single_prec (the
+default) the NUFFTs run in FP32 at eps = 1e-6; without it they run in FP64 at
+the reference's own eps = 1e-12 (nufft_ext.py:62) and the slices come back
+in float64, as the reference's f_type = float64 run has them
+(sequential/orientation_matching.py:32-36).  An explicit eps overrides this
+(below 1e-7 the FP64 kernels are used).
 """
 from __future__ import annotations
 
@@ -21,21 +28,25 @@ import numpy as np
 import torch
 
 from .. import _arrays, geom
-from ..nufft import NufftPlan
+from ..nufft import FP32_EPS_FLOOR, make_plan
 
 DEFAULT_EPS = 1e-6
+REFERENCE_EPS = 1e-12
 
 
 class NUFFT:
     def __init__(self, settings, pixel_position_reciprocal, pixel_distance_reciprocal,
-                 images_per_rank=None, ref_orientations=None, eps=DEFAULT_EPS, seed=None):
+                 images_per_rank=None, ref_orientations=None, eps=None, seed=None):
         self.N_orientations = settings.N_orientations
         self.N_batch_size = settings.N_batch_size
         self.reduced_det_shape = tuple(settings.reduced_det_shape)
         self.oversampling = settings.oversampling
         self.N_pixels = int(np.prod(self.reduced_det_shape))
         self.N_images = settings.N_images_per_rank if images_per_rank is None else images_per_rank
-        self.eps = eps
+        if eps is None:
+            eps = DEFAULT_EPS if getattr(settings, "use_single_prec", True) else REFERENCE_EPS
+        self.eps = float(eps)
+        self.fp64 = self.eps < FP32_EPS_FLOOR
         self.isign = -1
         ppr = np.asarray(pixel_position_reciprocal, dtype=np.float64)
         self.pixel_position_reciprocal = ppr
@@ -51,13 +62,22 @@ class NUFFT:
         dev = _arrays.device()
         self._quats = torch.as_tensor(self.ref_orientations, dtype=torch.float32, device=dev)
         self._ppr = torch.as_tensor(ppr.reshape(3, -1), dtype=torch.float32, device=dev)
+        if self.fp64:
+            self._quats64 = torch.as_tensor(self.ref_orientations, dtype=torch.float64,
+                                            device=dev)
+            self._ppr64 = torch.as_tensor(ppr.reshape(3, -1), dtype=torch.float64, device=dev)
         self._plans = {}
 
-    def plan(self, M) -> NufftPlan:
+    @property
+    def dtype(self):
+        """Device dtype of the slices: float64 at the reference's eps."""
+        return torch.float64 if self.fp64 else torch.float32
+
+    def plan(self, M):
         m = (M, M, M) if np.ndim(M) == 0 else tuple(M)
         p = self._plans.get(m)
         if p is None:
-            p = self._plans[m] = NufftPlan(m, self.eps)
+            p = self._plans[m] = make_plan(m, self.eps)
         return p
 
     def update_fields(self, n_images_per_rank):
@@ -70,13 +90,16 @@ class NUFFT:
             g = g.real
         elif not _arrays.is_torch(g):
             g = np.real(g)
-        g = _arrays.to_dev(g)
+        g = _arrays.to_dev(g, self.dtype)
         P = self.plan(g.shape)
         P.set_modes(g, support, isign=self.isign, want_imag=False)
         return P
 
-    def slice_real(self, P: NufftPlan, st: int, en: int, out=None, out_bf16=None):
-        """Real part of the type 2 at reference orientations st:en, [en-st, N_pixels]."""
+    def slice_real(self, P, st: int, en: int, out=None, out_bf16=None):
+        """Real part of the type 2 at reference orientations st:en, [en-st, N_pixels]
+        (float64 from an FP64 plan)."""
+        if P.dtype == torch.float64:
+            return P.slice(self._quats64[st:en], self._ppr64, self.mult, out=out)
         det = self.reduced_det_shape if len(self.reduced_det_shape) == 3 else None
         return P.slice(self._quats[st:en], self._ppr, self.mult, out=out, out_bf16=out_bf16,
                        det_shape=det)
@@ -88,11 +111,12 @@ class NUFFT:
             else:
                 assert np.all(np.isreal(ugrid))
         g = _arrays.to_dev(ugrid.real if _arrays.is_torch(ugrid) and torch.is_complex(ugrid)
-                           else (np.real(ugrid) if not _arrays.is_torch(ugrid) else ugrid))
+                           else (np.real(ugrid) if not _arrays.is_torch(ugrid) else ugrid),
+                           self.dtype)
         P = self.plan(g.shape)
         P.set_modes(g, support, isign=self.isign, want_imag=True)
         H, K, L = geom.hkl(self.ref_orientations[st:en], self.pixel_position_reciprocal)
-        x, y, z = (torch.as_tensor(a.reshape(-1) * self.mult, dtype=torch.float32,
+        x, y, z = (torch.as_tensor(a.reshape(-1) * self.mult, dtype=self.dtype,
                                    device=g.device) for a in (H, K, L))
         re, im = P.interp(x, y, z, want_imag=True)
         assert re.numel() == N

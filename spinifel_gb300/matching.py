@@ -82,6 +82,66 @@ def argmin_fp32(images: torch.Tensor, refs: torch.Tensor, images_sq=None, refs_s
     return t.result()
 
 
+class BestTracker64:
+    """FP64 running (distance, index) minimum per image across reference
+    batches, for matching at the reference's double precision: each batch's
+    [n_img, n_ref] distance block (dist_f64) is folded in by
+    spf_argmin_rows_f64 (lower index on ties, earlier batches kept on ties)."""
+
+    def __init__(self, n_img: int, device):
+        self.n_img = n_img
+        self.best_dist = torch.empty(n_img, device=device, dtype=torch.float64)
+        self.best_idx = torch.empty(n_img, device=device, dtype=torch.int64)
+        _lib.call("spf_best64_init", _lib.ptr(self.best_dist), _lib.ptr(self.best_idx), n_img,
+                  _lib.stream_handle())
+
+    def update_block(self, dist: torch.Tensor, ref_offset: int):
+        _lib.require_cuda(dist, "dist", torch.float64)
+        if dist.dim() != 2 or dist.shape[0] != self.n_img:
+            raise ValueError("dist must be [n_img, n_ref]")
+        _lib.call("spf_argmin_rows_f64", _lib.ptr(dist), dist.shape[0], dist.shape[1],
+                  int(ref_offset), _lib.ptr(self.best_dist), _lib.ptr(self.best_idx),
+                  _lib.stream_handle())
+
+    def update_fp64(self, img, ref, ref_offset: int, work: torch.Tensor | None = None):
+        """Fold the distances of img [n_img, n_pix] to ref [n_ref, n_pix]."""
+        self.update_block(dist_f64(ref, img, out=work), ref_offset)
+
+    def result(self):
+        return self.best_idx, self.best_dist
+
+
+def dist_f64(ref: torch.Tensor, data: torch.Tensor, out: torch.Tensor | None = None):
+    """[n_data, n_ref] sums over all pixels of (data - ref)^2 in FP64."""
+    _lib.require_cuda(ref, "ref", torch.float64)
+    _lib.require_cuda(data, "data", torch.float64)
+    if ref.shape[0] and data.shape[0] and ref[0].numel() != data[0].numel():
+        raise ValueError("images and references have different pixel counts")
+    n_pix = data[0].numel() if data.shape[0] else (ref[0].numel() if ref.shape[0] else 0)
+    if out is None:
+        out = torch.empty(data.shape[0], ref.shape[0], device=ref.device, dtype=torch.float64)
+    _lib.require_cuda(out, "out", torch.float64)
+    if out.numel() != data.shape[0] * ref.shape[0]:
+        raise ValueError("out has the wrong size")
+    _lib.call("spf_dist_f64", _lib.ptr(ref), _lib.ptr(data), ref.shape[0], data.shape[0], n_pix,
+              _lib.ptr(out), _lib.stream_handle())
+    return out.view(data.shape[0], ref.shape[0])
+
+
+def argmin_fp64(images: torch.Tensor, refs: torch.Tensor, batch: int = 4096):
+    """Index (int64) and FP64 distance of the nearest reference for every
+    image, references taken in batches of `batch` rows."""
+    t = BestTracker64(images.shape[0], images.device)
+    work = None
+    for st in range(0, refs.shape[0], batch):
+        blk = refs[st:st + batch]
+        if work is None or work.numel() != images.shape[0] * blk.shape[0]:
+            work = torch.empty(images.shape[0] * blk.shape[0], device=images.device,
+                               dtype=torch.float64)
+        t.update_fp64(images, blk, st, work)
+    return t.result()
+
+
 def knn_eudist(ref: torch.Tensor, data: torch.Tensor) -> torch.Tensor:
     """[n_data, n_ref] sum over the first 16*floor(P/16) pixels of (d - r)^2."""
     if ref.dtype != data.dtype:

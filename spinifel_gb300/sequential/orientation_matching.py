@@ -13,6 +13,13 @@ x2 + s2 - 2 x.s into a per-image running (distance, index) minimum with the
 plain FP32 distance kernel (:98-109, :179), so the N_orientations x N_slices
 distance matrix is never stored.  Ties go to the lower orientation index, as
 argmin(axis=0) does.
+
+With a NUFFT at the reference's own tolerance (settings.use_single_prec
+False, or an explicit eps below 1e-7) the same steps run in FP64, as the
+reference's float64 run does (f_type, :32-36): FP64 slicing at eps 1e-12,
+the std rescale in double and FP64 distances folded per batch into an FP64
+running minimum, so the argmin is the reference's own up to ties at the
+rounding level of double.
 """
 from __future__ import annotations
 
@@ -42,17 +49,36 @@ class SNM:
         assert tuple(slices_.shape) == (self.N_slices,) + self.reduced_det_shape
         self.reciprocal_extent = float(np.max(pixel_distance_reciprocal))
         self.pixel_position_reciprocal = pixel_position_reciprocal
-        self.slices_ = _arrays.to_dev(slices_).reshape(self.N_slices, self.N_pixels)
-        self.slices_2 = matching.row_sqnorm(self.slices_) if self.N_slices else None
-        self.slices_std = (self.slices_.double().std(unbiased=False).float()
-                           if self.N_slices else None)
+        self.fp64 = bool(getattr(nufft, "fp64", False))
+        dt = torch.float64 if self.fp64 else torch.float32
+        self.slices_ = _arrays.to_dev(slices_, dt).reshape(self.N_slices, self.N_pixels)
+        if self.fp64:
+            self.slices_2 = None
+            self.slices_std = self.slices_.std(unbiased=False) if self.N_slices else None
+        else:
+            self.slices_2 = matching.row_sqnorm(self.slices_) if self.N_slices else None
+            self.slices_std = (self.slices_.double().std(unbiased=False).float()
+                               if self.N_slices else None)
         self.nufft = nufft
         self.timings = {}
 
     def match_indices(self, ac) -> torch.Tensor:
-        """Best reference orientation index per image (device int32)."""
+        """Best reference orientation index per image (device int32; int64
+        in FP64 mode)."""
         P = self.nufft.set_model(ac, 1)
         B = self.N_batch_size
+        if self.fp64:
+            buf = torch.empty(B, self.N_pixels, device=self.slices_.device, dtype=torch.float64)
+            work = torch.empty(self.N_slices * B, device=self.slices_.device,
+                               dtype=torch.float64)
+            best = matching.BestTracker64(self.N_slices, self.slices_.device)
+            for i in range(self.N_orientations // B):
+                st = i * B
+                self.nufft.slice_real(P, st, st + B, out=buf)
+                buf *= self.slices_std / buf.std(unbiased=False)
+                best.update_fp64(self.slices_, buf, st, work)
+            idx, _ = best.result()
+            return idx
         buf = torch.empty(B, self.N_pixels, device=self.slices_.device, dtype=torch.float32)
         best = matching.BestTracker(self.N_slices, self.slices_.device)
         for i in range(self.N_orientations // B):
@@ -95,12 +121,12 @@ def slicing_and_match(ac, slices_, pixel_position_reciprocal, pixel_distance_rec
                   ref_orientations=ref_orientations)
     P = nufft.set_model(ac, 1)
     model_slices = torch.empty(N_orientations, N_pixels, device=nufft._quats.device,
-                               dtype=torch.float32)
+                               dtype=nufft.dtype)
     for i in range(N_orientations // N_batch_size):
         st = i * N_batch_size
         nufft.slice_real(P, st, st + N_batch_size, out=model_slices[st:st + N_batch_size])
-    data = _arrays.to_dev(np.asarray(slices_).reshape(N_slices, N_pixels))
+    data = _arrays.to_dev(np.asarray(slices_).reshape(N_slices, N_pixels), nufft.dtype)
     ratio = data.double().std(unbiased=False) / model_slices.double().std(unbiased=False)
-    model_slices *= ratio.float()
+    model_slices *= ratio.to(nufft.dtype)
     index = nn.nearest_neighbor(model_slices, data, N_batch_size)
     return ref_orientations[index]

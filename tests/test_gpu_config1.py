@@ -1,9 +1,14 @@
 """The CPU-runnable configuration end to end: a 41^3 float64 model, 4 x 32 x 32
 detector, 2,000 reference orientations sliced by type 2 at eps 1e-12 in the
 FP64 oracle, 500 Poisson frames (mean 2 photons/pixel) at other orientations.
-SNM on the GPU (type 2 at eps 1e-6, plain FP32 and bf16 + re-rank) must give
-the oracle's argmin (identical, or a tie within 1e-6 relative of the oracle
-distances)."""
+
+* SNM at the reference's precision (use_single_prec off: FP64 type 2 at eps
+  1e-12, FP64 distances) must give the oracle's argmin on every frame
+  (identical, or a tie within 1e-6 relative of the oracle distances).
+* The fast FP32 path (type 2 at eps 1e-6, plain FP32 and bf16 + re-rank)
+  must give the oracle's argmin on its own FP32 slices; against the eps-1e-12
+  slices it may differ only where the slice error moves two distances across
+  each other (a few percent of frames on this case)."""
 import numpy as np
 import pytest
 import torch
@@ -34,6 +39,28 @@ def case(lib):
     imgs = synth.poisson_images(slices(img_q), 2.0, rng).astype(np.float64)
     ref = slices(ref_q)
     return dict(model=model, ppr=ppr, pdr=pdr, ref_q=ref_q, imgs=imgs, ref=ref)
+
+
+def test_config1_snm_fp64_identical_to_the_oracle(case):
+    from spinifel_gb300 import Settings
+    from spinifel_gb300.extern.nufft_ext import NUFFT
+    from spinifel_gb300.sequential.orientation_matching import SNM
+
+    st = Settings(N_orientations=2000, N_batch_size=500, det_shape=(4, 32, 32), N_clipping=0,
+                  N_binning=0, M_override=41, use_single_prec=False)
+    nufft = NUFFT(st, case["ppr"], case["pdr"], ref_orientations=case["ref_q"])
+    snm = SNM(st, case["imgs"].reshape(500, 4, 32, 32), case["ppr"], case["pdr"], nufft)
+    gidx = snm.match_indices(case["model"]).cpu().numpy()
+    oidx, dist = om.snm_argmin([case["ref"][i:i + 500] for i in range(0, 2000, 500)],
+                               case["imgs"])
+    ok = om.ties_equal(gidx, oidx, dist, rtol=1e-6)
+    assert ok.all(), f"{(~ok).sum()} of 500 frames differ beyond 1e-6 ties"
+
+    # the FP64 slices themselves against the oracle's eps-1e-12 slices
+    P = nufft.set_model(case["model"], 1)
+    raw = nufft.slice_real(P, 0, 500).cpu().numpy()
+    rel = np.linalg.norm(raw - case["ref"][:500]) / np.linalg.norm(case["ref"][:500])
+    assert rel < 1e-10, rel
 
 
 def test_config1_snm_plain_and_bf16_match_the_oracle(case):
@@ -73,7 +100,9 @@ def test_config1_snm_plain_and_bf16_match_the_oracle(case):
     delta = np.abs(dist - dist_g)
     slack = delta[gidx, cols] + delta[oidx, cols] + 1e-5 * dist[oidx, cols]
     assert (dist[gidx, cols] - dist[oidx, cols] <= slack).all()
-    assert (gidx == oidx).mean() > 0.9
+    same = om.ties_equal(gidx, oidx, dist, rtol=1e-6).mean()
+    print(f"FP32 eps-1e-6 path: {same:.3f} of frames equal the eps-1e-12 argmin (ties 1e-6)")
+    assert same > 0.9
 
     # 3) bf16 tensor cores + re-rank on the same scaled slices: the plain
     #    FP32 argmin exactly

@@ -155,6 +155,9 @@ def test_adjoint_dispatch_sorted_spreading_by_size(monkeypatch):
     M = 4
 
     class Rec:
+        dtype = torch.float32
+        supports_sort = True
+
         def __init__(self):
             self.calls = []
 
@@ -173,8 +176,12 @@ def test_adjoint_dispatch_sorted_spreading_by_size(monkeypatch):
         def finish(self, isign, want_imag=False):
             return torch.zeros(M ** 3), torch.zeros(M ** 3)
 
-    def run(n, values, **kw):
-        P = Rec()
+    class Rec64(Rec):  # the FP64 plan has no sorted passes
+        dtype = torch.float64
+        supports_sort = False
+
+    def run(n, values, cls=Rec, **kw):
+        P = cls()
         xyz = [np.zeros(n, dtype=np.float32) for _ in range(3)]
         ac.adjoint(values(n), *xyz, M, plan=P, **kw)
         return P.calls
@@ -187,6 +194,8 @@ def test_adjoint_dispatch_sorted_spreading_by_size(monkeypatch):
     assert run(big, cplx) == ["sort", "zero", "spread_sorted", "zero", "spread_sorted"]
     assert run(10, real, sort=True) == ["sort", "zero", "spread_sorted"]
     assert run(big, real, sort=False) == ["zero", "spread"]
+    assert run(big, real, cls=Rec64) == ["zero", "spread"]
+    assert run(10, real, cls=Rec64, sort=True) == ["zero", "spread"]
 
 
 def test_spread_orient_dispatch_by_size(monkeypatch):

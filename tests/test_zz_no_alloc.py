@@ -1,10 +1,11 @@
 """spf_match_bf16_static: matching for callers that cannot allocate device
-memory (work recorded inside a CUDA stream capture, or a data-acquisition
-process whose GPU memory is fixed at start-up).  Called through the C ABI, it
-must give exactly what the allocating entry points (spf_dist_topk_bf16 +
-spf_rerank_fp32) give, on two calls in a row with different frames, without
-taking device memory after its first call, and must reject sizes beyond its
-static scratch.  This file is collected last on purpose."""
+memory (a data-acquisition process whose GPU memory is fixed at start-up, or
+a plug-in whose host application owns the device memory).  Called through
+the C ABI, it must give exactly what the allocating entry points
+(spf_dist_topk_bf16 + spf_rerank_fp32) give, on two calls in a row with
+different frames, without taking device memory after its first call and
+without a device error, and must reject sizes beyond its static scratch.
+This file is collected last on purpose."""
 import ctypes
 
 import numpy as np
@@ -66,6 +67,11 @@ def test_static_scratch_entry_point_matches_allocating_path(lib):
             free_before = torch.cuda.mem_get_info(dev)[0]
     free_after = torch.cuda.mem_get_info(dev)[0]
     assert free_after == free_before  # no device memory taken by the second call
+    code = ctypes.c_int(-1)
+    _lib.call("spf_device_error", _lib.stream_handle(), ctypes.byref(code))
+    assert code.value == 0  # no bounded wait gave up (the static path's word included)
+    for idx, _, _ in outs:
+        assert bool((idx >= 0).all())  # no frame was marked void
     for fr, (idx, dist, unc) in zip(frames, outs):
         ridx, rdist, runc = _allocating(_lib, fr, rs)
         assert torch.equal(idx, ridx)
