@@ -668,6 +668,48 @@ def run_merge(args):
                      "x": x}
     xt, xd = res["toeplitz"].pop("x"), res["direct"].pop("x")
     rel_td = float((xd - xt).norm() / xt.norm())
+    # the same system with the Toeplitz product in FP64 (the reference's
+    # double-precision operator on the same kernel and right-hand side)
+    op64 = MergeOperator(M, Mu, rl, fl, S, antisupport(M, 1))
+    op64.set_kernel(ugrid_conv.double())
+    op64.cg(d, x0, 2)  # warm-up
+    torch.cuda.synchronize()
+    ev[3].record()
+    x64, it64, hist64 = op64.cg(d, x0, W["iters"], rtol=1e-30)
+    ev[4].record()
+    torch.cuda.synchronize()
+    res["toeplitz_fp64"] = {"ms_total": ev[3].elapsed_time(ev[4]),
+                            "ms_per_iter": ev[3].elapsed_time(ev[4]) / W["iters"],
+                            "iterations": int(it64.item()),
+                            "residual_history": [round(float(h), 4) for h in hist64.cpu()]}
+    # pin: scipy's CG steps in numpy FP64 on the host (oracle/merge.py), same
+    # kernel, same right-hand side, x0 = 0, the same 30 iterations
+    pin = None
+    if not args.no_cpu_baseline:
+        import time
+
+        from oracle import merge as omerge
+
+        mo = omerge.MergeOracle(M, Mu, N, oversampling=1, workers=os.cpu_count())
+        F_conv = np.fft.fftn(np.fft.ifftshift(ugrid_conv.double().cpu().numpy())) / M ** 3
+        S_h = S.double().cpu().numpy()
+        t0h = time.perf_counter()
+        xh, hh = omerge.cg_recurrence(lambda u: mo.W(u, F_conv, S_h), d.cpu().numpy(),
+                                      np.zeros(M ** 3), W["iters"], rtol=1e-30)
+        host_s = time.perf_counter() - t0h
+        del F_conv
+        xh_t = torch.as_tensor(xh, device=dev)
+        nh = float(xh_t.norm())
+        pin = {"what": "scipy's CG steps in numpy FP64 (scipy.fft, %d threads) on the same "
+                       "kernel and right-hand side, x0 = 0, %d iterations" % (os.cpu_count(),
+                                                                             W["iters"]),
+               "host_seconds": host_s,
+               "residual_history_fp64_host": [round(float(h), 4) for h in hh],
+               "solution_rel_l2_vs_fp64": {
+                   "toeplitz_fp32_product": float((xt - xh_t).norm()) / nh,
+                   "toeplitz_fp64_product": float((x64 - xh_t).norm()) / nh,
+                   "direct": float((xd - xh_t).norm()) / nh}}
+    op64.close()
     # one application of each form to the same centrosymmetric vector
     g = torch.Generator(device=dev)
     g.manual_seed(5)
@@ -799,6 +841,7 @@ def run_merge(args):
            "config": {"workload": W["name"], "M": M, "n_points": npts, "iterations": W["iters"],
                       "eps": W["eps"]},
            "toeplitz": res["toeplitz"], "direct": res["direct"],
+           "toeplitz_fp64": res["toeplitz_fp64"], "pin_fp64_cg": pin,
            "solution_direct_vs_toeplitz_rel_l2": rel_td,
            "operator_direct_vs_toeplitz_rel_l2": op_rel,
            "data_term_direct_vs_toeplitz_rel_l2": conv_rel,

@@ -322,6 +322,14 @@ int spf_merge_destroy(spf_merge merge);
 int spf_merge_info(spf_merge merge, int *fft_size);
 int spf_merge_set_kernel(spf_merge merge, const float *d_ugrid_conv, int M_ups,
                          void *stream);
+/* The Toeplitz kernel in FP64 (d_ugrid_conv: M_ups^3 doubles): from this call
+ * on the form-0 product runs in FP64 (D2Z / Z2D on the L grid) as the
+ * reference's double-precision run computes it (use_single_prec false,
+ * spinifel/sequential/autocorrelation.py:130-149); spf_merge_set_kernel
+ * returns the operator to the FP32 product.  Allocates the FP64 buffers
+ * (4 L^3 doubles) on the first call. */
+int spf_merge_set_kernel_f64(spf_merge merge, const double *d_ugrid_conv, int M_ups,
+                             void *stream);
 /* The points are bin-sorted once here (spf_nufft_sort_orient) and every
  * direct-form product uses the sorted kernel; det_panels/det_nx/det_ny
  * describe a multi-panel detector (n_pix = their product, 0 = unordered). */

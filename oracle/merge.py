@@ -35,8 +35,36 @@ def support_from_estimate(ac_estimate: np.ndarray) -> np.ndarray:
     return (gaussian_filter(ac_estimate, 0.5) > 1e-12).astype(np.float64)
 
 
+def cg_recurrence(matvec, b, x0, maxiter, rtol=1e-5):
+    """scipy.sparse.linalg.cg's iteration without a preconditioner, step for
+    step (r = b - A x0; rho = r.r; p = r + (rho / rho_prev) p; q = A p;
+    alpha = rho / p.q; x += alpha p; r -= alpha q; stop when ||r|| <
+    rtol ||b||), returning also ||r|| at the start of every iteration (the
+    recurrence residual the device CG records)."""
+    b = np.asarray(b, dtype=np.float64)
+    x = np.array(x0, dtype=np.float64, copy=True)
+    r = b - matvec(x) if np.any(x) else b.copy()
+    atol = rtol * np.linalg.norm(b)
+    hist = []
+    p = None
+    rho_prev = None
+    for it in range(maxiter):
+        nr = np.linalg.norm(r)
+        hist.append(float(nr))
+        if nr < atol:
+            break
+        rho = float(r @ r)
+        p = r.copy() if p is None else r + (rho / rho_prev) * p
+        q = matvec(p)
+        alpha = rho / float(p @ q)
+        x += alpha * p
+        r -= alpha * q
+        rho_prev = rho
+    return x, np.array(hist)
+
+
 class MergeOracle:
-    def __init__(self, M, M_ups, N, oversampling=1, maxiter=100, eps=1e-12):
+    def __init__(self, M, M_ups, N, oversampling=1, maxiter=100, eps=1e-12, workers=None):
         self.M, self.M_ups, self.N = M, M_ups, N
         self.rlambda = 1.0 / N / 1000.0
         self.flambda = 1e3
@@ -45,20 +73,41 @@ class MergeOracle:
         self.F_antisupport = antisupport(M, oversampling)
         self.iterations = 0
         self.residuals = []
+        # workers: threads for scipy.fft (same FP64 transforms, for the large
+        # grids); None keeps numpy's FFT, the one the reference calls
+        self.workers = workers
+
+    def _fftn(self, a):
+        if self.workers is None:
+            return np.fft.fftn(a)
+        import scipy.fft as sfft
+
+        return sfft.fftn(a, workers=self.workers)
+
+    def _ifftn(self, a):
+        if self.workers is None:
+            return np.fft.ifftn(a)
+        import scipy.fft as sfft
+
+        return sfft.ifftn(a, workers=self.workers)
 
     def conv(self, x, F_conv, S):
         M, Mu = self.M, self.M_ups
         ups = np.zeros((Mu,) * 3)
         ups[:M, :M, :M] = x.reshape((M,) * 3) * S
-        out = np.fft.fftshift(np.fft.ifftn(np.fft.fftn(np.fft.ifftshift(ups)) * F_conv))
+        out = np.fft.fftshift(self._ifftn(self._fftn(np.fft.ifftshift(ups)) * F_conv))
         return (out[:M, :M, :M] * S).real.reshape(-1)
 
     def reg(self, x, S):
         M = self.M
         g = x.reshape((M,) * 3) * S
-        F = np.fft.fftn(np.fft.ifftshift(g))
-        r = np.fft.fftshift(np.fft.ifftn(F * np.fft.ifftshift(self.F_antisupport)))
+        F = self._fftn(np.fft.ifftshift(g))
+        r = np.fft.fftshift(self._ifftn(F * np.fft.ifftshift(self.F_antisupport)))
         return (r * S).real.reshape(-1)
+
+    def W(self, x, F_conv, S):
+        x = np.real(x)
+        return self.conv(x, F_conv, S) + self.rlambda * x + self.flambda * self.reg(x, S)
 
     def kernel(self, H_, K_, L_):
         """F_conv from the type 1 of ones onto the M_ups grid."""

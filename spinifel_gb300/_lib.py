@@ -75,6 +75,7 @@ SIGNATURES = {
     "spf_merge_destroy": [_c_void_p],
     "spf_merge_info": [_c_void_p, ctypes.POINTER(_int)],
     "spf_merge_set_kernel": [_c_void_p, _c_void_p, _int, _c_void_p],
+    "spf_merge_set_kernel_f64": [_c_void_p, _c_void_p, _int, _c_void_p],
     "spf_merge_set_direct": [_c_void_p, _c_void_p, _c_void_p, _i64, _c_void_p, _i64, _int, _int,
                              _int, _dbl, _c_void_p],
     "spf_nufft_sort_orient": [_c_void_p, _c_void_p, _i64, _c_void_p, _i64, _dbl, _c_void_p],

@@ -18,7 +18,10 @@
 //
 // CG follows scipy.sparse.linalg.cg (the solver the reference calls, :217)
 // step for step: stop when ||r|| < rtol ||b||, at most maxiter iterations.
-// x, r, p, q and every dot product are FP64; the operator is FP32.  Each
+// x, r, p, q and every dot product are FP64; the Toeplitz product is FP32
+// (R2C / C2R) after spf_merge_set_kernel and FP64 (D2Z / Z2D) after
+// spf_merge_set_kernel_f64, the form for the reference's double-precision
+// run.  Each
 // iteration is a fixed sequence of launches with no host synchronisation
 // (convergence is a device flag that turns later updates into no-ops), so a
 // whole solve can be captured in one CUDA graph.
@@ -61,6 +64,14 @@ struct spf_merge_s {
   int *flags = nullptr;        // [0] done, [1] iterations
   cufftHandle r2c_L = 0, c2r_L = 0, r2c_M = 0, c2r_M = 0;
   bool plans_ok = false;    // the L-grid pair
+  // FP64 Toeplitz product (spf_merge_set_kernel_f64): D2Z / Z2D on the L grid
+  bool conv64 = false;
+  double *kernel_hat64 = nullptr;  // nLh
+  double *conv_in64 = nullptr;     // L^3, zero outside the M^3 corner
+  double2 *conv_freq64 = nullptr;  // nLh
+  double *conv_out64 = nullptr;    // L^3
+  cufftHandle d2z_L = 0, z2d_L = 0;
+  bool plans64_ok = false;
   bool m_plans_ok = false;  // the M-grid D2Z / Z2D pair (regulariser without Rader)
   // regulariser of a prime M with smooth M - 1: Rader DFT and the full
   // real multiplier ifftshift(F_anti) on M^3
@@ -184,7 +195,8 @@ __global__ void k_cg_stage2(const double *partial, double *scal, const int *flag
 __global__ void k_cg_update_p(double *__restrict__ p, const double *__restrict__ r,
                               const double *__restrict__ scal, const int *__restrict__ flags,
                               const float *__restrict__ S, int M, int L, float *__restrict__ conv_in,
-                              double *__restrict__ reg_in, float *__restrict__ modes) {
+                              double *__restrict__ conv_in64, double *__restrict__ reg_in,
+                              float *__restrict__ modes) {
   const bool done = flags[0] != 0;
   const double beta = scal[S_BETA];
   const int64_t n = (int64_t)M * M * M;
@@ -201,6 +213,7 @@ __global__ void k_cg_update_p(double *__restrict__ p, const double *__restrict__
     const unsigned iu = (unsigned)i;  // M^3 < 2^31 (M <= 1024)
     int c = (int)(iu % M), b = (int)((iu / M) % M), a = (int)(iu / (unsigned)(M * M));
     if (conv_in) conv_in[((int64_t)a * L + b) * L + c] = v;
+    if (conv_in64) conv_in64[((int64_t)a * L + b) * L + c] = vd;
     if (modes) modes[i] = v;
     // ifftshift: reg_in[j] = in[(j + M/2) mod M]  <=>  in[i] lands at j = (i - M/2) mod M
     int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
@@ -210,8 +223,8 @@ __global__ void k_cg_update_p(double *__restrict__ p, const double *__restrict__
 
 // apply to a plain vector (x0 or a test vector): same as update_p without the CG update
 __global__ void k_load_input(const double *__restrict__ x, const float *__restrict__ S, int M,
-                             int L, float *__restrict__ conv_in, double *__restrict__ reg_in,
-                             float *__restrict__ modes) {
+                             int L, float *__restrict__ conv_in, double *__restrict__ conv_in64,
+                             double *__restrict__ reg_in, float *__restrict__ modes) {
   const int64_t n = (int64_t)M * M * M;
   const int h = M / 2;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -221,6 +234,7 @@ __global__ void k_load_input(const double *__restrict__ x, const float *__restri
     const unsigned iu = (unsigned)i;  // M^3 < 2^31 (M <= 1024)
     int c = (int)(iu % M), b = (int)((iu / M) % M), a = (int)(iu / (unsigned)(M * M));
     if (conv_in) conv_in[((int64_t)a * L + b) * L + c] = v;
+    if (conv_in64) conv_in64[((int64_t)a * L + b) * L + c] = vd;
     if (modes) modes[i] = v;
     int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
     reg_in[((int64_t)ja * M + jb) * M + jc] = vd;
@@ -250,7 +264,8 @@ __global__ void k_mul_real_d(double2 *__restrict__ z, const double *__restrict__
 // direct form)
 __global__ void __launch_bounds__(RED_THREADS)
     k_assemble(const double *__restrict__ x, const float *__restrict__ S, int M, int L,
-               const float *__restrict__ conv_out, const float *__restrict__ t1_out,
+               const float *__restrict__ conv_out, const double *__restrict__ conv_out64,
+               const float *__restrict__ t1_out,
                double conv_scale, const double *__restrict__ reg_out, double rlambda,
                double flambda, double *__restrict__ q, double *__restrict__ partial) {
   const int64_t n = (int64_t)M * M * M;
@@ -262,7 +277,8 @@ __global__ void __launch_bounds__(RED_THREADS)
     const unsigned iu = (unsigned)i;  // M^3 < 2^31 (M <= 1024)
     int c = (int)(iu % M), b = (int)((iu / M) % M), a = (int)(iu / (unsigned)(M * M));
     double sv = S[i];
-    double cv = conv_out ? (double)conv_out[((int64_t)a * L + b) * L + c] : (double)t1_out[i];
+    const int64_t li = ((int64_t)a * L + b) * L + c;
+    double cv = conv_out64 ? conv_out64[li] : conv_out ? (double)conv_out[li] : (double)t1_out[i];
     // fftshift: out[i] = reg_out[(i - M/2) mod M]
     int ja = (a - h + M) % M, jb = (b - h + M) % M, jc = (c - h + M) % M;
     double rv = reg_out[((int64_t)ja * M + jb) * M + jc];
@@ -298,8 +314,9 @@ __global__ void k_sub(const double *__restrict__ b, const double *__restrict__ q
 }
 
 // kernel_hat: g[m] = ugrid_conv[d + Mu/2] at m = d mod L for |d| <= M-1
-__global__ void k_embed_kernel(const float *__restrict__ ugrid_conv, int Mu, int M, int L,
-                               float *__restrict__ g) {
+template <typename Tin, typename Tout>
+__global__ void k_embed_kernel(const Tin *__restrict__ ugrid_conv, int Mu, int M, int L,
+                               Tout *__restrict__ g) {
   const int64_t nL = (int64_t)L * L * L;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nL;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -307,17 +324,24 @@ __global__ void k_embed_kernel(const float *__restrict__ ugrid_conv, int Mu, int
     int d1 = m1 <= L / 2 ? m1 : m1 - L;
     int d2 = m2 <= L / 2 ? m2 : m2 - L;
     int d3 = m3 <= L / 2 ? m3 : m3 - L;
-    float v = 0.0f;
+    Tout v = Tout(0);
     if (abs(d1) <= M - 1 && abs(d2) <= M - 1 && abs(d3) <= M - 1) {
       int a = d1 + Mu / 2, b = d2 + Mu / 2, c = d3 + Mu / 2;
       if (a >= 0 && a < Mu && b >= 0 && b < Mu && c >= 0 && c < Mu)
-        v = ugrid_conv[((int64_t)a * Mu + b) * Mu + c];
+        v = (Tout)ugrid_conv[((int64_t)a * Mu + b) * Mu + c];
     }
     g[i] = v;
   }
 }
 
 __global__ void k_real_part(const float2 *__restrict__ z, float *__restrict__ out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = z[i].x;
+}
+
+__global__ void k_real_part_d(const double2 *__restrict__ z, double *__restrict__ out,
+                              int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     out[i] = z[i].x;
@@ -368,7 +392,18 @@ static int grid1(int64_t n) { return grid_for(n, 256, (int64_t)sm_count() * 8); 
 
 // conv part of the operator from conv_in / reg_in / modes already loaded
 static int apply_operator_core(spf_merge_s *G, bool direct, cudaStream_t s) {
-  if (!direct) {
+  if (!direct && G->conv64) {
+    cufftSetStream(G->d2z_L, s);
+    cufftSetStream(G->z2d_L, s);
+    SPF_TRY(cufft_ok(cufftExecD2Z(G->d2z_L, G->conv_in64,
+                                  reinterpret_cast<cufftDoubleComplex *>(G->conv_freq64)),
+                     "conv D2Z"));
+    k_mul_real_d<<<grid1(G->nLh), 256, 0, s>>>(G->conv_freq64, G->kernel_hat64, G->nLh);
+    SPF_TRY(check_launch("k_mul_real_d"));
+    SPF_TRY(cufft_ok(cufftExecZ2D(G->z2d_L, reinterpret_cast<cufftDoubleComplex *>(G->conv_freq64),
+                                  G->conv_out64),
+                     "conv Z2D"));
+  } else if (!direct) {
     cufftSetStream(G->r2c_L, s);
     cufftSetStream(G->c2r_L, s);
     SPF_TRY(cufft_ok(cufftExecR2C(G->r2c_L, G->conv_in, reinterpret_cast<cufftComplex *>(G->conv_freq)),
@@ -500,7 +535,8 @@ int spf_merge_destroy(spf_merge_s *G) {
   if (!G) return SPF_OK;
   void *bufs[] = {G->support, G->kernel_hat, G->mask_hat, G->conv_in, G->conv_freq,
                   G->conv_out, G->reg_in, G->reg_freq, G->reg_out, G->modes, G->t1_out,
-                  G->r, G->p, G->q, G->partial, G->scal, G->flags, G->mask_full};
+                  G->r, G->p, G->q, G->partial, G->scal, G->flags, G->mask_full,
+                  G->kernel_hat64, G->conv_in64, G->conv_freq64, G->conv_out64};
   for (void *b : bufs) cudaFree(b);
   free_sweep(G->sweep);
   prime_dft_free(G->pd);
@@ -511,6 +547,10 @@ int spf_merge_destroy(spf_merge_s *G) {
   if (G->m_plans_ok) {
     cufftDestroy(G->r2c_M);
     cufftDestroy(G->c2r_M);
+  }
+  if (G->plans64_ok) {
+    cufftDestroy(G->d2z_L);
+    cufftDestroy(G->z2d_L);
   }
   delete G;
   return SPF_OK;
@@ -532,7 +572,58 @@ int spf_merge_set_kernel(spf_merge_s *G, const float *d_ugrid_conv, int M_ups, v
   SPF_TRY(cufft_ok(cufftExecR2C(G->r2c_L, G->conv_out, reinterpret_cast<cufftComplex *>(G->conv_freq)),
                    "kernel R2C"));
   k_real_part<<<grid1(G->nLh), 256, 0, s>>>(G->conv_freq, G->kernel_hat, G->nLh);
-  return check_launch("k_real_part");
+  SPF_TRY(check_launch("k_real_part"));
+  G->conv64 = false;
+  return SPF_OK;
+}
+
+int spf_merge_set_kernel_f64(spf_merge_s *G, const double *d_ugrid_conv, int M_ups,
+                             void *stream) {
+  SPF_REQUIRE(G && d_ugrid_conv, "spf_merge_set_kernel_f64: NULL pointer");
+  SPF_REQUIRE(M_ups >= 2 * G->M - 1, "spf_merge_set_kernel_f64: M_ups < 2M-1");
+  cudaStream_t s = as_stream(stream);
+  if (!G->plans64_ok) {
+    int st = SPF_OK;
+    auto alloc = [&](void **p, size_t bytes) {
+      if (st == SPF_OK) st = check_cuda(cudaMalloc(p, bytes), "spf_merge_set_kernel_f64");
+    };
+    alloc((void **)&G->kernel_hat64, G->nLh * sizeof(double));
+    alloc((void **)&G->conv_in64, G->nL * sizeof(double));
+    alloc((void **)&G->conv_freq64, G->nLh * sizeof(double2));
+    alloc((void **)&G->conv_out64, G->nL * sizeof(double));
+    SPF_TRY(st);
+    SPF_TRY(check_cuda(cudaMemsetAsync(G->conv_in64, 0, G->nL * sizeof(double), s),
+                       "spf_merge_set_kernel_f64"));
+    if (cufftPlan3d(&G->d2z_L, G->L, G->L, G->L, CUFFT_D2Z) != CUFFT_SUCCESS) {
+      set_error("spf_merge_set_kernel_f64: cufftPlan3d D2Z (L = %d) failed", G->L);
+      return SPF_ERR_CUDA;
+    }
+    if (cufftPlan3d(&G->z2d_L, G->L, G->L, G->L, CUFFT_Z2D) != CUFFT_SUCCESS) {
+      cufftDestroy(G->d2z_L);
+      set_error("spf_merge_set_kernel_f64: cufftPlan3d Z2D (L = %d) failed", G->L);
+      return SPF_ERR_CUDA;
+    }
+    G->plans64_ok = true;
+  }
+  // the FP64 product's kernel ...
+  k_embed_kernel<<<grid1(G->nL), 256, 0, s>>>(d_ugrid_conv, M_ups, G->M, G->L, G->conv_out64);
+  SPF_TRY(check_launch("k_embed_kernel (f64)"));
+  cufftSetStream(G->d2z_L, s);
+  SPF_TRY(cufft_ok(cufftExecD2Z(G->d2z_L, G->conv_out64,
+                                reinterpret_cast<cufftDoubleComplex *>(G->conv_freq64)),
+                   "kernel D2Z"));
+  k_real_part_d<<<grid1(G->nLh), 256, 0, s>>>(G->conv_freq64, G->kernel_hat64, G->nLh);
+  SPF_TRY(check_launch("k_real_part_d"));
+  // ... and the FP32 one, rounded, which the batched sweep reads
+  k_embed_kernel<<<grid1(G->nL), 256, 0, s>>>(d_ugrid_conv, M_ups, G->M, G->L, G->conv_out);
+  SPF_TRY(check_launch("k_embed_kernel"));
+  cufftSetStream(G->r2c_L, s);
+  SPF_TRY(cufft_ok(cufftExecR2C(G->r2c_L, G->conv_out, reinterpret_cast<cufftComplex *>(G->conv_freq)),
+                   "kernel R2C"));
+  k_real_part<<<grid1(G->nLh), 256, 0, s>>>(G->conv_freq, G->kernel_hat, G->nLh);
+  SPF_TRY(check_launch("k_real_part"));
+  G->conv64 = true;
+  return SPF_OK;
 }
 
 int spf_merge_set_direct(spf_merge_s *G, spf_nufft_plan_s *plan, const float *d_quats,
@@ -564,13 +655,16 @@ int spf_merge_apply(spf_merge_s *G, int form, const double *d_x, double *d_y, vo
   SPF_REQUIRE(form == 0 || (form == 1 && G->nufft), "spf_merge_apply: bad form / no direct set-up");
   cudaStream_t s = as_stream(stream);
   bool direct = form == 1;
+  const bool c64 = !direct && G->conv64;
   k_load_input<<<grid1(G->n), 256, 0, s>>>(d_x, G->support, G->M, G->L,
-                                           direct ? nullptr : G->conv_in, G->reg_in,
+                                           (direct || c64) ? nullptr : G->conv_in,
+                                           c64 ? G->conv_in64 : nullptr, G->reg_in,
                                            direct ? G->modes : nullptr);
   SPF_TRY(check_launch("k_load_input"));
   SPF_TRY(apply_operator_core(G, direct, s));
   k_assemble<<<RED_BLOCKS, RED_THREADS, 0, s>>>(
-      d_x, G->support, G->M, G->L, direct ? nullptr : G->conv_out, G->t1_out,
+      d_x, G->support, G->M, G->L, (direct || c64) ? nullptr : G->conv_out,
+      c64 ? G->conv_out64 : nullptr, G->t1_out,
       direct ? G->direct_scale : G->conv_scale, G->reg_out, G->rlambda, G->flambda, d_y, nullptr);
   return check_launch("k_assemble");
 }
@@ -585,6 +679,7 @@ int spf_merge_cg(spf_merge_s *G, int form, const double *d_b, double *d_x, int x
   SPF_REQUIRE(form == 0 || (form == 1 && G->nufft), "spf_merge_cg: bad form / no direct set-up");
   cudaStream_t s = as_stream(stream);
   bool direct = form == 1;
+  const bool c64 = !direct && G->conv64;
   const int64_t n = G->n;
   // r = b - W x0
   if (x0_is_zero) {
@@ -606,12 +701,14 @@ int spf_merge_cg(spf_merge_s *G, int form, const double *d_b, double *d_x, int x
     k_cg_stage1<<<1, RED_THREADS, 0, s>>>(G->partial, it, G->scal, G->flags, d_hist);
     SPF_TRY(check_launch("k_cg_stage1"));
     k_cg_update_p<<<grid1(n), 256, 0, s>>>(G->p, G->r, G->scal, G->flags, G->support, G->M, G->L,
-                                           direct ? nullptr : G->conv_in, G->reg_in,
+                                           (direct || c64) ? nullptr : G->conv_in,
+                                           c64 ? G->conv_in64 : nullptr, G->reg_in,
                                            direct ? G->modes : nullptr);
     SPF_TRY(check_launch("k_cg_update_p"));
     SPF_TRY(apply_operator_core(G, direct, s));
     k_assemble<<<RED_BLOCKS, RED_THREADS, 0, s>>>(
-        G->p, G->support, G->M, G->L, direct ? nullptr : G->conv_out, G->t1_out,
+        G->p, G->support, G->M, G->L, (direct || c64) ? nullptr : G->conv_out,
+        c64 ? G->conv_out64 : nullptr, G->t1_out,
         direct ? G->direct_scale : G->conv_scale, G->reg_out, G->rlambda, G->flambda, G->q,
         G->partial);
     SPF_TRY(check_launch("k_assemble"));

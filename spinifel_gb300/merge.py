@@ -51,10 +51,21 @@ class MergeOperator:
         except Exception:
             pass
 
-    def set_kernel(self, ugrid_conv: torch.Tensor):
-        """ugrid_conv: real M_ups^3 (type 1 of ones onto M_ups modes / M_ups^3)."""
-        u = ugrid_conv.to(device=self.device, dtype=torch.float32).contiguous()
-        _lib.call("spf_merge_set_kernel", self._h, _lib.ptr(u), u.shape[0], _lib.stream_handle())
+    def set_kernel(self, ugrid_conv: torch.Tensor, fp64: bool | None = None):
+        """ugrid_conv: real M_ups^3 (type 1 of ones onto M_ups modes / M_ups^3).
+        fp64 (default: ugrid_conv is float64) runs the Toeplitz product in
+        FP64, as the reference's double-precision run does."""
+        if fp64 is None:
+            fp64 = ugrid_conv.dtype == torch.float64
+        if fp64:
+            u = ugrid_conv.to(device=self.device, dtype=torch.float64).contiguous()
+            _lib.call("spf_merge_set_kernel_f64", self._h, _lib.ptr(u), u.shape[0],
+                      _lib.stream_handle())
+        else:
+            u = ugrid_conv.to(device=self.device, dtype=torch.float32).contiguous()
+            _lib.call("spf_merge_set_kernel", self._h, _lib.ptr(u), u.shape[0],
+                      _lib.stream_handle())
+        self.fp64 = bool(fp64)
         torch.cuda.current_stream().synchronize()
 
     def set_direct(self, plan: NufftPlan, quats: torch.Tensor, ppr: torch.Tensor, scale: float,

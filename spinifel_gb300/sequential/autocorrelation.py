@@ -13,6 +13,11 @@ step stays on the device: the type-1 NUFFTs, the FFT convolution and a
 device-resident CG whose vectors and dot products are FP64.
 form="direct" applies W through type 2 -> type 1 NUFFTs every iteration
 instead of the Toeplitz FFT (same operator for centrosymmetric x).
+
+With a NUFFT at the reference's own tolerance (use_single_prec off: FP64 at
+eps 1e-12) the two type-1 NUFFTs run in FP64 and the Toeplitz product in
+FP64 too, so the solve is the reference's double-precision one; otherwise
+the NUFFTs and the product are FP32 (CG vectors and dots FP64 either way).
 """
 from __future__ import annotations
 
@@ -40,7 +45,8 @@ class Merge:
         self.rlambda = 1 / self.N / 1000
         self.flambda = 1e3
         self.data = _arrays.to_dev(np.asarray(slices_, dtype=np.float64).reshape(-1)
-                                   if not _arrays.is_torch(slices_) else slices_.reshape(-1))
+                                   if not _arrays.is_torch(slices_) else slices_.reshape(-1),
+                                   torch.float64)
         self.F_antisupport = antisupport(self.M, settings.oversampling)
         self.nufft = nufft
         self.form = form
@@ -57,28 +63,31 @@ class Merge:
 
     def setup_linops(self, H, K, L, ac_support, x0, orientations=None):
         dev = _arrays.device()
-        H_, K_, L_ = (torch.as_tensor(np.asarray(a).reshape(-1) * self.mult, dtype=torch.float32,
+        fp64 = bool(getattr(self.nufft, "fp64", False))
+        dt = torch.float64 if fp64 else torch.float32
+        H_, K_, L_ = (torch.as_tensor(np.asarray(a).reshape(-1) * self.mult, dtype=dt,
                                       device=dev) for a in (H, K, L))
-        ones = torch.ones(H_.numel(), dtype=torch.float32, device=dev)
+        ones = torch.ones(H_.numel(), dtype=dt, device=dev)
         ugrid_conv = self.nufft.adjoint(ones, H_, K_, L_, 1, self.use_reciprocal_symmetry,
                                         self.M_ups)
         sup = torch.as_tensor(np.asarray(ac_support, dtype=np.float32), device=dev)
         op = MergeOperator(self.M, self.M_ups, self.rlambda, self.flambda, sup,
                            self.F_antisupport)
-        op.set_kernel(ugrid_conv)
+        op.set_kernel(ugrid_conv, fp64=fp64)
         if self.form == "direct":
             assert orientations is not None
             # a plan of its own: the operator keeps its bin-sorted points for
             # the whole solve, while the adjoints below sort on the shared one
             from ..nufft import NufftPlan
 
-            plan = NufftPlan(self.M, self.nufft.eps)
+            plan = NufftPlan(self.M, max(self.nufft.eps, 1e-6))
             det = tuple(self.pixel_position_reciprocal.shape[1:])
             op.set_direct(plan, torch.as_tensor(orientations, dtype=torch.float32, device=dev),
                           torch.as_tensor(self.pixel_position_reciprocal.reshape(3, -1),
                                           dtype=torch.float32, device=dev), self.mult,
                           det_shape=det if len(det) == 3 else None)
-        uvect_ADb = self.nufft.adjoint(self.data, H_, K_, L_, sup,
+        sup_t = sup.to(dt) if fp64 else sup
+        uvect_ADb = self.nufft.adjoint(self.data, H_, K_, L_, sup_t,
                                        self.use_reciprocal_symmetry, self.M).reshape(-1)
         d = uvect_ADb.double() + self.rlambda * x0
         self.op = op

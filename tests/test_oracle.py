@@ -202,3 +202,28 @@ def test_prep_restatement_matches_reference_golden():
     q, saxs = prep.get_saxs(dist, f4.mean(axis=0))
     np.testing.assert_array_equal(q, g["saxs_q"])
     np.testing.assert_array_equal(saxs, g["saxs"])
+
+
+def test_cg_recurrence_is_scipys_cg():
+    """oracle.merge.cg_recurrence (which also records ||r|| per iteration)
+    takes scipy's CG steps: same iterate on a merge system, and with
+    scipy.fft threads the same FP64 operator as numpy's FFT."""
+    from scipy.sparse.linalg import LinearOperator, cg
+
+    from oracle import merge as omerge
+
+    M = 9
+    rng = np.random.default_rng(5)
+    mo = omerge.MergeOracle(M, 2 * M, 5000)
+    mo_t = omerge.MergeOracle(M, 2 * M, 5000, workers=2)
+    g = rng.standard_normal((2 * M,) * 3)
+    g = g + g[::-1, ::-1, ::-1]
+    F_conv = np.fft.fftn(np.fft.ifftshift(np.abs(np.fft.fftn(g)))) / M ** 3
+    S = (rng.random((M,) * 3) > 0.2).astype(np.float64)
+    b = rng.standard_normal(M ** 3)
+    A = LinearOperator(dtype=np.float64, shape=(M ** 3,) * 2, matvec=lambda u: mo.W(u, F_conv, S))
+    xs, _ = cg(A, b, x0=np.zeros(M ** 3), maxiter=15, rtol=1e-30)
+    xr, hist = omerge.cg_recurrence(lambda u: mo_t.W(u, F_conv, S), b, np.zeros(M ** 3), 15,
+                                    rtol=1e-30)
+    assert hist.size == 15 and hist[0] == np.linalg.norm(b)
+    np.testing.assert_allclose(xr, xs, rtol=0, atol=1e-9 * np.abs(xs).max())
