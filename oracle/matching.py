@@ -4,7 +4,8 @@ Orientation-matching semantics of the reference, restated in numpy FP64:
 
 * sklearn_argmin: euclidean_distances(model_slices, slices) + argmin(axis=0),
   the reference's CPU branch (spinifel/sequential/nearest_neighbor.py:134-135);
-  euclidean_distances computes ||x||^2 - 2 x.y + ||y||^2 (clipped at 0).
+  euclidean_distances computes ||x||^2 - 2 x.y + ||y||^2 (clipped at 0);
+  sklearn_argmin_stream does the same over references given in blocks.
 * snm_dist: SNM's dist = x2 + y2 - 2 x.y over orientation batches with the
   per-batch std rescale (spinifel/sequential/orientation_matching.py:148-179).
 * knn_topk: the CUDA KNN top-k (orientation_matching_sp.cu:535-609):
@@ -34,6 +35,35 @@ def sklearn_argmin(model_slices, slices):
     """argmin over references of the squared distance, per image (FP64)."""
     d = np.maximum(sq_dists(model_slices, slices), 0.0)  # [n_ref, n_img]
     return np.argmin(d, axis=0), d
+
+
+def sklearn_argmin_stream(blocks, slices):
+    """sklearn_argmin over references that arrive in blocks (an iterable of
+    [B_i, P] arrays in reference order), so that no [n_ref, n_img] matrix is
+    held: per image the index of the smallest euclidean_distances value
+    (sqrt of the clipped GEMM form, as nearest_neighbor.py:134-135 computes
+    it) and its squared distance; the lower index wins ties, as np.argmin's
+    first occurrence does.  Returns (index, squared distance, references seen)."""
+    y = np.asarray(slices, dtype=np.float64)
+    y2 = np.einsum("ij,ij->i", y, y)
+    best = np.full(y.shape[0], np.inf)
+    best_sq = np.full(y.shape[0], np.inf)
+    idx = np.full(y.shape[0], -1, dtype=np.int64)
+    cols = np.arange(y.shape[0])
+    start = 0
+    for blk in blocks:
+        b = np.asarray(blk, dtype=np.float64)
+        d = np.einsum("ij,ij->i", b, b)[:, None] + y2[None, :] - 2.0 * (b @ y.T)
+        np.maximum(d, 0.0, out=d)
+        e = np.sqrt(d)
+        m = np.argmin(e, axis=0)
+        v = e[m, cols]
+        upd = v < best
+        best[upd] = v[upd]
+        best_sq[upd] = d[m, cols][upd]
+        idx[upd] = m[upd] + start
+        start += b.shape[0]
+    return idx, best_sq, start
 
 
 def snm_argmin(batches, slices):

@@ -227,3 +227,24 @@ def test_cg_recurrence_is_scipys_cg():
                                     rtol=1e-30)
     assert hist.size == 15 and hist[0] == np.linalg.norm(b)
     np.testing.assert_allclose(xr, xs, rtol=0, atol=1e-9 * np.abs(xs).max())
+
+
+def test_streamed_sklearn_argmin_equals_whole_matrix():
+    """sklearn_argmin_stream over reference blocks (exact duplicates across
+    blocks included: the first wins) equals sklearn_argmin on the whole
+    matrix and the reference's own sklearn call."""
+    euclidean_distances = pytest.importorskip("sklearn.metrics.pairwise").euclidean_distances
+
+    rng = np.random.default_rng(8)
+    refs = rng.random((500, 300))
+    refs[450] = refs[20]
+    imgs = rng.random((40, 300))
+    imgs[0] = refs[20] + 1e-3
+    idx_w, d_w = om.sklearn_argmin(refs, imgs)
+    blocks = (refs[s:s + 128] for s in range(0, 500, 128))
+    idx_s, dsq_s, n = om.sklearn_argmin_stream(blocks, imgs)
+    assert n == 500
+    np.testing.assert_array_equal(idx_s, idx_w)
+    np.testing.assert_array_equal(idx_s, np.argmin(euclidean_distances(refs, imgs), axis=0))
+    np.testing.assert_allclose(dsq_s, d_w[idx_w, np.arange(40)], rtol=1e-12)
+    assert idx_s[0] == 20
