@@ -62,6 +62,31 @@ class SNM:
         self.nufft = nufft
         self.timings = {}
 
+    def capture(self, ac):
+        """Record one generation (model set-up, every orientation batch's
+        slicing, std rescale, distances and running argmin) as a CUDA graph
+        on a static copy of the model; match_indices_graphed then replays it
+        for each new model.  The launch sequence does not depend on the
+        model, so one capture serves every generation of this SNM."""
+        self._g_ac = _arrays.to_dev(np.real(ac) if not _arrays.is_torch(ac) else ac,
+                                    self.nufft.dtype).clone()
+        self.match_indices(self._g_ac)  # plans, module loading and workspaces outside the capture
+        torch.cuda.synchronize()
+        self._graph = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(self._graph, stream=s):
+                self._g_idx = self.match_indices(self._g_ac)
+        torch.cuda.current_stream().wait_stream(s)
+
+    def match_indices_graphed(self, ac) -> torch.Tensor:
+        """match_indices by replaying the captured generation (capture first)."""
+        self._g_ac.copy_(_arrays.to_dev(np.real(ac) if not _arrays.is_torch(ac) else ac,
+                                        self.nufft.dtype))
+        self._graph.replay()
+        return self._g_idx.clone()
+
     def match_indices(self, ac) -> torch.Tensor:
         """Best reference orientation index per image (device int32; int64
         in FP64 mode)."""

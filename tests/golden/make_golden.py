@@ -30,8 +30,10 @@ oracle/nufft.py for the un-vendored finufft) and then calls, unmodified:
     (numpy 2 dropped numpy.infty, which phase() reads; it is set to inf)
 
 Inputs are regenerated from the stored seeds by tests (numpy PCG64 streams are
-stable), so only small outputs are committed.  Run in the build container:
-    python tests/golden/make_golden.py
+stable), so only small outputs are committed.  Run where the reference's
+sources are checked out:
+    python tests/golden/make_golden.py [path-to-spinifel-checkout]
+(or set SPINIFEL_REFERENCE).
 """
 from __future__ import annotations
 
@@ -43,7 +45,9 @@ import types
 
 import numpy as np
 
-REF = "/root/reference"
+# the reference project's checkout: first argument, or SPINIFEL_REFERENCE
+REF = (sys.argv[1] if len(sys.argv) > 1 else
+       os.environ.get("SPINIFEL_REFERENCE", "/root/reference"))
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)

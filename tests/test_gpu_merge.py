@@ -268,3 +268,53 @@ def test_solve_ac_fp64_matches_reference_golden(lib):
     err = rel(ac, g["ac"])
     print(f"FP64 merge vs the reference's solve_ac: rel-L2 {err:.2e}")
     assert err < 1e-5
+
+
+def test_direct_form_cg_captured_in_a_cuda_graph(setup):
+    """The direct-form CG (type 2 -> type 1 over the bin-sorted points every
+    iteration) recorded as one CUDA graph: its replay gives the eager
+    solution.  The spreading adds in the order its atomics land, and this
+    system's CG (flambda = 1e3 against rlambda = 1/N/1000) amplifies that
+    rounding over the iterations: two eager solves differ by about 1e-5
+    relative after 10 iterations, so replay and eager are held to 1e-3 and
+    the first operator application to 1e-6."""
+    from spinifel_gb300.nufft import NufftPlan
+
+    M = setup["M"]
+    S = np.ones((M,) * 3)
+    op, mo, _ = _operator(setup, S)
+    dev = torch.device("cuda", 0)
+    op.set_direct(NufftPlan(M, 1e-6), torch.as_tensor(setup["orient"], device=dev),
+                  torch.as_tensor(setup["ppr"].reshape(3, -1), device=dev),
+                  float(np.pi / setup["pdr"].max()))
+    rng = np.random.default_rng(55)
+    xs = rng.standard_normal((M,) * 3)
+    xs = 0.5 * (xs + xs[::-1, ::-1, ::-1])
+    b = op.apply(torch.as_tensor(xs.reshape(-1).copy(), device=dev), form=1)
+    x = torch.zeros_like(b)
+    hist = torch.zeros(10, dtype=torch.float64, device=dev)
+    iters = torch.zeros(1, dtype=torch.int32, device=dev)
+    op.cg_into(b, x, hist, iters, 10, 1e-12, form=1, x0_is_zero=True)
+    torch.cuda.synchronize()
+    eager, eager_hist = x.clone(), hist.clone()
+    x.zero_()
+    op.cg_into(b, x, hist, iters, 10, 1e-12, form=1, x0_is_zero=True)
+    torch.cuda.synchronize()
+    print(f"two eager direct-form solves differ by {float((x - eager).norm() / eager.norm()):.2e}")
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        x.zero_()
+        with torch.cuda.graph(g, stream=s):
+            op.cg_into(b, x, hist, iters, 10, 1e-12, form=1, x0_is_zero=True)
+    torch.cuda.current_stream().wait_stream(s)
+    for _ in range(2):
+        x.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        assert int(iters.item()) == 10
+        assert float((x - eager).norm() / eager.norm()) < 1e-3
+        # ||b|| and ||r_1|| = ||b - alpha W b||: one application of W
+        np.testing.assert_allclose(hist[:2].cpu().numpy(), eager_hist[:2].cpu().numpy(),
+                                   rtol=1e-6)

@@ -362,3 +362,26 @@ def test_spread_orient_sorted_equals_patch(dev):
 
     matching.check_device_error()
     assert rel(out[1], out[0]) < 1e-6
+
+
+@pytest.mark.parametrize("eps,tol", [(1e-6, TOL), (1e-12, 1e-10)])
+def test_gen_model_slices_matches_oracle(dev, eps, tol):
+    """slicing.gen_model_slices (the reference's signature) and its batched
+    form against the oracle's type 2 at the normalised rotated positions."""
+    from spinifel_gb300 import geom
+    from spinifel_gb300.slicing import gen_model_slices, gen_model_slices_batch
+
+    model, ppr, pdr, quats = _slice_case(21, (4, 16, 16), 12, 90)
+    n_pix = ppr[0].size
+    s = gen_model_slices(model, quats, ppr, pdr.max(), 1, None, n_pix, None, eps=eps)
+    H, K, L = geom.hkl(quats, ppr)
+    mult = np.pi / pdr.max()
+    want = onufft.nufft3d2(H.reshape(-1) * mult, K.reshape(-1) * mult, L.reshape(-1) * mult,
+                           model, -1, 1e-12).real
+    assert s.shape == (12 * n_pix,)
+    assert rel(s, want) < tol
+    sb = gen_model_slices_batch(model, quats, ppr, pdr.max(), 1, None, n_pix, batch_size=4,
+                                eps=eps)
+    np.testing.assert_array_equal(sb, s)
+    with pytest.raises(ValueError):
+        gen_model_slices(model, quats, ppr, pdr.max(), 1, None, n_pix, "cpu")
