@@ -352,6 +352,9 @@ def run_nufft(args):
         return e0.elapsed_time(e1) / reps
 
     npts = n_or * n_pix
+    from spinifel_gb300 import autotune
+
+    tuned_slice = autotune.tune_slice(P, q[:min(n_or, 500)], ppr_t, mult, det)
     t_slice = timed(lambda: P.slice(q, ppr_t, mult, out=out, det_shape=det))
     _lib.call("spf_nufft_sort_orient", P.handle, _lib.ptr(q), n_or, _lib.ptr(ppr_t), n_pix, mult,
               _lib.stream_handle())
@@ -437,7 +440,8 @@ def run_nufft(args):
         "slice_t2": {"ms": t_slice, "points_per_s": npts / (t_slice / 1e3),
                      "tflops": npts * (2 * w ** 3 + 3 * w) / (t_slice / 1e3) / 1e12,
                      "fp32_peak_tflops_nominal": fp32_peak,
-                     "out_gbs": npts * 4 / (t_slice / 1e3) / 1e9},
+                     "out_gbs": npts * 4 / (t_slice / 1e3) / 1e9,
+                     "autotune": tuned_slice},
         "interp_spread_sorted": {"ms": t_isp, "points_per_s": npts / (t_isp / 1e3)},
         "spread_t1_patch": {"ms": t_spr, "points_per_s": npts / (t_spr / 1e3),
                             "gbs_points": npts * 16 / (t_spr / 1e3) / 1e9,
@@ -701,6 +705,19 @@ def run_merge(args):
     S = torch.ones((M,) * 3, dtype=torch.float32, device=dev)
     N = data.numel()
     rl, fl = 1.0 / N / 1000.0, 1e3
+    # work-item size of the fused interpolate / spread pass, measured on
+    # these points (the operator then sorts with it)
+    from spinifel_gb300 import autotune
+
+    def sort_fn():
+        _lib.call("spf_nufft_sort_orient", P.handle, _lib.ptr(q), W["n_frames"], _lib.ptr(ppr_t),
+                  n_pix, mult, _lib.stream_handle())
+
+    def pass_fn():
+        P.spread_zero()
+        _lib.call("spf_nufft_interp_spread_sorted", P.handle, None, _lib.stream_handle())
+
+    tuned_items = autotune.tune_sort_item(P, sort_fn, pass_fn, tag=W["name"])
     op = MergeOperator(M, Mu, rl, fl, S, antisupport(M, 1))
     op.set_kernel(ugrid_conv)
     op.set_direct(P, q, ppr_t, mult, det_shape=det)
@@ -897,6 +914,7 @@ def run_merge(args):
                       "eps": W["eps"]},
            "toeplitz": res["toeplitz"], "direct": res["direct"],
            "toeplitz_fp64": res["toeplitz_fp64"], "pin_fp64_cg": pin,
+           "autotune": {"sort_item": tuned_items},
            "solution_direct_vs_toeplitz_rel_l2": rel_td,
            "operator_direct_vs_toeplitz_rel_l2": op_rel,
            "data_term_direct_vs_toeplitz_rel_l2": conv_rel,
@@ -991,6 +1009,10 @@ def main():
     plan.set_modes(torch.as_tensor(model, device=dev))
 
     # --- slicing: all references resident (timed separately) ---------------
+    from spinifel_gb300 import autotune
+
+    tuned_slice = autotune.tune_slice(plan, ref_q[:2000], ppr_t, mult, det)
+    tuned_slice.pop("trials", None)
     refs = torch.empty(W["n_ref"], n_pix, dtype=torch.float32, device=dev)
     B = 5000
     barrier()
@@ -1041,7 +1063,8 @@ def main():
     from spinifel_gb300 import autotune
 
     tuned = {"bf16": autotune.tune_bf16(frames, rset),
-             "fp32": autotune.tune_fp32(frames.f32, frames.sq, rset)}
+             "fp32": autotune.tune_fp32(frames.f32, frames.sq, rset),
+             "slice": tuned_slice}
     for k in tuned:
         tuned[k].pop("trials", None)
 

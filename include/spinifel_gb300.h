@@ -61,11 +61,21 @@ int spf_selftest_bounded_wait(int64_t timeout_ms, int *d_result, void *stream);
  *   SPF_TUNE_PRIME_DFT    : the merge regulariser on a prime grid size M
  *                           (read by spf_merge_create): 1 = Rader DFT
  *                           (default, when M - 1 is 2,3,5,7-smooth),
- *                           2 = cuFFT D2Z / Z2D */
+ *                           2 = cuFFT D2Z / Z2D
+ *   SPF_TUNE_SLICE_SHAPE  : tile shape of spf_slice_t2_det (patch and warp
+ *                           block, codes 0..5; default 0 = 16 x 16 patches
+ *                           of 4 x 8 warp blocks); every shape gives the
+ *                           same bits
+ *   SPF_TUNE_SORT_ITEM    : points per work item of the bin-sorted passes
+ *                           (read by spf_nufft_sort_orient /
+ *                           spf_nufft_sort_points; default 2048,
+ *                           256 .. 4096) */
 #define SPF_TUNE_BF16_GROUP_M 1
 #define SPF_TUNE_FP32_GROUP_M 2
 #define SPF_TUNE_BF16_GRID 3
 #define SPF_TUNE_PRIME_DFT 4
+#define SPF_TUNE_SLICE_SHAPE 5
+#define SPF_TUNE_SORT_ITEM 6
 int spf_tune_set(int param, int64_t value);
 int spf_tune_get(int param, int64_t *value);
 

@@ -29,6 +29,8 @@ SPF_TUNE_BF16_GROUP_M = 1
 SPF_TUNE_FP32_GROUP_M = 2
 SPF_TUNE_BF16_GRID = 3
 SPF_TUNE_PRIME_DFT = 4
+SPF_TUNE_SLICE_SHAPE = 5
+SPF_TUNE_SORT_ITEM = 6
 
 
 class SpfError(RuntimeError):

@@ -1,4 +1,4 @@
-"""Autotuner for the launch parameters of the matching kernels.
+"""Autotuner for the launch parameters and tile shapes of the hot kernels.
 
 The tensor-core kernel is persistent (one CTA per SM by default) and walks
 its (image tile, reference tile) pairs in groups of GROUP_M image tiles, so
@@ -10,6 +10,12 @@ fastest is kept through spf_tune_set and cached in a JSON file keyed by
 device, kernel and shape (SPF_TUNE_CACHE overrides the file's location).
 Results do not depend on these parameters (only the order in which tiles are
 visited changes), so tuning never changes an answer.
+
+The fused NUFFT kernels are tuned the same way: the tile shape of the
+panel-detector slicing kernel (patch and warp block, SPF_TUNE_SLICE_SHAPE;
+every shape gives the same bits) and the work-item size of the bin-sorted
+interpolate / spread passes (SPF_TUNE_SORT_ITEM; the points of an item are
+summed in another grouping, so sums may differ in the last bits).
 """
 from __future__ import annotations
 
@@ -136,3 +142,63 @@ def tune_fp32(frames_f32, frames_sq, refs, group_sizes=(4, 8, 16), reps=1, force
         cache[key] = rec
         _save(cache)
         return dict(rec, cached=False)
+
+
+SLICE_SHAPES = {0: "16x16 patch, 4x8 warps", 1: "16x16 patch, 8x4 warps",
+                2: "8x32 patch, 2x16 warps", 3: "8x32 patch, 4x8 warps",
+                4: "32x8 patch, 8x4 warps", 5: "32x8 patch, 16x2 warps"}
+
+
+def tune_slice(plan, quats, ppr, scale: float, det_shape, reps=2, force=False):
+    """Pick SPF_TUNE_SLICE_SHAPE for spf_slice_t2_det on this model grid and
+    detector (quats: the orientations to time on, a few thousand suffice);
+    returns {"shape", "tile", "ms", "trials"}."""
+    name = torch.cuda.get_device_name()
+    key = f"{name}|slice|{plan.n_fine}|w{plan.width}|{tuple(det_shape)}"
+    with _lock:
+        cache = _load()
+        if not force and key in cache:
+            best = cache[key]
+            _lib.call("spf_tune_set", _lib.SPF_TUNE_SLICE_SHAPE, int(best["shape"]))
+            return dict(best, cached=True)
+        out = torch.empty(quats.shape[0], int(ppr[0].numel()), device=quats.device)
+        trials = {}
+        for code in SLICE_SHAPES:
+            _lib.call("spf_tune_set", _lib.SPF_TUNE_SLICE_SHAPE, code)
+            trials[code] = _time(lambda: plan.slice(quats, ppr, scale, out=out,
+                                                    det_shape=det_shape), reps)
+        code = min(trials, key=trials.get)
+        _lib.call("spf_tune_set", _lib.SPF_TUNE_SLICE_SHAPE, code)
+        best = {"shape": code, "tile": SLICE_SHAPES[code], "ms": trials[code]}
+        cache[key] = best
+        _save(cache)
+        return dict(best, trials={SLICE_SHAPES[k]: v for k, v in trials.items()}, cached=False)
+
+
+def tune_sort_item(plan, sort_fn, pass_fn, sizes=(1024, 2048, 4096), reps=2,
+                   force=False, tag=""):
+    """Pick SPF_TUNE_SORT_ITEM (points per work item of the bin-sorted
+    passes): for each size sort_fn() re-sorts the points and pass_fn() is
+    timed; the best size is set and the points re-sorted with it.  Returns
+    {"items", "ms", "trials"}."""
+    name = torch.cuda.get_device_name()
+    key = f"{name}|sort_item|{plan.n_fine}|w{plan.width}|{tag}"
+    with _lock:
+        cache = _load()
+        if not force and key in cache:
+            best = cache[key]
+            _lib.call("spf_tune_set", _lib.SPF_TUNE_SORT_ITEM, int(best["items"]))
+            sort_fn()
+            return dict(best, cached=True)
+        trials = {}
+        for n in sizes:
+            _lib.call("spf_tune_set", _lib.SPF_TUNE_SORT_ITEM, int(n))
+            sort_fn()
+            trials[n] = _time(pass_fn, reps)
+        n = min(trials, key=trials.get)
+        _lib.call("spf_tune_set", _lib.SPF_TUNE_SORT_ITEM, int(n))
+        sort_fn()
+        best = {"items": n, "ms": trials[n]}
+        cache[key] = best
+        _save(cache)
+        return dict(best, trials=trials, cached=False)

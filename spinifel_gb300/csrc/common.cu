@@ -82,9 +82,14 @@ const char *spf_last_error(void) { return spf::get_error(); }
 uint64_t spf_launch_count(void) { return spf::g_launches.load(); }
 
 int spf_tune_set(int param, int64_t value) {
-  SPF_REQUIRE(param >= 1 && param <= 4, "spf_tune_set: unknown parameter %d", param);
+  SPF_REQUIRE(param >= 1 && param <= 6, "spf_tune_set: unknown parameter %d", param);
   if (param == SPF_TUNE_PRIME_DFT)
     SPF_REQUIRE(value >= 0 && value <= 2, "spf_tune_set: prime DFT choice is 0, 1 or 2");
+  if (param == SPF_TUNE_SLICE_SHAPE)
+    SPF_REQUIRE(value >= 0 && value <= 5, "spf_tune_set: slicing tile shape is 0 .. 5");
+  if (param == SPF_TUNE_SORT_ITEM)
+    SPF_REQUIRE(value == 0 || (value >= 256 && value <= 4096),
+                "spf_tune_set: sort item size is 256 .. 4096 (0 = default)");
   if (param == SPF_TUNE_BF16_GROUP_M || param == SPF_TUNE_FP32_GROUP_M)
     SPF_REQUIRE(value >= 0 && value <= 1024, "spf_tune_set: group size out of range");
   if (param == SPF_TUNE_BF16_GRID)
@@ -99,7 +104,7 @@ int spf_tune_set(int param, int64_t value) {
 }
 
 int spf_tune_get(int param, int64_t *value) {
-  SPF_REQUIRE(param >= 1 && param <= 4 && value, "spf_tune_get: bad arguments");
+  SPF_REQUIRE(param >= 1 && param <= 6 && value, "spf_tune_get: bad arguments");
   *value = spf::tune_get(param, 0);
   return SPF_OK;
 }

@@ -371,22 +371,45 @@ __device__ __forceinline__ int patch_dx(int t) { return ((t >> 5) >> 1) * 4 + ((
 __device__ __forceinline__ int patch_dy(int t) { return ((t >> 5) & 1) * 8 + (t & 7); }
 constexpr int SLICE_SMEM_FLOATS = 11264;  // 44 KB
 
+// Tile shapes of the slicing kernel (256 threads, one pixel each): the patch
+// is px x py pixels of a panel and each warp takes a wx x wy block of it.
+// The shape decides how many distinct box rows a warp's loads touch (bank
+// conflicts) and the box's size; which is fastest depends on the detector's
+// pixel spacing in grid cells, so the autotuner picks it
+// (SPF_TUNE_SLICE_SHAPE).  Every shape gives the same bits.
+struct PatchShape {
+  int px, py, wx, wy;
+};
+constexpr int N_SLICE_SHAPES = 6;
+__host__ __device__ inline PatchShape slice_shape(int code) {
+  switch (code) {
+    case 1: return PatchShape{16, 16, 8, 4};
+    case 2: return PatchShape{8, 32, 2, 16};
+    case 3: return PatchShape{8, 32, 4, 8};
+    case 4: return PatchShape{32, 8, 8, 4};
+    case 5: return PatchShape{32, 8, 16, 2};
+    default: return PatchShape{16, 16, 4, 8};
+  }
+}
+
 template <int W>
 __global__ void __launch_bounds__(256)
     k_slice_t2_det(const float *__restrict__ re_pad, GridGeom g, const float *__restrict__ quats,
                    const float *__restrict__ ppr, int n_panels, int nx, int ny, float scale1,
                    float scale2, float scale3, float *__restrict__ out,
-                   __nv_bfloat16 *__restrict__ out_bf16) {
+                   __nv_bfloat16 *__restrict__ out_bf16, PatchShape ps) {
   __shared__ float box[SLICE_SMEM_FLOATS];
   __shared__ int bb[6];
   const int64_t o = blockIdx.x;
-  const int patches_y = (ny + SLICE_PATCH - 1) / SLICE_PATCH;
-  const int patches_x = (nx + SLICE_PATCH - 1) / SLICE_PATCH;
+  const int patches_y = (ny + ps.py - 1) / ps.py;
+  const int patches_x = (nx + ps.px - 1) / ps.px;
   const int pid = blockIdx.y;
   const int panel = pid / (patches_x * patches_y);
   const int rem = pid % (patches_x * patches_y);
-  const int px = (rem / patches_y) * SLICE_PATCH + patch_dx((int)threadIdx.x);
-  const int py = (rem % patches_y) * SLICE_PATCH + patch_dy((int)threadIdx.x);
+  const int t = (int)threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int warps_y = ps.py / ps.wy;
+  const int px = (rem / patches_y) * ps.px + (warp / warps_y) * ps.wx + lane / ps.wy;
+  const int py = (rem % patches_y) * ps.py + (warp % warps_y) * ps.wy + lane % ps.wy;
   const bool valid = px < nx && py < ny && panel < n_panels;
   const int64_t n_pix = (int64_t)n_panels * nx * ny;
   const int64_t p = ((int64_t)panel * nx + (valid ? px : 0)) * ny + (valid ? py : 0);
@@ -692,7 +715,9 @@ __global__ void k_interp_spread_orient(const float *__restrict__ re_pad,
 // bin-sorted points: 8^3-cell bins of the padded grid
 // ---------------------------------------------------------------------------
 constexpr int BIN = 8;
-constexpr int BIN_CHUNK = 2048;  // points per work item (big bins are split)
+constexpr int BIN_CHUNK = 2048;      // default points per work item (big bins are split)
+constexpr int BIN_CHUNK_MAX = 4096;  // largest item SPF_TUNE_SORT_ITEM may pick: the cell
+                                     // sort stages an item in 24 KB of shared memory
 
 // The points of the sorted passes: orientation points (point o * n_pix + p
 // is pixel p of the detector rotated by quaternion o, coordinates made in the
@@ -793,12 +818,17 @@ __device__ __forceinline__ int axis_cell(float x, float s, int n, int off) {
 template <int W>
 __global__ void __launch_bounds__(256)
     k_item_cellsort(GridGeom g, BinDims bd, const int4 *__restrict__ items,
-                    int32_t *__restrict__ sorted, PointSrc src, float s1, float s2, float s3) {
+                    int32_t *__restrict__ sorted, PointSrc src, float s1, float s2, float s3,
+                    unsigned int *__restrict__ err) {
   constexpr int NC = BIN * BIN * BIN;
-  __shared__ int32_t idx[BIN_CHUNK];
-  __shared__ int16_t key[BIN_CHUNK];
+  __shared__ int32_t idx[BIN_CHUNK_MAX];
+  __shared__ int16_t key[BIN_CHUNK_MAX];
   __shared__ int32_t cnt[NC];
   const int4 it = items[blockIdx.x];
+  if (it.z > BIN_CHUNK_MAX) {  // an item larger than the staging arrays is never read
+    if (threadIdx.x == 0 && err) atomicExch(err, (unsigned int)(-SPF_ERR_ARG));
+    return;
+  }
   const int b = it.x;
   const int bi = b / (bd.nb[1] * bd.nb[2]), bj = (b / bd.nb[2]) % bd.nb[1], bk = b % bd.nb[2];
   const int i0b = bi * BIN, j0b = bj * BIN, k0b = bk * BIN;
@@ -1246,8 +1276,9 @@ int spf_slice_t2_det(spf_nufft_plan P, const float *d_quats, int64_t n_orient, c
               "spf_slice_t2_det: negative size");
   if (n_orient == 0 || n_panels == 0 || nx == 0 || ny == 0) return SPF_OK;
   SPF_REQUIRE(d_quats && d_ppr && d_out, "spf_slice_t2_det: NULL pointer");
-  int64_t patches = (int64_t)n_panels * ((nx + SLICE_PATCH - 1) / SLICE_PATCH) *
-                    ((ny + SLICE_PATCH - 1) / SLICE_PATCH);
+  const int code = (int)tune_get(SPF_TUNE_SLICE_SHAPE, 0);
+  const PatchShape ps = slice_shape(code >= 0 && code < N_SLICE_SHAPES ? code : 0);
+  int64_t patches = (int64_t)n_panels * ((nx + ps.px - 1) / ps.px) * ((ny + ps.py - 1) / ps.py);
   SPF_REQUIRE(n_orient < (1LL << 31) && patches <= 65535, "spf_slice_t2_det: size too large");
   cudaStream_t s = as_stream(stream);
   GridGeom g = geom_of(P);
@@ -1258,7 +1289,7 @@ int spf_slice_t2_det(spf_nufft_plan P, const float *d_quats, int64_t n_orient, c
   auto *bf = reinterpret_cast<__nv_bfloat16 *>(d_out_bf16);
   SPF_W_DISPATCH(P->w, (k_slice_t2_det<W><<<grid, 256, 0, s>>>(P->re_pad, g, d_quats, d_ppr,
                                                                   n_panels, nx, ny, s1, s2, s3,
-                                                                  d_out, bf)));
+                                                                  d_out, bf, ps)));
   return check_launch("k_slice_t2_det");
 }
 
@@ -1421,10 +1452,12 @@ static int sort_points(spf_nufft_plan P, PointSrc src, int64_t n, double scale, 
   cudaFree(counts);
   if (st != SPF_OK) return st;
   std::vector<int4> h_items;
+  int32_t chunk = (int32_t)tune_get(SPF_TUNE_SORT_ITEM, BIN_CHUNK);
+  if (chunk < 1 || chunk > BIN_CHUNK_MAX) chunk = BIN_CHUNK;  // the cell sort stages <= the max
   for (int64_t b = 0; b < n_bins; ++b)
-    for (int32_t c = 0; c < h_counts[b]; c += BIN_CHUNK)
+    for (int32_t c = 0; c < h_counts[b]; c += chunk)
       h_items.push_back(make_int4((int)b, h_offsets[b] + c,
-                                  h_counts[b] - c < BIN_CHUNK ? h_counts[b] - c : BIN_CHUNK, 0));
+                                  h_counts[b] - c < chunk ? h_counts[b] - c : chunk, 0));
   if ((int64_t)h_items.size() > P->items_cap) {
     cudaFree(P->items);
     P->items = nullptr;
@@ -1438,7 +1471,8 @@ static int sort_points(spf_nufft_plan P, PointSrc src, int64_t n, double scale, 
   P->n_sorted = n;
   if (P->n_items > 0) {  // points sharing a footprint cell become consecutive
     SPF_W_DISPATCH(P->w, (k_item_cellsort<W><<<(unsigned)P->n_items, 256, 0, s>>>(
-                             g, bd, P->items, P->sorted, src, s1, s2, s3)));
+                             g, bd, P->items, P->sorted, src, s1, s2, s3,
+                             device_error_word())));
     SPF_TRY(check_launch("k_item_cellsort"));
   }
   P->s_quats = src.quats;

@@ -190,7 +190,9 @@ def test_slice_full_size_subset_and_linearity(dev):
 @pytest.mark.parametrize("det", [(4, 32, 32), (4, 128, 128), (2, 20, 37)])
 def test_patch_slicing_identical_to_point_slicing(dev, det):
     """spf_slice_t2_det (shared-memory patches) gives the same bits as
-    spf_slice_t2 (thread per point), ragged patches included."""
+    spf_slice_t2 (thread per point), ragged patches included, with every
+    tile shape the autotuner chooses from."""
+    from spinifel_gb300 import _lib
     from spinifel_gb300.nufft import NufftPlan
 
     model, ppr, pdr, quats = _slice_case(81, det, 64, 25)
@@ -198,8 +200,13 @@ def test_patch_slicing_identical_to_point_slicing(dev, det):
     P = NufftPlan(81, 1e-6)
     P.set_modes(t(model, dev))
     a = P.slice(t(quats, dev), ppr_t, np.pi / pdr.max())
-    b = P.slice(t(quats, dev), ppr_t, np.pi / pdr.max(), det_shape=det)
-    assert torch.equal(a, b)
+    try:
+        for shape in range(6):
+            _lib.call("spf_tune_set", _lib.SPF_TUNE_SLICE_SHAPE, shape)
+            b = P.slice(t(quats, dev), ppr_t, np.pi / pdr.max(), det_shape=det)
+            assert torch.equal(a, b), shape
+    finally:
+        _lib.call("spf_tune_set", _lib.SPF_TUNE_SLICE_SHAPE, 0)
 
 
 def test_spread_orient_equals_spread_points(dev):
@@ -385,3 +392,33 @@ def test_gen_model_slices_matches_oracle(dev, eps, tol):
     np.testing.assert_array_equal(sb, s)
     with pytest.raises(ValueError):
         gen_model_slices(model, quats, ppr, pdr.max(), 1, None, n_pix, "cpu")
+
+
+def test_sorted_pass_item_size_keeps_the_operator(dev):
+    """The bin-sorted direct operator split into work items of 512, 1,024 or
+    4,096 points (SPF_TUNE_SORT_ITEM; the default is 2,048) gives the
+    default's result to rounding, and reports no device error."""
+    from spinifel_gb300 import _lib
+    from spinifel_gb300.nufft import NufftPlan
+
+    model, ppr, pdr, quats = _slice_case(31, (4, 32, 32), 120, 46)
+    q, ppr_t = t(quats, dev), t(ppr.reshape(3, -1), dev)
+    mult = np.pi / pdr.max()
+    P = NufftPlan(31, 1e-6)
+    P.set_modes(t(model, dev))
+    res = {}
+    try:
+        for n in (0, 512, 1024, 4096):
+            _lib.call("spf_tune_set", _lib.SPF_TUNE_SORT_ITEM, n)
+            _lib.call("spf_nufft_sort_orient", P.handle, _lib.ptr(q), q.shape[0],
+                      _lib.ptr(ppr_t), ppr_t.shape[1], float(mult), _lib.stream_handle())
+            P.spread_zero()
+            _lib.call("spf_nufft_interp_spread_sorted", P.handle, None, _lib.stream_handle())
+            res[n] = P.finish(+1)[0].cpu().numpy()
+    finally:
+        _lib.call("spf_tune_set", _lib.SPF_TUNE_SORT_ITEM, 0)
+    from spinifel_gb300 import matching
+
+    matching.check_device_error()
+    for n in (512, 1024, 4096):
+        assert rel(res[n], res[0]) < 1e-6
