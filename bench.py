@@ -453,6 +453,22 @@ def run_nufft(args):
                                     "points_per_s": npts / (t_srt / 1e3),
                                     "points_per_s_with_sort": npts / ((t_srt + t_sort) / 1e3),
                                     "gbs_points": npts * 16 / (t_srt / 1e3) / 1e9}}
+    # the reference's precision: FP64 slicing at eps 1e-12 (w = 13) of a
+    # subset of the orientations, and its relative L2 against the FP32 slices
+    from spinifel_gb300.nufft import NufftPlan64
+
+    n64 = min(n_or, 50)
+    P64 = NufftPlan64(M, 1e-12)
+    P64.set_modes(torch.as_tensor(model, dtype=torch.float64, device=dev))
+    q64, ppr64 = q[:n64].double(), ppr_t.double()
+    out64 = torch.empty(n64, n_pix, dtype=torch.float64, device=dev)
+    t64 = timed(lambda: P64.slice(q64, ppr64, mult, out=out64), reps=1)
+    d32 = P.slice(q[:n64], ppr_t, mult, det_shape=det).double()
+    rec["slice_t2_fp64"] = {"ms": t64, "orientations": n64, "width": P64.width,
+                            "points_per_s": n64 * n_pix / (t64 / 1e3),
+                            "fp64_tflops": n64 * n_pix * 2 * P64.width ** 3 / (t64 / 1e3) / 1e12,
+                            "fp32_slices_rel_l2_vs_fp64":
+                                float((d32 - out64).norm() / out64.norm())}
     print(json.dumps(rec), flush=True)
 
 
