@@ -69,7 +69,7 @@ int spf_selftest_bounded_wait(int64_t timeout_ms, int *d_result, void *stream);
  *   SPF_TUNE_SORT_ITEM    : points per work item of the bin-sorted passes
  *                           (read by spf_nufft_sort_orient /
  *                           spf_nufft_sort_points; default 2048,
- *                           256 .. 4096) */
+ *                           256 .. 8192) */
 #define SPF_TUNE_BF16_GROUP_M 1
 #define SPF_TUNE_FP32_GROUP_M 2
 #define SPF_TUNE_BF16_GRID 3

@@ -175,7 +175,7 @@ def tune_slice(plan, quats, ppr, scale: float, det_shape, reps=2, force=False):
         return dict(best, trials={SLICE_SHAPES[k]: v for k, v in trials.items()}, cached=False)
 
 
-def tune_sort_item(plan, sort_fn, pass_fn, sizes=(1024, 2048, 4096), reps=2,
+def tune_sort_item(plan, sort_fn, pass_fn, sizes=(2048, 4096, 8192), reps=2,
                    force=False, tag=""):
     """Pick SPF_TUNE_SORT_ITEM (points per work item of the bin-sorted
     passes): for each size sort_fn() re-sorts the points and pass_fn() is

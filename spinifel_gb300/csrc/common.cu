@@ -88,8 +88,8 @@ int spf_tune_set(int param, int64_t value) {
   if (param == SPF_TUNE_SLICE_SHAPE)
     SPF_REQUIRE(value >= 0 && value <= 5, "spf_tune_set: slicing tile shape is 0 .. 5");
   if (param == SPF_TUNE_SORT_ITEM)
-    SPF_REQUIRE(value == 0 || (value >= 256 && value <= 4096),
-                "spf_tune_set: sort item size is 256 .. 4096 (0 = default)");
+    SPF_REQUIRE(value == 0 || (value >= 256 && value <= 8192),
+                "spf_tune_set: sort item size is 256 .. 8192 (0 = default)");
   if (param == SPF_TUNE_BF16_GROUP_M || param == SPF_TUNE_FP32_GROUP_M)
     SPF_REQUIRE(value >= 0 && value <= 1024, "spf_tune_set: group size out of range");
   if (param == SPF_TUNE_BF16_GRID)

@@ -716,8 +716,9 @@ __global__ void k_interp_spread_orient(const float *__restrict__ re_pad,
 // ---------------------------------------------------------------------------
 constexpr int BIN = 8;
 constexpr int BIN_CHUNK = 2048;      // default points per work item (big bins are split)
-constexpr int BIN_CHUNK_MAX = 4096;  // largest item SPF_TUNE_SORT_ITEM may pick: the cell
-                                     // sort stages an item in 24 KB of shared memory
+constexpr int BIN_CHUNK_MAX = 8192;  // largest item SPF_TUNE_SORT_ITEM may pick: the cell
+                                     // sort stages an item in 48 KB of dynamic shared memory
+constexpr size_t CELLSORT_SMEM = (size_t)BIN_CHUNK_MAX * (sizeof(int32_t) + sizeof(int16_t));
 
 // The points of the sorted passes: orientation points (point o * n_pix + p
 // is pixel p of the detector rotated by quaternion o, coordinates made in the
@@ -821,8 +822,9 @@ __global__ void __launch_bounds__(256)
                     int32_t *__restrict__ sorted, PointSrc src, float s1, float s2, float s3,
                     unsigned int *__restrict__ err) {
   constexpr int NC = BIN * BIN * BIN;
-  __shared__ int32_t idx[BIN_CHUNK_MAX];
-  __shared__ int16_t key[BIN_CHUNK_MAX];
+  extern __shared__ __align__(16) unsigned char cs_smem[];  // CELLSORT_SMEM bytes
+  int32_t *idx = reinterpret_cast<int32_t *>(cs_smem);              // BIN_CHUNK_MAX
+  int16_t *key = reinterpret_cast<int16_t *>(idx + BIN_CHUNK_MAX);  // BIN_CHUNK_MAX
   __shared__ int32_t cnt[NC];
   const int4 it = items[blockIdx.x];
   if (it.z > BIN_CHUNK_MAX) {  // an item larger than the staging arrays is never read
@@ -1470,7 +1472,10 @@ static int sort_points(spf_nufft_plan P, PointSrc src, int64_t n, double scale, 
   P->n_items = (int64_t)h_items.size();
   P->n_sorted = n;
   if (P->n_items > 0) {  // points sharing a footprint cell become consecutive
-    SPF_W_DISPATCH(P->w, (k_item_cellsort<W><<<(unsigned)P->n_items, 256, 0, s>>>(
+    SPF_W_DISPATCH(P->w, (cudaFuncSetAttribute(k_item_cellsort<W>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)CELLSORT_SMEM),
+                          k_item_cellsort<W><<<(unsigned)P->n_items, 256, CELLSORT_SMEM, s>>>(
                              g, bd, P->items, P->sorted, src, s1, s2, s3,
                              device_error_word())));
     SPF_TRY(check_launch("k_item_cellsort"));

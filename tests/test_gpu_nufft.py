@@ -395,9 +395,9 @@ def test_gen_model_slices_matches_oracle(dev, eps, tol):
 
 
 def test_sorted_pass_item_size_keeps_the_operator(dev):
-    """The bin-sorted direct operator split into work items of 512, 1,024 or
-    4,096 points (SPF_TUNE_SORT_ITEM; the default is 2,048) gives the
-    default's result to rounding, and reports no device error."""
+    """The bin-sorted direct operator split into work items of 512, 1,024,
+    4,096 or 8,192 points (SPF_TUNE_SORT_ITEM; the default is 2,048) gives
+    the default's result to rounding, and reports no device error."""
     from spinifel_gb300 import _lib
     from spinifel_gb300.nufft import NufftPlan
 
@@ -408,7 +408,7 @@ def test_sorted_pass_item_size_keeps_the_operator(dev):
     P.set_modes(t(model, dev))
     res = {}
     try:
-        for n in (0, 512, 1024, 4096):
+        for n in (0, 512, 1024, 4096, 8192):
             _lib.call("spf_tune_set", _lib.SPF_TUNE_SORT_ITEM, n)
             _lib.call("spf_nufft_sort_orient", P.handle, _lib.ptr(q), q.shape[0],
                       _lib.ptr(ppr_t), ppr_t.shape[1], float(mult), _lib.stream_handle())
@@ -420,5 +420,5 @@ def test_sorted_pass_item_size_keeps_the_operator(dev):
     from spinifel_gb300 import matching
 
     matching.check_device_error()
-    for n in (512, 1024, 4096):
+    for n in (512, 1024, 4096, 8192):
         assert rel(res[n], res[0]) < 1e-6
