@@ -1146,6 +1146,32 @@ def main():
                 "kernel": "k_dist_topk_bf16",
                 "kernel_ms": k_ms, "peak_source": f"bf16_tflops ({peak_src}, burst)"}
 
+    # --- end to end through the host API ------------------------------------
+    # one library call per step (spf_match_bf16_host): pinned uint16 frames
+    # in, indices and distances out; chunked copies overlap the matching
+    e2e_out = {}
+
+    def e2e_step():
+        e2e_out["idx"], e2e_out["dist"] = matching.match_bf16_host(imgs_u16_host, rset)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    with ClockSampler(local) as clk_e2e:
+        t0.record()
+        for _ in range(args.steps):
+            e2e_step()
+        t1.record()
+        barrier()
+    e2e_ms = t0.elapsed_time(t1) / args.steps
+    e2e = {"value": W["n_img"] * world / (e2e_ms / 1e3), "unit": "frames/s",
+           "h2d_bytes_per_step": int(imgs_u16_host.numel() * 2),
+           "d2h_bytes_per_step": int(W["n_img"] * 8),
+           "call": "spf_match_bf16_host (chunks of 2560 frames; copy and ingest of the next "
+                   "chunk under the GEMM of the current one)",
+           "clocks": clk_e2e.summary()}
+    same_e2e = bool(np.array_equal(e2e_out["idx"], idx_bf.cpu().numpy()))
+
     # --- the plain FP32 path on the same GPU, same frames -------------------
     def step_plain(fr):
         return matching.argmin_fp32(fr.f32, rset.f32, images_sq=fr.sq, refs_sq=rset.sq)
@@ -1171,29 +1197,6 @@ def main():
         da = ((xs - ra) ** 2).sum(1)
         db = ((xs - rb) ** 2).sum(1)
         n_nontie = int(((da - db).abs() > 1e-6 * torch.maximum(da, db)).sum().item())
-
-    # --- end to end through the host API ------------------------------------
-    # one library call per step (spf_match_bf16_host): pinned uint16 frames
-    # in, indices and distances out; chunked copies overlap the matching
-    e2e_out = {}
-
-    def e2e_step():
-        e2e_out["idx"], e2e_out["dist"] = matching.match_bf16_host(imgs_u16_host, rset)
-
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    barrier()
-    t0.record()
-    for _ in range(args.steps):
-        e2e_step()
-    t1.record()
-    barrier()
-    e2e_ms = t0.elapsed_time(t1) / args.steps
-    e2e = {"value": W["n_img"] * world / (e2e_ms / 1e3), "unit": "frames/s",
-           "h2d_bytes_per_step": int(imgs_u16_host.numel() * 2),
-           "d2h_bytes_per_step": int(W["n_img"] * 8),
-           "call": "spf_match_bf16_host (chunks of 2560 frames, copies overlapped)"}
-    same_e2e = bool(np.array_equal(e2e_out["idx"], idx_bf.cpu().numpy()))
 
     # --- accuracy against FP64 ---------------------------------------------
     accuracy = None

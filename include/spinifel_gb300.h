@@ -467,10 +467,12 @@ int spf_complete_open(const float *d_cand_d, const int32_t *d_cand_i, int64_t n_
  * reference's slicing_and_match step (host frames in, host indices out;
  * spinifel/sequential/orientation_matching.py:113-186): h_counts [n_img][n_pix]
  * uint16 (pinned memory lets the copies overlap the work) is moved to the
- * device in chunks of chunk_frames (<= 0: 2560) on an internal copy stream
- * while the previous chunk is ingested, matched on the tensor cores and
- * re-ranked on `stream`; the frames the certificate leaves open are completed
- * from each chunk's kept tile lists at the end.  h_idx / h_dist (n_img each;
+ * device in chunks on an internal copy stream and ingested (FP32, bf16,
+ * norms) on an internal ingest stream while the chunk before it is matched on
+ * the tensor cores and re-ranked on `stream`; chunk_frames > 0 gives fixed
+ * chunks, 0 fixed chunks of 2560 frames and a negative value chunks doubling
+ * from -chunk_frames (>= -2^30).  The frames the certificate leaves open are
+ * completed from each chunk's kept tile lists at the end.  h_idx / h_dist (n_img each;
  * h_dist may be NULL) receive the plain FP32 path's answer; h_stats (may be
  * NULL, 3 int64) gets {uncertified frames, frames completed by the range
  * GEMM, frames completed by the plain pass}.  Scratch comes from the

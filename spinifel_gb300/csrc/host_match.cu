@@ -3,15 +3,24 @@
 // (spinifel/sequential/orientation_matching.py:113-186), which takes host
 // frames and returns host indices, with the copies overlapped by the work.
 //
-// The frames are split into chunks.  A copy stream moves chunk k+1 host ->
-// device while the caller's stream ingests chunk k (FP32, bf16, norms), runs
-// the bf16 tcgen05 top-8 and the exact FP32 re-rank.  Each chunk keeps its
-// per-tile candidate lists; the frames the certificate leaves open are
-// completed at the end in one pass over all chunks (their in-band list
-// entries re-ranked exactly; no second pass over the references unless a
-// tile list may hide one); indices and distances are copied back.  Scratch comes from the device's stream-ordered pool
-// (cudaMallocAsync), whose release threshold is raised once so that repeated
-// calls reuse the memory.
+// The frames are split into chunks (2,560 frames by default).  A copy stream
+// moves the chunks host -> device one after another, an ingest stream turns
+// each landed chunk into FP32, bf16 and norms, and the caller's stream runs
+// the bf16 tcgen05 top-8 and the exact FP32 re-rank of each chunk in order.
+// The copies (211 GB/s from pinned memory on GB300) and the ingest (a
+// bandwidth-bound pass that shares the SMs with the one-CTA-per-SM GEMM) of
+// chunk k + 1 run under the GEMM of chunk k, so only the first chunk's copy
+// and ingest are exposed.  The GEMMs stay on one stream: two GEMMs that run
+// at once stream the references twice and fall off the tensor roofline.
+// Chunks may also double from a small first chunk; over 1e5 references that
+// is slower (every chunk streams all references once).
+// Each chunk keeps its per-tile candidate lists; the frames the certificate
+// leaves open are completed at the end in one pass over all chunks (their
+// in-band list entries re-ranked exactly; no second pass over the references
+// unless a tile list may hide one); indices and distances are copied back.
+// Scratch comes from the device's stream-ordered pool (cudaMallocAsync),
+// whose release threshold is raised once so that repeated calls reuse the
+// memory.
 #include <algorithm>
 #include <mutex>
 #include <vector>
@@ -52,6 +61,25 @@ void keep_pool_memory(int dev) {
   done[dev] = true;
 }
 
+// Chunks of the batch as (first frame, frames): chunk_frames > 0 fixed
+// chunks; 0 fixed chunks of 2,560 frames; < 0 chunks doubling from
+// -chunk_frames.  A doubling plan folds a remainder smaller than half a chunk
+// into the last chunk.
+std::vector<std::pair<int64_t, int64_t>> chunk_plan(int64_t n_img, int64_t chunk_frames) {
+  std::vector<std::pair<int64_t, int64_t>> plan;
+  const bool grow = chunk_frames < 0;
+  int64_t size = chunk_frames > 0 ? chunk_frames : (chunk_frames < 0 ? -chunk_frames : 2560);
+  for (int64_t r0 = 0; r0 < n_img;) {
+    const int64_t rem = n_img - r0;
+    int64_t n = std::min(size, rem);
+    if (grow && rem - n < n / 2) n = rem;
+    plan.emplace_back(r0, n);
+    r0 += n;
+    if (grow && size < (int64_t(1) << 40)) size *= 2;
+  }
+  return plan;
+}
+
 }  // namespace
 
 extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
@@ -66,9 +94,9 @@ extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
   if (n_img == 0) return SPF_OK;
   SPF_REQUIRE(h_counts && d_ref_bf16 && d_ref && d_ref_sq && d_ref_m2 && h_idx,
               "spf_match_bf16_host: NULL pointer");
-  const int64_t chunk =
-      chunk_frames > 0 ? std::min(chunk_frames, n_img) : std::min<int64_t>(n_img, 2560);
-  const int64_t n_chunks = (n_img + chunk - 1) / chunk;
+  SPF_REQUIRE(chunk_frames >= -(int64_t(1) << 30), "spf_match_bf16_host: bad chunk_frames");
+  const std::vector<std::pair<int64_t, int64_t>> plan = chunk_plan(n_img, chunk_frames);
+  const int64_t n_chunks = (int64_t)plan.size();
   SPF_REQUIRE(n_chunks <= 4096, "spf_match_bf16_host: more than 4096 chunks");
   int dev = 0;
   cudaGetDevice(&dev);
@@ -77,8 +105,17 @@ extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
   void *sv = s;
   const int64_t tiles = spf_dist_topk_bf16_tiles(n_ref);
   int st = SPF_OK;
-  cudaStream_t cs = nullptr;
+  cudaStream_t cs = nullptr, is = nullptr;
   std::vector<cudaEvent_t> ev;
+  auto new_event = [&](cudaEvent_t *e) {
+    *e = nullptr;
+    if (st == SPF_OK)
+      st = spf::check_cuda(cudaEventCreateWithFlags(e, cudaEventDisableTiming),
+                           "spf_match_bf16_host");
+    if (*e) ev.push_back(*e);
+  };
+  // chunk k's tile lists start at frame offset r0 of the candidate arrays
+  auto cand_at = [&](auto *base, int64_t k) { return base + (size_t)tiles * plan[k].first * 8; };
   {
     Scratch W(s);
     uint16_t *u16 = W.get<uint16_t>((size_t)n_img * n_pix * 2);
@@ -88,43 +125,45 @@ extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
     float *work = W.get<float>(n_img * 4), *dist = W.get<float>(n_img * 4);
     int32_t *idx = W.get<int32_t>(n_img * 4), *unc = W.get<int32_t>(n_img * 4);
     // every chunk keeps its tile lists for the completion of its open frames
-    const size_t cslot = (size_t)tiles * chunk * 8;
-    float *cand_d = W.get<float>(cslot * 4 * n_chunks);
-    int32_t *cand_i = W.get<int32_t>(cslot * 4 * n_chunks);
+    float *cand_d = W.get<float>((size_t)tiles * n_img * 8 * 4);
+    int32_t *cand_i = W.get<int32_t>((size_t)tiles * n_img * 8 * 4);
     float *mrg_d = W.get<float>((size_t)n_img * 8 * 4);
     int32_t *mrg_i = W.get<int32_t>((size_t)n_img * 8 * 4);
     st = W.st;
-    if (st == SPF_OK)
-      st = spf::check_cuda(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking),
-                           "spf_match_bf16_host");
-    // the scratch above is ordered on s; the copy stream must not run ahead of it
-    cudaEvent_t ready = nullptr;
-    if (st == SPF_OK)
-      st = spf::check_cuda(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming),
-                           "spf_match_bf16_host");
-    if (ready) ev.push_back(ready);
+    for (cudaStream_t *x : {&cs, &is})
+      if (st == SPF_OK)
+        st = spf::check_cuda(cudaStreamCreateWithFlags(x, cudaStreamNonBlocking),
+                             "spf_match_bf16_host");
+    // the scratch above is ordered on s; the other streams must not run ahead of it
+    cudaEvent_t ready;
+    new_event(&ready);
     if (st == SPF_OK) st = spf::check_cuda(cudaEventRecord(ready, s), "spf_match_bf16_host");
-    if (st == SPF_OK) st = spf::check_cuda(cudaStreamWaitEvent(cs, ready, 0), "spf_match_bf16_host");
+    for (cudaStream_t x : {cs, is})
+      if (st == SPF_OK)
+        st = spf::check_cuda(cudaStreamWaitEvent(x, ready, 0), "spf_match_bf16_host");
     for (int64_t k = 0; k < n_chunks && st == SPF_OK; ++k) {
-      const int64_t r0 = k * chunk, n = std::min(chunk, n_img - r0);
-      cudaEvent_t e = nullptr;
-      st = spf::check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming),
-                           "spf_match_bf16_host");
-      if (st != SPF_OK) break;
-      ev.push_back(e);
-      st = spf::check_cuda(cudaMemcpyAsync(u16 + r0 * n_pix, h_counts + r0 * n_pix,
-                                           (size_t)n * n_pix * 2, cudaMemcpyHostToDevice, cs),
-                           "spf_match_bf16_host: frames to device");
-      if (st == SPF_OK) st = spf::check_cuda(cudaEventRecord(e, cs), "spf_match_bf16_host");
-      if (st == SPF_OK) st = spf::check_cuda(cudaStreamWaitEvent(s, e, 0), "spf_match_bf16_host");
+      const int64_t r0 = plan[k].first, n = plan[k].second;
+      cudaEvent_t copied, ingested;
+      new_event(&copied);
+      new_event(&ingested);
+      if (st == SPF_OK)
+        st = spf::check_cuda(cudaMemcpyAsync(u16 + r0 * n_pix, h_counts + r0 * n_pix,
+                                             (size_t)n * n_pix * 2, cudaMemcpyHostToDevice, cs),
+                             "spf_match_bf16_host: frames to device");
+      if (st == SPF_OK) st = spf::check_cuda(cudaEventRecord(copied, cs), "spf_match_bf16_host");
+      if (st == SPF_OK)
+        st = spf::check_cuda(cudaStreamWaitEvent(is, copied, 0), "spf_match_bf16_host");
       if (st == SPF_OK)
         st = spf_frames_ingest_u16(u16 + r0 * n_pix, n, n_pix, f32 + r0 * n_pix, bf16 + r0 * ld * 2,
-                                   ld, sq + r0, nullptr, sv);
+                                   ld, sq + r0, nullptr, is);
+      if (st == SPF_OK) st = spf::check_cuda(cudaEventRecord(ingested, is), "spf_match_bf16_host");
+      if (st == SPF_OK)
+        st = spf::check_cuda(cudaStreamWaitEvent(s, ingested, 0), "spf_match_bf16_host");
       if (st == SPF_OK)
         st = spf_dist_topk_bf16(bf16 + r0 * ld * 2, n, d_ref_bf16, n_ref, n_pix, ld, d_ref_sq,
-                                cand_d + k * cslot, cand_i + k * cslot, sv);
+                                cand_at(cand_d, k), cand_at(cand_i, k), sv);
       if (st == SPF_OK)
-        st = spf_rerank_fp32_keep(cand_d + k * cslot, cand_i + k * cslot, tiles, f32 + r0 * n_pix,
+        st = spf_rerank_fp32_keep(cand_at(cand_d, k), cand_at(cand_i, k), tiles, f32 + r0 * n_pix,
                                   sq + r0, n, d_ref, d_ref_sq, d_ref_m2, ref_sq_max, n_ref, n_pix,
                                   0, work + r0, idx + r0, dist + r0, unc + r0, mrg_d + r0 * 8,
                                   mrg_i + r0 * 8, sv);
@@ -151,7 +190,7 @@ extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
     constexpr int CAP = 512;
     std::vector<int64_t> rows_g, rows_l, off(n_chunks + 1, 0);
     for (int64_t k = 0; k < n_chunks; ++k) {
-      const int64_t r0 = k * chunk, n = std::min(chunk, n_img - r0);
+      const int64_t r0 = plan[k].first, n = plan[k].second;
       off[k] = (int64_t)rows_g.size();
       for (int64_t i = 0; i < n; ++i)
         if (h_unc[r0 + i]) {
@@ -186,8 +225,8 @@ extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
       for (int64_t k = 0; st == SPF_OK && k < n_chunks; ++k) {
         const int64_t nk = off[k + 1] - off[k];
         if (!nk) continue;
-        const int64_t n = std::min(chunk, n_img - k * chunk);
-        st = spf_scan_band_bf16(cand_d + k * cslot, cand_i + k * cslot, tiles, n, d_rl + off[k], nk,
+        const int64_t n = plan[k].second;
+        st = spf_scan_band_bf16(cand_at(cand_d, k), cand_at(cand_i, k), tiles, n, d_rl + off[k], nk,
                                 thr_c + off[k], lst + off[k] * CAP, cnt + off[k], CAP, sv);
       }
       if (st == SPF_OK) st = spf_best_init(best, nb, sv);
@@ -212,7 +251,7 @@ extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
         }
       // the rare frames whose tile lists may hide references, per chunk
       for (int64_t k = 0; st == SPF_OK && k < n_chunks; ++k) {
-        const int64_t r0 = k * chunk, n = std::min(chunk, n_img - r0);
+        const int64_t r0 = plan[k].first, n = plan[k].second;
         std::vector<int64_t> ov;
         for (int64_t j = off[k]; j < off[k + 1]; ++j)
           if (h_cnt[j] > CAP) ov.push_back(rows_l[j]);
@@ -224,7 +263,7 @@ extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
         st = spf::check_cuda(cudaMemcpyAsync(d_rl, ov.data(), no * 8, cudaMemcpyHostToDevice, s),
                              "spf_match_bf16_host");
         if (st == SPF_OK)
-          st = spf_complete_open(cand_d + k * cslot, cand_i + k * cslot, tiles, bf16 + r0 * ld * 2,
+          st = spf_complete_open(cand_at(cand_d, k), cand_at(cand_i, k), tiles, bf16 + r0 * ld * 2,
                                  f32 + r0 * n_pix, sq + r0, work + r0, n, d_rl, no, d_ref_bf16,
                                  d_ref, d_ref_sq, n_ref, n_pix, ld, idx2, dist2, hs, sv);
         if (st == SPF_OK)
@@ -248,8 +287,9 @@ extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
       h_stats[2] = n_plain;
     }
   }
-  cudaStreamSynchronize(s);  // the scratch frees are ordered before the copy stream goes
+  cudaStreamSynchronize(s);  // the scratch frees are ordered before the streams go
   for (cudaEvent_t e : ev) cudaEventDestroy(e);
-  if (cs) cudaStreamDestroy(cs);
+  for (cudaStream_t x : {cs, is})
+    if (x) cudaStreamDestroy(x);
   return st;
 }

@@ -315,19 +315,26 @@ __global__ void k_row_sqnorm(const float *__restrict__ x, int64_t n_rows, int64_
   }
 }
 
-// uint16 counts -> f32 (+ bf16) (+ squared norm, 4-norm); one warp per frame.
-// The squared norm of integer counts is summed exactly in 64-bit integers
-// (at most 65535^2 * n_pix, far below 2^64) and rounded once to float, the
-// same value an exact FP64 sum gives; the 4-norm (FP64) is only computed when
-// asked for.  Rows move as 16-byte vectors (8 counts) when aligned.
-__global__ void k_ingest_u16(const uint16_t *__restrict__ in, int64_t n_img, int64_t n_pix,
-                             float *__restrict__ f32, __nv_bfloat16 *__restrict__ bf, int64_t ld,
-                             float *__restrict__ sq, float *__restrict__ n4, int vec) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  int nwarps = (gridDim.x * blockDim.x) >> 5;
+// uint16 counts -> f32 (+ bf16) (+ squared norm, 4-norm); one CTA of 256
+// threads per frame (a warp per frame left 10,000 frames in just over one
+// wave of resident warps, half the time spent in the tail).  The squared norm
+// of integer counts is summed exactly in 64-bit integers (at most 65535^2 *
+// n_pix, far below 2^64) and rounded once to float, the same value an exact
+// FP64 sum gives; the 4-norm (FP64) is only computed when asked for.  Rows
+// move as 16-byte vectors (8 counts) when aligned, four loads in flight per
+// thread.
+constexpr int INGEST_THREADS = 256;
+
+__global__ void __launch_bounds__(INGEST_THREADS)
+    k_ingest_u16(const uint16_t *__restrict__ in, int64_t n_img, int64_t n_pix,
+                 float *__restrict__ f32, __nv_bfloat16 *__restrict__ bf, int64_t ld,
+                 float *__restrict__ sq, float *__restrict__ n4, int vec) {
+  constexpr int NW = INGEST_THREADS / 32;
+  __shared__ unsigned long long sh2[NW];
+  __shared__ double sh4[NW];
+  const int t = (int)threadIdx.x, lane = t & 31, wid = t >> 5;
   const bool want4 = n4 != nullptr;
-  for (int64_t r = warp; r < n_img; r += nwarps) {
+  for (int64_t r = blockIdx.x; r < n_img; r += gridDim.x) {
     const uint16_t *p = in + r * n_pix;
     unsigned long long s2 = 0;
     double s4 = 0.0;
@@ -336,37 +343,46 @@ __global__ void k_ingest_u16(const uint16_t *__restrict__ in, int64_t n_img, int
       float4 *fv = reinterpret_cast<float4 *>(f32 + r * n_pix);
       uint4 *bv = bf ? reinterpret_cast<uint4 *>(bf + r * ld) : nullptr;
       const int64_t n8 = n_pix / 8;
-      for (int64_t k = lane; k < n8; k += 32) {
-        const uint4 raw = __ldg(pv + k);
-        const uint32_t w[4] = {raw.x, raw.y, raw.z, raw.w};
-        float v[8];
+      constexpr int U = 4;
+      for (int64_t k0 = t; k0 < n8; k0 += INGEST_THREADS * U) {
+        uint4 raw[U];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const uint32_t lo = w[q] & 0xffffu, hi = w[q] >> 16;
-          v[2 * q] = (float)lo;
-          v[2 * q + 1] = (float)hi;
-          s2 += (unsigned long long)(lo * lo) + (unsigned long long)(hi * hi);
-          if (want4) {
-            const double a = (double)lo * (double)lo, b = (double)hi * (double)hi;
-            s4 = fma(a, a, s4);
-            s4 = fma(b, b, s4);
-          }
-        }
-        fv[2 * k] = make_float4(v[0], v[1], v[2], v[3]);
-        fv[2 * k + 1] = make_float4(v[4], v[5], v[6], v[7]);
-        if (bv) {
-          uint4 o;
-          uint32_t *ow = reinterpret_cast<uint32_t *>(&o);
+        for (int u = 0; u < U; ++u)
+          if (k0 + INGEST_THREADS * u < n8) raw[u] = __ldg(pv + k0 + INGEST_THREADS * u);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int64_t k = k0 + INGEST_THREADS * u;
+          if (k >= n8) break;
+          const uint32_t w[4] = {raw[u].x, raw[u].y, raw[u].z, raw[u].w};
+          float v[8];
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
-            ow[q] = *reinterpret_cast<uint32_t *>(&h);
+            const uint32_t lo = w[q] & 0xffffu, hi = w[q] >> 16;
+            v[2 * q] = (float)lo;
+            v[2 * q + 1] = (float)hi;
+            s2 += (unsigned long long)(lo * lo) + (unsigned long long)(hi * hi);
+            if (want4) {
+              const double a = (double)lo * (double)lo, b = (double)hi * (double)hi;
+              s4 = fma(a, a, s4);
+              s4 = fma(b, b, s4);
+            }
           }
-          bv[k] = o;
+          fv[2 * k] = make_float4(v[0], v[1], v[2], v[3]);
+          fv[2 * k + 1] = make_float4(v[4], v[5], v[6], v[7]);
+          if (bv) {
+            uint4 o;
+            uint32_t *ow = reinterpret_cast<uint32_t *>(&o);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+              ow[q] = *reinterpret_cast<uint32_t *>(&h);
+            }
+            bv[k] = o;
+          }
         }
       }
     } else {
-      for (int64_t k = lane; k < n_pix; k += 32) {
+      for (int64_t k = t; k < n_pix; k += INGEST_THREADS) {
         const uint32_t c = p[k];
         const float v = (float)c;
         f32[r * n_pix + k] = v;
@@ -379,16 +395,29 @@ __global__ void k_ingest_u16(const uint16_t *__restrict__ in, int64_t n_img, int
       }
     }
     if (bf)
-      for (int64_t k = n_pix + lane; k < ld; k += 32) bf[r * ld + k] = __float2bfloat16_rn(0.0f);
+      for (int64_t k = n_pix + t; k < ld; k += INGEST_THREADS)
+        bf[r * ld + k] = __float2bfloat16_rn(0.0f);
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
       s2 += __shfl_xor_sync(0xffffffffu, s2, o);
       if (want4) s4 += __shfl_xor_sync(0xffffffffu, s4, o);
     }
     if (lane == 0) {
-      if (sq) sq[r] = __ull2float_rn(s2);
-      if (n4) n4[r] = (float)sqrt(s4);
+      sh2[wid] = s2;
+      sh4[wid] = s4;
     }
+    __syncthreads();
+    if (t == 0) {
+      unsigned long long a2 = 0;
+      double a4 = 0.0;
+      for (int w = 0; w < NW; ++w) {
+        a2 += sh2[w];
+        a4 += sh4[w];
+      }
+      if (sq) sq[r] = __ull2float_rn(a2);
+      if (n4) n4[r] = (float)sqrt(a4);
+    }
+    __syncthreads();  // the partial sums are reused by the next frame
   }
 }
 
@@ -574,10 +603,11 @@ int spf_frames_ingest_u16(const uint16_t *d_counts, int64_t n_img, int64_t n_pix
   SPF_REQUIRE(!d_bf16 || ld >= n_pix, "spf_frames_ingest_u16: ld < n_pix");
   if (n_img == 0 || n_pix == 0) return SPF_OK;
   SPF_REQUIRE(d_counts && d_f32, "spf_frames_ingest_u16: NULL pointer");
-  int blocks = grid_for(n_img * 32, 256, (int64_t)sm_count() * 32);
+  // one CTA per frame; frames beyond 2^24 are taken by a grid-stride loop
+  const int blocks = (int)std::min<int64_t>(n_img, int64_t(1) << 24);
   const int vec = n_pix % 8 == 0 && aligned(d_counts, 16) && aligned(d_f32, 16) &&
                   (!d_bf16 || (aligned(d_bf16, 16) && ld % 8 == 0));
-  k_ingest_u16<<<blocks, 256, 0, as_stream(stream)>>>(
+  k_ingest_u16<<<blocks, INGEST_THREADS, 0, as_stream(stream)>>>(
       d_counts, n_img, n_pix, d_f32, reinterpret_cast<__nv_bfloat16 *>(d_bf16), ld, d_sq, d_n4,
       vec);
   return check_launch("spf_frames_ingest_u16");

@@ -348,8 +348,10 @@ def match_bf16_host(frames_u16_host: torch.Tensor, refs: ReferenceSet, chunk_fra
     """Host frames in, host indices out, in one library call
     (spf_match_bf16_host): chunked host -> device copies overlapped with the
     tensor-core matching of the previous chunk.  frames_u16_host: [n, n_pix]
-    16-bit counts in host memory (pinned for the overlap).  Returns numpy
-    (indices int32, distances float32), the plain FP32 path's answer."""
+    16-bit counts in host memory (pinned for the overlap).  chunk_frames > 0:
+    fixed chunks; 0: fixed chunks of 2,560 frames; < 0: chunks doubling
+    from -chunk_frames.  Returns numpy (indices int32, distances float32), the
+    plain FP32 path's answer."""
     if frames_u16_host.is_cuda or frames_u16_host.dtype not in (torch.int16, torch.uint16):
         raise TypeError("frames must be 16-bit counts in host memory")
     if frames_u16_host.dim() != 2 or frames_u16_host.shape[1] != refs.n_pix:

@@ -125,7 +125,7 @@ def test_native_server_rejects_bad_requests(world):
         assert ok.result(timeout=60).shape == (3,)
 
 
-@pytest.mark.parametrize("chunk", [0, 300, 1200])
+@pytest.mark.parametrize("chunk", [0, -100, 300, 1200])
 def test_host_batch_call_equals_plain_fp32(world, chunk):
     """spf_match_bf16_host (chunked copies overlapped with matching, each
     chunk's open frames completed from its kept tile lists): indices and
