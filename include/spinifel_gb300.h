@@ -63,9 +63,11 @@ int spf_selftest_bounded_wait(int64_t timeout_ms, int *d_result, void *stream);
  *                           (default, when M - 1 is 2,3,5,7-smooth),
  *                           2 = cuFFT D2Z / Z2D
  *   SPF_TUNE_SLICE_SHAPE  : tile shape of spf_slice_t2_det (patch and warp
- *                           block, codes 0..5; default 0 = 16 x 16 patches
- *                           of 4 x 8 warp blocks); every shape gives the
- *                           same bits
+ *                           block, codes 0..5; 6 and 7 are shapes 0 and 1
+ *                           with a per-CTA choice of the shared box's
+ *                           strides against bank conflicts; default 0 =
+ *                           16 x 16 patches of 4 x 8 warp blocks); every
+ *                           shape gives the same bits
  *   SPF_TUNE_SORT_ITEM    : points per work item of the bin-sorted passes
  *                           (read by spf_nufft_sort_orient /
  *                           spf_nufft_sort_points; default 2048,

@@ -146,7 +146,9 @@ def tune_fp32(frames_f32, frames_sq, refs, group_sizes=(4, 8, 16), reps=1, force
 
 SLICE_SHAPES = {0: "16x16 patch, 4x8 warps", 1: "16x16 patch, 8x4 warps",
                 2: "8x32 patch, 2x16 warps", 3: "8x32 patch, 4x8 warps",
-                4: "32x8 patch, 8x4 warps", 5: "32x8 patch, 16x2 warps"}
+                4: "32x8 patch, 8x4 warps", 5: "32x8 patch, 16x2 warps",
+                6: "16x16 patch, 4x8 warps, stride search",
+                7: "16x16 patch, 8x4 warps, stride search"}
 
 
 def tune_slice(plan, quats, ppr, scale: float, det_shape, reps=2, force=False):

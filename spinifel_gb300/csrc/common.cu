@@ -86,7 +86,7 @@ int spf_tune_set(int param, int64_t value) {
   if (param == SPF_TUNE_PRIME_DFT)
     SPF_REQUIRE(value >= 0 && value <= 2, "spf_tune_set: prime DFT choice is 0, 1 or 2");
   if (param == SPF_TUNE_SLICE_SHAPE)
-    SPF_REQUIRE(value >= 0 && value <= 5, "spf_tune_set: slicing tile shape is 0 .. 5");
+    SPF_REQUIRE(value >= 0 && value <= 7, "spf_tune_set: slicing tile shape is 0 .. 7");
   if (param == SPF_TUNE_SORT_ITEM)
     SPF_REQUIRE(value == 0 || (value >= 256 && value <= 8192),
                 "spf_tune_set: sort item size is 256 .. 8192 (0 = default)");

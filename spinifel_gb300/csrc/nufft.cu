@@ -377,29 +377,42 @@ constexpr int SLICE_SMEM_FLOATS = 11264;  // 44 KB
 // conflicts) and the box's size; which is fastest depends on the detector's
 // pixel spacing in grid cells, so the autotuner picks it
 // (SPF_TUNE_SLICE_SHAPE).  Every shape gives the same bits.
+//
+// search picks the box's row and plane strides per CTA: a lane's W^3 loads
+// all sit at fixed offsets from its footprint start, so the bank of that
+// start, ((li * sj + lj) * sk + lk) mod 32, fixes the warp's bank conflicts
+// for the whole interpolation.  The CTA scores 16 candidate strides (sj = dj
+// + 0..3, sk = dk + 0..3) by the number of distinct banks its warps'
+// footprint starts hit (one warp-wide OR of bank bits per candidate) and
+// keeps the best one that fits in shared memory.
 struct PatchShape {
-  int px, py, wx, wy;
+  int px, py, wx, wy, search;
 };
-constexpr int N_SLICE_SHAPES = 6;
+constexpr int N_SLICE_SHAPES = 8;
+constexpr int SLICE_SEARCH = 4;  // candidates per stride
 __host__ __device__ inline PatchShape slice_shape(int code) {
   switch (code) {
-    case 1: return PatchShape{16, 16, 8, 4};
-    case 2: return PatchShape{8, 32, 2, 16};
-    case 3: return PatchShape{8, 32, 4, 8};
-    case 4: return PatchShape{32, 8, 8, 4};
-    case 5: return PatchShape{32, 8, 16, 2};
-    default: return PatchShape{16, 16, 4, 8};
+    case 1: return PatchShape{16, 16, 8, 4, 0};
+    case 2: return PatchShape{8, 32, 2, 16, 0};
+    case 3: return PatchShape{8, 32, 4, 8, 0};
+    case 4: return PatchShape{32, 8, 8, 4, 0};
+    case 5: return PatchShape{32, 8, 16, 2, 0};
+    case 6: return PatchShape{16, 16, 4, 8, 1};
+    case 7: return PatchShape{16, 16, 8, 4, 1};
+    default: return PatchShape{16, 16, 4, 8, 0};
   }
 }
 
-template <int W>
+template <int W, bool SEARCH>
 __global__ void __launch_bounds__(256)
     k_slice_t2_det(const float *__restrict__ re_pad, GridGeom g, const float *__restrict__ quats,
                    const float *__restrict__ ppr, int n_panels, int nx, int ny, float scale1,
                    float scale2, float scale3, float *__restrict__ out,
                    __nv_bfloat16 *__restrict__ out_bf16, PatchShape ps) {
   __shared__ float box[SLICE_SMEM_FLOATS];
-  __shared__ int bb[6];
+  constexpr int NCAND = SLICE_SEARCH * SLICE_SEARCH;
+  __shared__ int bb[7];
+  __shared__ int score[8][NCAND];
   const int64_t o = blockIdx.x;
   const int patches_y = (ny + ps.py - 1) / ps.py;
   const int patches_x = (nx + ps.px - 1) / ps.px;
@@ -444,7 +457,41 @@ __global__ void __launch_bounds__(256)
   const int imin = bb[0], jmin = bb[1], kmin = bb[2];
   const int di = bb[3] - imin + W, dj = bb[4] - jmin + W, dk = bb[5] - kmin + W;
   // odd row strides spread neighbouring points' rows over the banks
-  const int sj = dj | 1, sk = dk | 1;
+  int sj = dj | 1, sk = dk | 1;
+  if (SEARCH && bb[3] >= imin) {
+    const int li = i0 - imin, lj = j0 - jmin, lk = k0 - kmin;
+    const unsigned vmask = valid ? 0xffffffffu : 0u;
+    unsigned mine = 0;  // lane c keeps candidate c's bank bits
+#pragma unroll
+    for (int a = 0; a < SLICE_SEARCH; ++a) {
+      const int r = li * (dj + a) + lj;
+      int start = r * dk + lk;
+#pragma unroll
+      for (int b = 0; b < SLICE_SEARCH; ++b) {
+        const unsigned m = __reduce_or_sync(0xffffffffu, (1u << (start & 31)) & vmask);
+        if (lane == a * SLICE_SEARCH + b) mine = m;
+        start += r;
+      }
+    }
+    if (lane < NCAND) score[warp][lane] = __popc(mine);
+    __syncthreads();
+    if (warp == 0) {
+      const int sjc = dj + lane / SLICE_SEARCH, skc = dk + lane % SLICE_SEARCH;
+      int tot = 0;
+      if (lane < NCAND)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += score[w][lane];
+      const bool fits = lane < NCAND && (int64_t)di * sjc * skc <= SLICE_SMEM_FLOATS;
+      // most distinct banks; ties go to the lower candidate (the smaller box)
+      const int key = fits ? (tot << 5) | (31 - lane) : -1;
+      const int best = __reduce_max_sync(0xffffffffu, key);
+      if (lane == 0) bb[6] = best < 0 ? -1 : 31 - (best & 31);
+    }
+    __syncthreads();
+    if (bb[6] >= 0) {
+      sj = dj + bb[6] / SLICE_SEARCH;
+      sk = dk + bb[6] % SLICE_SEARCH;
+    }
+  }
   const int64_t svol = (int64_t)di * sj * sk;
   float acc = 0.0f;
   if (bb[3] >= imin && svol <= SLICE_SMEM_FLOATS) {
@@ -1289,9 +1336,15 @@ int spf_slice_t2_det(spf_nufft_plan P, const float *d_quats, int64_t n_orient, c
   float s3 = (float)(scale * P->n[2] / (2.0 * M_PI));
   dim3 grid((unsigned)n_orient, (unsigned)patches);
   auto *bf = reinterpret_cast<__nv_bfloat16 *>(d_out_bf16);
-  SPF_W_DISPATCH(P->w, (k_slice_t2_det<W><<<grid, 256, 0, s>>>(P->re_pad, g, d_quats, d_ppr,
-                                                                  n_panels, nx, ny, s1, s2, s3,
-                                                                  d_out, bf, ps)));
+  if (ps.search) {
+    SPF_W_DISPATCH(P->w, (k_slice_t2_det<W, true><<<grid, 256, 0, s>>>(
+                             P->re_pad, g, d_quats, d_ppr, n_panels, nx, ny, s1, s2, s3, d_out,
+                             bf, ps)));
+  } else {
+    SPF_W_DISPATCH(P->w, (k_slice_t2_det<W, false><<<grid, 256, 0, s>>>(
+                             P->re_pad, g, d_quats, d_ppr, n_panels, nx, ny, s1, s2, s3, d_out,
+                             bf, ps)));
+  }
   return check_launch("k_slice_t2_det");
 }
 

@@ -201,7 +201,7 @@ def test_patch_slicing_identical_to_point_slicing(dev, det):
     P.set_modes(t(model, dev))
     a = P.slice(t(quats, dev), ppr_t, np.pi / pdr.max())
     try:
-        for shape in range(6):
+        for shape in range(8):
             _lib.call("spf_tune_set", _lib.SPF_TUNE_SLICE_SHAPE, shape)
             b = P.slice(t(quats, dev), ppr_t, np.pi / pdr.max(), det_shape=det)
             assert torch.equal(a, b), shape
