@@ -346,6 +346,63 @@ __device__ __forceinline__ void box_load(float *box, const float *__restrict__ g
   }
 }
 
+// Box fill with 16-byte loads, for a padded grid whose rows are 16-byte
+// aligned (p3 % 4 == 0): each box row [kmin, kmin + dk) is read as the
+// aligned quads from kmin & ~3, which never leave the grid row; unit (row,
+// quad) goes to thread unit mod blockDim.x, four loads in flight, and each
+// quad stores the cells that lie inside the box row.  Fills the same cells
+// with the same values as box_load, in about a third of the instructions.
+__device__ __forceinline__ void box_load_q(float *box, const float *__restrict__ grid,
+                                           const GridGeom &g, const BoxShape &b) {
+  constexpr int U = 2;
+  const int lead = b.kmin & 3;
+  const int nq = (lead + b.dk + 3) >> 2;
+  const int units = b.di * b.dj * nq;
+  const int nt = blockDim.x;
+  const int p3q = g.p3 >> 2, p2q = g.p2 * p3q;
+  const float4 *base = reinterpret_cast<const float4 *>(
+      grid + ((size_t)b.imin * g.p2 + b.jmin) * g.p3 + (b.kmin - lead));
+  int u = threadIdx.x;
+  int q = u % nq, r = u / nq;
+  int jj = r % b.dj, ii = r / b.dj;
+  const int stq = nt % nq, str = nt / nq;
+  const int stj = str % b.dj, sti = str / b.dj;
+  while (u < units) {
+    float4 v[U];
+    int row[U], c0[U];
+    bool ok[U];
+#pragma unroll
+    for (int x = 0; x < U; ++x) {
+      ok[x] = u < units;
+      row[x] = ii * b.sp + jj * b.sr;
+      c0[x] = 4 * q - lead;
+      if (ok[x]) v[x] = __ldg(base + (ii * p2q + jj * p3q + q));
+      u += nt;
+      q += stq;
+      jj += stj;
+      ii += sti;
+      if (q >= nq) {
+        q -= nq;
+        ++jj;
+      }
+      if (jj >= b.dj) {
+        jj -= b.dj;
+        ++ii;
+      }
+    }
+#pragma unroll
+    for (int x = 0; x < U; ++x) {
+      if (!ok[x]) continue;
+      const float e[4] = {v[x].x, v[x].y, v[x].z, v[x].w};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int c = c0[x] + t;
+        if (c >= 0 && c < b.dk) box[row[x] + c] = e[t];
+      }
+    }
+  }
+}
+
 __device__ __forceinline__ void box_flush(const float *box, float *__restrict__ grid,
                                           const GridGeom &g, const BoxShape &b) {
   box_rows(b, [&](int ii, int jj, int kk, int s) {
@@ -495,7 +552,11 @@ __global__ void __launch_bounds__(256)
   const int64_t svol = (int64_t)di * sj * sk;
   float acc = 0.0f;
   if (bb[3] >= imin && svol <= SLICE_SMEM_FLOATS) {
-    box_load(box, re_pad, g, BoxShape{imin, jmin, kmin, di, dj, dk, sj * sk, sk});
+    const BoxShape shape{imin, jmin, kmin, di, dj, dk, sj * sk, sk};
+    if ((g.p3 & 3) == 0)
+      box_load_q(box, re_pad, g, shape);
+    else
+      box_load(box, re_pad, g, shape);
     __syncthreads();
     // only valid points' footprints are inside the box
     if (!valid) return;
@@ -1200,6 +1261,9 @@ int spf_nufft_plan_create(int m1, int m2, int m3, double eps, double upsampfac,
     P->n[d] = next_smooth_even(want);
     P->np[d] = P->n[d] + 2 * P->pad;
   }
+  // rows of the padded grid start on 16-byte boundaries (the slicing box is
+  // filled with 16-byte loads); the extra cells are never inside a footprint
+  P->np[2] = (P->np[2] + 3) & ~3;
   int st = SPF_OK;
   size_t nfine = (size_t)P->n[0] * P->n[1] * P->n[2];
   size_t npad = (size_t)P->np[0] * P->np[1] * P->np[2];
