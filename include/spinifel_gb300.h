@@ -71,13 +71,20 @@ int spf_selftest_bounded_wait(int64_t timeout_ms, int *d_result, void *stream);
  *   SPF_TUNE_SORT_ITEM    : points per work item of the bin-sorted passes
  *                           (read by spf_nufft_sort_orient /
  *                           spf_nufft_sort_points; default 2048,
- *                           256 .. 8192) */
+ *                           256 .. 8192)
+ *   SPF_TUNE_STATIC_ABORT_TEST : 1 makes spf_match_bf16_static record a
+ *                           given-up GEMM wait (SPF_ERR_TIMEOUT in its
+ *                           error word, after the GEMM) so that tests can
+ *                           check the void answers and the report through
+ *                           spf_device_error without a device hang; 0
+ *                           (default) in production */
 #define SPF_TUNE_BF16_GROUP_M 1
 #define SPF_TUNE_FP32_GROUP_M 2
 #define SPF_TUNE_BF16_GRID 3
 #define SPF_TUNE_PRIME_DFT 4
 #define SPF_TUNE_SLICE_SHAPE 5
 #define SPF_TUNE_SORT_ITEM 6
+#define SPF_TUNE_STATIC_ABORT_TEST 7
 int spf_tune_set(int param, int64_t value);
 int spf_tune_get(int param, int64_t *value);
 

@@ -31,6 +31,7 @@ SPF_TUNE_BF16_GRID = 3
 SPF_TUNE_PRIME_DFT = 4
 SPF_TUNE_SLICE_SHAPE = 5
 SPF_TUNE_SORT_ITEM = 6
+SPF_TUNE_STATIC_ABORT_TEST = 7
 
 
 class SpfError(RuntimeError):

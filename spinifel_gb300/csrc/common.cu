@@ -82,7 +82,9 @@ const char *spf_last_error(void) { return spf::get_error(); }
 uint64_t spf_launch_count(void) { return spf::g_launches.load(); }
 
 int spf_tune_set(int param, int64_t value) {
-  SPF_REQUIRE(param >= 1 && param <= 6, "spf_tune_set: unknown parameter %d", param);
+  SPF_REQUIRE(param >= 1 && param <= 7, "spf_tune_set: unknown parameter %d", param);
+  if (param == SPF_TUNE_STATIC_ABORT_TEST)
+    SPF_REQUIRE(value == 0 || value == 1, "spf_tune_set: the abort test switch is 0 or 1");
   if (param == SPF_TUNE_PRIME_DFT)
     SPF_REQUIRE(value >= 0 && value <= 2, "spf_tune_set: prime DFT choice is 0, 1 or 2");
   if (param == SPF_TUNE_SLICE_SHAPE)
@@ -104,7 +106,7 @@ int spf_tune_set(int param, int64_t value) {
 }
 
 int spf_tune_get(int param, int64_t *value) {
-  SPF_REQUIRE(param >= 1 && param <= 6 && value, "spf_tune_get: bad arguments");
+  SPF_REQUIRE(param >= 1 && param <= 7 && value, "spf_tune_get: bad arguments");
   *value = spf::tune_get(param, 0);
   return SPF_OK;
 }

@@ -1359,6 +1359,13 @@ static __device__ __align__(256) unsigned char g_match_scratch[STATIC_SCRATCH_BY
 
 // After a GEMM that gave up a bounded wait (*err != 0): idx -1, distance
 // NaN and uncertified for every frame of the call.
+// Test hook (SPF_TUNE_STATIC_ABORT_TEST): records a given-up wait, as the
+// GEMM's own timeout path does, so that the void answers and their report
+// can be checked without making any wait run out.
+__global__ void k_static_inject_timeout(unsigned int *__restrict__ err) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) atomicExch(err, (unsigned int)(-SPF_ERR_TIMEOUT));
+}
+
 __global__ void k_static_abort_mark(const unsigned int *__restrict__ err, int64_t n_img,
                                     int32_t *__restrict__ idx, float *__restrict__ dist,
                                     int32_t *__restrict__ unc) {
@@ -1471,6 +1478,10 @@ extern "C" int spf_match_bf16_static(const void *d_img_bf16, const float *d_img,
                                                             n_pix, cand_d, cand_i, nullptr,
                                                             nullptr, nullptr, 0, GROUP_M, err);
   SPF_TRY(check_launch("k_dist_topk_bf16 (static scratch)"));
+  if (tune_get(SPF_TUNE_STATIC_ABORT_TEST, 0)) {
+    k_static_inject_timeout<<<1, 32, 0, s>>>(err);
+    SPF_TRY(check_launch("k_static_inject_timeout"));
+  }
   k_merge_top8<<<(unsigned)n_img, RR_THREADS, 0, s>>>(cand_d, cand_i, tiles, d_img, n_img,
                                                       d_ref_m2, n_pix, work, cand_d, cand_i);
   SPF_TRY(check_launch("k_merge_top8 (static scratch)"));

@@ -90,11 +90,13 @@ def test_tunables_validated_without_a_device(lib):
     v = ctypes.c_int64(-1)
     assert lib.spf_tune_set(_lib.SPF_TUNE_PRIME_DFT, 3) == _lib.SPF_ERR_ARG
     assert lib.spf_tune_set(_lib.SPF_TUNE_PRIME_DFT, -1) == _lib.SPF_ERR_ARG
-    assert lib.spf_tune_set(7, 1) == _lib.SPF_ERR_ARG
+    assert lib.spf_tune_set(8, 1) == _lib.SPF_ERR_ARG
+    assert lib.spf_tune_set(_lib.SPF_TUNE_STATIC_ABORT_TEST, 2) == _lib.SPF_ERR_ARG
     assert lib.spf_tune_set(_lib.SPF_TUNE_SLICE_SHAPE, 8) == _lib.SPF_ERR_ARG
     assert lib.spf_tune_set(_lib.SPF_TUNE_SORT_ITEM, 100) == _lib.SPF_ERR_ARG
     assert lib.spf_tune_set(_lib.SPF_TUNE_SORT_ITEM, 8193) == _lib.SPF_ERR_ARG
-    for param, value in ((_lib.SPF_TUNE_SLICE_SHAPE, 7), (_lib.SPF_TUNE_SORT_ITEM, 1024)):
+    for param, value in ((_lib.SPF_TUNE_SLICE_SHAPE, 7), (_lib.SPF_TUNE_SORT_ITEM, 1024),
+                         (_lib.SPF_TUNE_STATIC_ABORT_TEST, 1)):
         assert lib.spf_tune_set(param, value) == _lib.SPF_OK
         assert lib.spf_tune_get(param, ctypes.byref(v)) == _lib.SPF_OK and v.value == value
         assert lib.spf_tune_set(param, 0) == _lib.SPF_OK

@@ -79,6 +79,45 @@ def test_static_scratch_entry_point_matches_allocating_path(lib):
         assert torch.equal(unc, runc)
 
 
+def test_static_scratch_abort_is_reported_and_voids_the_call(lib):
+    """A GEMM that gave up a bounded wait (recorded by the library's test hook
+    right after the GEMM, as the kernel's own timeout path records it): every
+    frame of the call comes back void (index -1, distance NaN, uncertified)
+    and spf_device_error reports SPF_ERR_TIMEOUT once; the next call is
+    exact again."""
+    from spinifel_gb300 import _lib, matching
+
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(91)
+    n_ref, n_pix = 1000, 1024
+    refs = rng.gamma(0.5, 1.0, (n_ref, n_pix)).astype(np.float32)
+    rs = matching.ReferenceSet(torch.as_tensor(refs, device=dev))
+    pick = rng.integers(0, n_ref, 50)
+    fr = matching.FrameSet(torch.as_tensor(rng.poisson(refs[pick]).astype(np.float32), device=dev))
+    out = (torch.zeros(fr.n, dtype=torch.int32, device=dev),
+           torch.zeros(fr.n, dtype=torch.float32, device=dev),
+           torch.zeros(fr.n, dtype=torch.int32, device=dev))
+    code = ctypes.c_int(-1)
+    _lib.call("spf_device_error", _lib.stream_handle(), ctypes.byref(code))  # start clean
+    _lib.call("spf_tune_set", _lib.SPF_TUNE_STATIC_ABORT_TEST, 1)
+    try:
+        _static(_lib, fr, rs, *out)
+    finally:
+        _lib.call("spf_tune_set", _lib.SPF_TUNE_STATIC_ABORT_TEST, 0)
+    idx, dist, unc = out
+    assert bool((idx == -1).all())
+    assert bool(torch.isnan(dist).all())
+    assert bool((unc == 1).all())
+    _lib.call("spf_device_error", _lib.stream_handle(), ctypes.byref(code))
+    assert code.value == -_lib.SPF_ERR_TIMEOUT
+    _lib.call("spf_device_error", _lib.stream_handle(), ctypes.byref(code))
+    assert code.value == 0  # reported once, then cleared
+    _static(_lib, fr, rs, *out)
+    ridx, rdist, runc = _allocating(_lib, fr, rs)
+    assert torch.equal(out[0], ridx) and torch.equal(out[1], rdist)
+    assert torch.equal(out[2], runc)
+
+
 def test_static_scratch_entry_point_rejects_oversize(lib):
     from spinifel_gb300 import _lib
 
