@@ -19,7 +19,9 @@ cpu_baseline: the reference's CPU matching (sklearn-form FP64 distances +
         100,000 references on the host cores, measured, not extrapolated.
 
 `--impl reference` times that CPU implementation alone as the reference arm
-(each step: 32 frames against all 100,000 references).
+(each step: 32 frames against all 100,000 references).  Other workloads
+(--workload merge | nufft | serving | phasing | eval | ingest | gemm) measure
+the paths around the matching step and single kernels.
 """
 from __future__ import annotations
 
@@ -665,6 +667,65 @@ def run_eval(args):
     print(json.dumps(out), flush=True)
 
 
+def run_gemm(args):
+    """The tcgen05 distance GEMM + per-tile top-8 alone (spf_dist_topk_bf16) on
+    random bf16 operands, 10,000 frames x 8,192 references x 65,536 pixels by
+    default (--n-img / --n-ref override): the kernel's steady state without the
+    slicing, the re-rank or the completion, for profiling and its roofline."""
+    import ctypes
+
+    import torch
+
+    from spinifel_gb300 import _lib
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    n_img = args.n_img or 10_000
+    n_ref = args.n_ref or 8_192
+    n_pix = 65_536
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(20261204)
+    a = torch.empty(n_img, n_pix, device=dev).exponential_(2.0, generator=gen).to(torch.bfloat16)
+    b = torch.empty(n_ref, n_pix, device=dev).exponential_(2.0, generator=gen).to(torch.bfloat16)
+    bsq = b.float().pow(2).sum(1).contiguous()
+    tiles = int(_lib.lib().spf_dist_topk_bf16_tiles(n_ref))
+    cd = torch.empty(tiles * n_img * 8, device=dev)
+    ci = torch.empty(tiles * n_img * 8, dtype=torch.int32, device=dev)
+
+    def launch():
+        _lib.call("spf_dist_topk_bf16", _lib.ptr(a), n_img, _lib.ptr(b), n_ref, n_pix, n_pix,
+                  _lib.ptr(bsq), _lib.ptr(cd), _lib.ptr(ci), _lib.stream_handle())
+
+    for _ in range(args.warmup):
+        launch()
+    torch.cuda.synchronize()
+    ms = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(args.steps):
+        e0.record()
+        launch()
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    code = ctypes.c_int(-1)
+    _lib.call("spf_device_error", _lib.stream_handle(), ctypes.byref(code))
+    if code.value:
+        raise RuntimeError(f"device error {code.value}")
+    k_ms = float(np.median(ms))
+    flops = 2.0 * n_img * n_ref * n_pix
+    peaks, peak_src = load_peaks()
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    tf = flops / (k_ms / 1e3) / 1e12
+    out = {"metric": "tcgen05 distance GEMM + top-8 (TFLOP/s)", "value": tf, "unit": "TFLOP/s",
+           "higher_is_better": True, "n_gpus": 1, "data": "synthetic", "dtype": "bf16",
+           "config": {"workload": "gemm", "n_img": n_img, "n_ref": n_ref, "n_pix": n_pix,
+                      "tiles": tiles * ((n_img + 127) // 128)},
+           "ms_per_launch": k_ms, "launches_ms": ms,
+           "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s",
+                        "frac": tf / peak, "peak_source": f"bf16_tflops ({peak_src}, burst)"}}
+    print(json.dumps(out), flush=True)
+
+
 def run_merge(args):
     """Autocorrelation merge at 151^3 with 2,000 frames x 65,536 pixels
     (1.31e8 points): setup (two type-1 NUFFTs), then 30 CG iterations in the
@@ -959,7 +1020,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--workload", default="match",
                     choices=["match", "merge", "serving", "nufft", "phasing", "eval",
-                             "ingest"])
+                             "ingest", "gemm"])
     args = ap.parse_args()
     if args.workload == "merge":
         run_merge(args)
@@ -975,6 +1036,9 @@ def main():
         return
     if args.workload == "ingest":
         run_ingest(args)
+        return
+    if args.workload == "gemm":
+        run_gemm(args)
         return
     if args.workload == "serving":
         WORKLOAD.update(name="om-serving-200k", n_ref=200_000, n_img=20_000)
