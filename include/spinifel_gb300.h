@@ -392,12 +392,14 @@ int spf_cg_solve(spf_merge merge, int form, const double *d_b, double *d_x, int 
  * The precision form of SNM.euclidean_dist + argmin
  * (spinifel/sequential/orientation_matching.py:98-109,179): x.s on tcgen05
  * tensor cores from bf16 copies (FP32 accumulation), the 8 smallest
- * s2 - 2 x.s per image and 256-reference tile written to the candidate
- * buffers d_cand_d / d_cand_i, each tiles * n_img * 8 entries with
- * tiles = spf_dist_topk_bf16_tiles(n_ref) (scratch owned by the caller).
- * Rows are ld bf16 elements apart (ld >= n_pix, ld % 8 == 0, pad with 0).
- * Needs sm_103 (GB300). */
+ * s2 - 2 x.s per image and reference tile (tile t holds references
+ * [t * R, (t + 1) * R), R = spf_dist_topk_bf16_tile_refs() = 224) written
+ * to the candidate buffers d_cand_d / d_cand_i, each tiles * n_img * 8
+ * entries with tiles = spf_dist_topk_bf16_tiles(n_ref) (scratch owned by the
+ * caller).  Rows are ld bf16 elements apart (ld >= n_pix, ld % 8 == 0, pad
+ * with 0).  Needs sm_103 (GB300). */
 int64_t spf_dist_topk_bf16_tiles(int64_t n_ref);
+int64_t spf_dist_topk_bf16_tile_refs(void);
 int spf_dist_topk_bf16(const void *d_img_bf16, int64_t n_img, const void *d_ref_bf16,
                        int64_t n_ref, int64_t n_pix, int64_t ld, const float *d_ref_sq,
                        float *d_cand_d, int32_t *d_cand_i, void *stream);
@@ -501,7 +503,7 @@ int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img, const void *d_r
  * caller completes uncertified frames), but all scratch lives in a static
  * device array of the library: 16 MiB + 16 KiB + 256 B held by every GPU
  * that loads the library until the process exits.  Limits per call: n_img <=
- * SPF_STATIC_MAX_FRAMES and ceil(n_ref/256) * n_img <=
+ * SPF_STATIC_MAX_FRAMES and spf_dist_topk_bf16_tiles(n_ref) * n_img <=
  * SPF_STATIC_MAX_TILE_FRAMES; larger calls are rejected with SPF_ERR_ARG.
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) and sets the kernel's shared-memory limit; make it

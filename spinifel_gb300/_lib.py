@@ -104,6 +104,7 @@ SIGNATURES = {
                             _c_void_p, _c_void_p],
     "spf_best_unpack": [_c_void_p, _i64, _c_void_p, _c_void_p, _c_void_p],
     "spf_dist_topk_bf16_tiles": [_i64],
+    "spf_dist_topk_bf16_tile_refs": [],
     "spf_dist_topk_bf16": [_c_void_p, _i64, _c_void_p, _i64, _i64, _i64, _c_void_p, _c_void_p,
                            _c_void_p, _c_void_p],
     "spf_rerank_fp32": [_c_void_p, _c_void_p, _i64, _c_void_p, _c_void_p, _i64, _c_void_p,
@@ -194,6 +195,7 @@ _RESTYPES = {
     "spf_last_error": ctypes.c_char_p,
     "spf_launch_count": ctypes.c_uint64,
     "spf_dist_topk_bf16_tiles": ctypes.c_int64,
+    "spf_dist_topk_bf16_tile_refs": ctypes.c_int64,
     "spf_serve_clock": ctypes.c_double,
 }
 

@@ -4,13 +4,14 @@
 //
 // Distance: dist(i, r) = ||x_i||^2 + ||s_r||^2 - 2 x_i . s_r.  The x.s term is
 // a GEMM X[n_img, K] . S[n_ref, K]^T, both operands K-major bf16.  One CTA
-// (persistent, one per SM) computes 128 x 256 tiles (images x references):
-//   warp 0   : TMA producer, 4-stage ring of (A 16 KB + B 32 KB) k-blocks of
+// (persistent, one per SM) computes 128 x 224 tiles (images x references):
+//   warp 0   : TMA producer, 5-stage ring of (A 16 KB + B 28 KB) k-blocks of
 //              64 pixels, 128-byte swizzle;
-//   warp 1   : allocates 512 TMEM columns (two 128 x 256 FP32 accumulators)
-//              and issues tcgen05.mma kind::f16 (M128 N256 K16) from one lane;
+//   warp 1   : allocates 512 TMEM columns (two 128 x 224 FP32 accumulators,
+//              256 columns apart) and issues tcgen05.mma kind::f16 (M128 N224
+//              K16) from one lane;
 //   warps 2-5: epilogue -- each thread owns one image row (TMEM lane), reads
-//              its 256 accumulators with tcgen05.ld, forms s2 - 2 acc and keeps
+//              its 224 accumulators with tcgen05.ld, forms s2 - 2 acc and keeps
 //              the 8 smallest (ties to the lower index), then writes them to
 //              the candidate buffer cand[n_tile][image][8].
 // Accumulators are double-buffered so the epilogue of tile t overlaps the
@@ -38,9 +39,14 @@ namespace spf {
 namespace bf16mm {
 
 constexpr int BM = 128;
-constexpr int BN = 256;
+// 224 references per tile: a stage (A 16 KB + B 28 KB) leaves room for five
+// stages in the 227 KB of shared memory a CTA may hold, one more than 256-row
+// tiles allow, and the deeper ring rides out more of the L2-miss latency of
+// the TMA loads (the tensor pipe idled a quarter of the cycles with four).
+constexpr int BN = 224;
 constexpr int BK = 64;  // bf16 elements = 128 bytes = one swizzle atom row
-constexpr int STAGES = 4;
+constexpr int STAGES = 5;
+constexpr int ACC_STRIDE = 256;  // TMEM columns between the two accumulators
 constexpr int A_BYTES = BM * BK * 2;
 constexpr int B_BYTES = BN * BK * 2;
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
@@ -50,6 +56,12 @@ constexpr int GROUP_M = 16;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint64_t TIMEOUT_NS = 1000000000ull;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+static_assert(SMEM_BYTES <= 227 * 1024, "one CTA's shared memory");
+static_assert(BN % 16 == 0 && BN <= 256 && BN <= ACC_STRIDE && 2 * ACC_STRIDE <= 512,
+              "MMA N and the two TMEM accumulators");
+static_assert((STAGES * A_BYTES) % 1024 == 0 && B_BYTES % 1024 == 0 && A_BYTES % 1024 == 0,
+              "128-byte-swizzled stages start on 1024-byte boundaries");
+static_assert(2 * STAGES * 8 + 5 * 8 + 8 <= 256, "barriers, TMEM slot and abort flag");
 
 // Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
 // (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
@@ -302,7 +314,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         uint32_t b = tc & 1, use = tc >> 1;
         if (!mbar_wait(&acc_empty[b], (use & 1) ^ 1, abort)) break;
         tc_fence_after();
-        uint32_t d_tmem = tmem_base + b * BN;
+        uint32_t d_tmem = tmem_base + b * ACC_STRIDE;
         for (int kb = 0; kb < nkb; ++kb, ++it) {
           int s = it % STAGES;
           uint32_t ph = (it / STAGES) & 1;
@@ -350,7 +362,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll 1
         for (int c = 0; c < BN / 32; ++c) {
           uint32_t r[32];
-          tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + b * BN + c * 32, r);
+          tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + b * ACC_STRIDE + c * 32, r);
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             int64_t col = col0 + c * 32 + j;
@@ -371,7 +383,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll 1
         for (int c = 0; c < BN / 32; ++c) {
           uint32_t r[32];
-          tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + b * BN + c * 32, r);
+          tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + b * ACC_STRIDE + c * 32, r);
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             int64_t col = col0 + c * 32 + j;
@@ -968,6 +980,8 @@ extern "C" {
 
 int64_t spf_dist_topk_bf16_tiles(int64_t n_ref) { return (n_ref + BN - 1) / BN; }
 
+int64_t spf_dist_topk_bf16_tile_refs(void) { return BN; }
+
 static int launch_bf16(bool range, const void *d_img_bf16, int64_t n_img, const void *d_ref_bf16,
                        int64_t n_ref, int64_t n_pix, int64_t ld, const float *d_ref_sq,
                        float *d_cand_d, int32_t *d_cand_i, const float *d_thresh,
@@ -1440,7 +1454,7 @@ extern "C" int spf_match_bf16_static(const void *d_img_bf16, const float *d_img,
               "%s: %lld frames exceed the static scratch limit of %lld frames per call", name,
               (long long)n_img, (long long)STATIC_MAX_FRAMES);
   SPF_REQUIRE(tiles * n_img <= STATIC_MAX_TILE_FRAMES,
-              "%s: ceil(n_ref/256) * n_img = %lld exceeds the static scratch limit of %lld "
+              "%s: ceil(n_ref/224) * n_img = %lld exceeds the static scratch limit of %lld "
               "(split the references or the frames)",
               name, (long long)(tiles * n_img), (long long)STATIC_MAX_TILE_FRAMES);
   SPF_REQUIRE(d_img_bf16 && d_img && d_img_sq && d_ref_bf16 && d_ref && d_ref_sq && d_ref_m2 &&

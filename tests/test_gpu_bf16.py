@@ -31,7 +31,7 @@ def _raw_candidates(frames, refs):
 
 
 @pytest.mark.parametrize("shape", [(128, 256, 64), (130, 600, 256), (300, 1000, 1000),
-                                   (7, 3, 8)])
+                                   (7, 3, 8), (129, 224, 72), (64, 449, 200)])
 def test_tcgen05_tile_topk_matches_torch(dev, shape):
     from spinifel_gb300 import matching
 
@@ -48,8 +48,12 @@ def test_tcgen05_tile_topk_matches_torch(dev, shape):
     approx = rs.sq.double()[None, :] - 2.0 * xb @ sb.T  # [n_img, n_ref]
     scale = float(approx.abs().max())
     tiles = cd.shape[0]
+    from spinifel_gb300 import _lib
+
+    tile_refs = int(_lib.lib().spf_dist_topk_bf16_tile_refs())
+    assert tiles == -(-n_ref // tile_refs)
     for t in range(tiles):
-        lo, hi = t * 256, min((t + 1) * 256, n_ref)
+        lo, hi = t * tile_refs, min((t + 1) * tile_refs, n_ref)
         k = min(8, hi - lo)
         ref_vals, ref_idx = torch.sort(approx[:, lo:hi], dim=1, stable=True)
         got_d = cd[t, :, :k].double()

@@ -129,7 +129,7 @@ def test_static_scratch_entry_point_rejects_oversize(lib):
                                  ctypes.c_void_p(16), None, None, None)
     assert st == _lib.SPF_ERR_ARG
     assert b"static scratch limit" in L.spf_last_error()
-    # 2000 frames x 200,000 references: 782 tiles * 2000 > 262,144
+    # 2000 frames x 200,000 references: 893 tiles * 2000 > 262,144
     st = L.spf_match_bf16_static(ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16),
                                  2000, ctypes.c_void_p(16), ctypes.c_void_p(16),
                                  ctypes.c_void_p(16), ctypes.c_void_p(16), 1.0, 200_000, 64, 64,
