@@ -1454,9 +1454,9 @@ extern "C" int spf_match_bf16_static(const void *d_img_bf16, const float *d_img,
               "%s: %lld frames exceed the static scratch limit of %lld frames per call", name,
               (long long)n_img, (long long)STATIC_MAX_FRAMES);
   SPF_REQUIRE(tiles * n_img <= STATIC_MAX_TILE_FRAMES,
-              "%s: ceil(n_ref/224) * n_img = %lld exceeds the static scratch limit of %lld "
+              "%s: ceil(n_ref/%d) * n_img = %lld exceeds the static scratch limit of %lld "
               "(split the references or the frames)",
-              name, (long long)(tiles * n_img), (long long)STATIC_MAX_TILE_FRAMES);
+              name, BN, (long long)(tiles * n_img), (long long)STATIC_MAX_TILE_FRAMES);
   SPF_REQUIRE(d_img_bf16 && d_img && d_img_sq && d_ref_bf16 && d_ref && d_ref_sq && d_ref_m2 &&
                   d_idx,
               "%s: NULL pointer", name);
