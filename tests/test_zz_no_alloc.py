@@ -79,6 +79,49 @@ def test_static_scratch_entry_point_matches_allocating_path(lib):
         assert torch.equal(unc, runc)
 
 
+def test_static_scratch_call_replays_from_a_cuda_graph(lib):
+    """The static entry point recorded in a CUDA graph (after a first call on
+    the device, which looks up the scratch and sets the kernel attributes)
+    and replayed on new frame contents copied into the same buffers gives
+    exactly the allocating path's answer for those frames."""
+    from spinifel_gb300 import _lib, matching
+
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(92)
+    n_ref, n_pix, n = 2000, 1024, 150
+    refs = rng.gamma(0.5, 1.0, (n_ref, n_pix)).astype(np.float32)
+    rs = matching.ReferenceSet(torch.as_tensor(refs, device=dev))
+
+    def frames():
+        pick = rng.integers(0, n_ref, n)
+        x = torch.as_tensor(rng.poisson(refs[pick]).astype(np.float32), device=dev)
+        return matching.FrameSet(x)
+
+    fr, fr_b = frames(), frames()
+    out = (torch.empty(n, dtype=torch.int32, device=dev),
+           torch.empty(n, dtype=torch.float32, device=dev),
+           torch.empty(n, dtype=torch.int32, device=dev))
+    _static(_lib, fr, rs, *out)  # first call on the device: outside the capture
+    L = _lib
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        L.call("spf_match_bf16_static", L.ptr(fr.bf16), L.ptr(fr.f32), L.ptr(fr.sq), fr.n,
+               L.ptr(rs.bf16), L.ptr(rs.f32), L.ptr(rs.sq), L.ptr(rs.m2), float(rs.sq_max),
+               rs.n_ref, rs.n_pix, rs.ld, L.ptr(out[0]), L.ptr(out[1]), L.ptr(out[2]),
+               L.stream_handle())
+    fr.f32.copy_(fr_b.f32)
+    fr.bf16.copy_(fr_b.bf16)
+    fr.sq.copy_(fr_b.sq)
+    g.replay()
+    torch.cuda.synchronize()
+    code = ctypes.c_int(-1)
+    _lib.call("spf_device_error", _lib.stream_handle(), ctypes.byref(code))
+    assert code.value == 0
+    ridx, rdist, runc = _allocating(_lib, fr_b, rs)
+    assert torch.equal(out[0], ridx) and torch.equal(out[1], rdist)
+    assert torch.equal(out[2], runc)
+
+
 def test_static_scratch_abort_is_reported_and_voids_the_call(lib):
     """A GEMM that gave up a bounded wait (recorded by the library's test hook
     right after the GEMM, as the kernel's own timeout path records it): every
