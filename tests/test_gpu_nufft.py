@@ -422,3 +422,71 @@ def test_sorted_pass_item_size_keeps_the_operator(dev):
     matching.check_device_error()
     for n in (512, 1024, 4096, 8192):
         assert rel(res[n], res[0]) < 1e-6
+
+
+# Every kernel width the FP32 plan compiles (w = ceil(-log10(eps / 10)): 3 .. 8),
+# not only the w = 7 of eps 1e-6: type 2 and type 1 against the direct sums with
+# a tolerance that follows eps (the kernel's error) above FP32's floor, the
+# bin-sorted spreading against the per-point spreading, and the patch slicing
+# (every tile shape, the stride search included) bit for bit against the
+# per-point slicing.
+WIDTH_EPS = [(1e-2, 3), (1e-3, 4), (1e-4, 5), (1e-5, 6), (1e-7, 8)]
+
+
+def _width_tol(eps):
+    return max(20.0 * eps, 1e-5)
+
+
+@pytest.mark.parametrize("eps,w", WIDTH_EPS)
+def test_type2_and_type1_every_width(dev, eps, w):
+    from spinifel_gb300.nufft import NufftPlan
+
+    rng = np.random.default_rng(60 + w)
+    m = (13, 12, 11)
+    P = NufftPlan(m, eps)
+    assert P.width == w
+    f = rng.standard_normal(m)
+    x, y, z = rng.uniform(-3 * np.pi + 1e-3, 3 * np.pi - 1e-3, (3, 2000)).astype(np.float32)
+    P.set_modes(t(f, dev), isign=-1, want_imag=True)
+    re, im = P.interp(t(x, dev), t(y, dev), t(z, dev), want_imag=True)
+    got = re.cpu().numpy() + 1j * im.cpu().numpy()
+    assert rel(got, onufft.nudft3d2(x, y, z, f, -1)) < _width_tol(eps)
+    c = rng.standard_normal(2000).astype(np.float32)
+    P.spread_zero()
+    P.spread(t(x, dev), t(y, dev), t(z, dev), t(c, dev))
+    re1, im1 = P.finish(+1, want_imag=True)
+    exact1 = onufft.nudft3d1(x, y, z, c, m, +1)
+    g1 = re1.cpu().numpy() + 1j * im1.cpu().numpy()
+    assert rel(g1, exact1) < _width_tol(eps)
+    # the bin-sorted pass over the same points gives the same sums (up to the
+    # order of the float additions)
+    P.sort_points(t(x, dev), t(y, dev), t(z, dev))
+    P.spread_zero()
+    P.spread_sorted(t(c, dev))
+    re2, im2 = P.finish(+1, want_imag=True)
+    g2 = re2.cpu().numpy() + 1j * im2.cpu().numpy()
+    assert rel(g2, g1) < 1e-5
+
+
+@pytest.mark.parametrize("eps,w", WIDTH_EPS)
+def test_patch_slicing_every_width_and_shape(dev, eps, w):
+    from spinifel_gb300 import _lib
+    from spinifel_gb300.nufft import NufftPlan
+
+    det = (2, 20, 37)
+    model, ppr, pdr, quats = _slice_case(41, det, 24, 30 + w)
+    ppr_t = t(ppr.reshape(3, -1), dev)
+    P = NufftPlan(41, eps)
+    assert P.width == w
+    P.set_modes(t(model, dev))
+    mult = np.pi / pdr.max()
+    a = P.slice(t(quats, dev), ppr_t, mult)
+    exact = _oracle_slices(model, ppr, pdr, quats)
+    assert rel(a.cpu().numpy().astype(np.float64), exact) < _width_tol(eps)
+    try:
+        for shape in range(8):
+            _lib.call("spf_tune_set", _lib.SPF_TUNE_SLICE_SHAPE, shape)
+            b = P.slice(t(quats, dev), ppr_t, mult, det_shape=det)
+            assert torch.equal(a, b), shape
+    finally:
+        _lib.call("spf_tune_set", _lib.SPF_TUNE_SLICE_SHAPE, 0)
