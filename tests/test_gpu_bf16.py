@@ -170,3 +170,27 @@ def test_autotuner_picks_a_candidate_and_never_changes_results(dev, tmp_path, mo
     finally:
         _lib.call("spf_tune_set", _lib.SPF_TUNE_BF16_GROUP_M, 0)
         _lib.call("spf_tune_set", _lib.SPF_TUNE_BF16_GRID, 0)
+
+
+def test_bf16_paths_accept_empty_inputs(dev):
+    """No frames: the tensor-core path, the one-call host path and the static
+    entry point all return empty answers (and launch nothing that fails)."""
+    import ctypes
+
+    from spinifel_gb300 import _lib, matching
+
+    g = torch.Generator(device="cpu").manual_seed(41)
+    rs = matching.ReferenceSet(torch.rand(300, 64, generator=g).to(dev))
+    fr = matching.FrameSet(torch.empty(0, 64, device=dev))
+    idx, dist = matching.match_bf16(fr, rs)
+    assert idx.numel() == 0 and dist.numel() == 0
+    h_idx, h_dist = matching.match_bf16_host(torch.empty(0, 64, dtype=torch.int16).pin_memory(),
+                                             rs)
+    assert h_idx.size == 0 and h_dist.size == 0
+    L = _lib.lib()
+    assert L.spf_match_bf16_static(ctypes.c_void_p(16), ctypes.c_void_p(16),
+                                   ctypes.c_void_p(16), 0, ctypes.c_void_p(16),
+                                   ctypes.c_void_p(16), ctypes.c_void_p(16),
+                                   ctypes.c_void_p(16), 1.0, 300, 64, 64, ctypes.c_void_p(16),
+                                   None, None, None) == _lib.SPF_OK
+    matching.check_device_error()
