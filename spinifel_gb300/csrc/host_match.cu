@@ -168,6 +168,16 @@ extern "C" int spf_match_bf16_host(const uint16_t *h_counts, int64_t n_img,
                                   0, work + r0, idx + r0, dist + r0, unc + r0, mrg_d + r0 * 8,
                                   mrg_i + r0 * 8, sv);
     }
+    // the caller's stream waits for everything queued on the copy and ingest
+    // streams, also after an error, so that no copy can outlive the scratch
+    // (whose frees are ordered on s) or the caller's host buffer
+    for (cudaStream_t x : {cs, is}) {
+      cudaEvent_t joined = nullptr;
+      if (x && cudaEventCreateWithFlags(&joined, cudaEventDisableTiming) == cudaSuccess) {
+        ev.push_back(joined);
+        if (cudaEventRecord(joined, x) == cudaSuccess) cudaStreamWaitEvent(s, joined, 0);
+      }
+    }
     // results and the open frames back to the host
     std::vector<int32_t> h_unc(n_img);
     std::vector<float> h_d(h_dist ? 0 : n_img);
