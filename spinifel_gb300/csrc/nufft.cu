@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "tma.cuh"
 #include "es_params.cuh"
 
 struct spf_nufft_plan_s {
@@ -1012,13 +1013,15 @@ __global__ void __launch_bounds__(SORTED_THREADS, 4)
                            GridGeom g, BinDims bd, const int4 *__restrict__ items,
                            const int32_t *__restrict__ sorted, PointSrc src, float s1, float s2,
                            float s3, const float *__restrict__ weights,
+                           const __grid_constant__ CUtensorMap tmap, int use_tma,
                            unsigned int *__restrict__ err) {
   static_assert(W <= 8, "eight lanes per footprint row, two rows per lane");
   constexpr int D = BIN + W - 1;
   constexpr int SR = SORTED_ROW_STRIDE;
   constexpr int SP = D * SR;
   static_assert(D <= SR, "row stride holds a footprint row");
-  __shared__ float tbox[INTERP ? D * SP : 1];
+  __shared__ __align__(128) float tbox[INTERP ? D * SP : 1];
+  __shared__ __align__(8) uint64_t tbar;
   __shared__ float abox[D * SP];
   __shared__ float4 pt_tw[SORTED_THREADS];  // per warp: 32 prepared points
   __shared__ int pt_key[SORTED_THREADS];
@@ -1028,9 +1031,35 @@ __global__ void __launch_bounds__(SORTED_THREADS, 4)
   const int i0b = bi * BIN, j0b = bj * BIN, k0b = bk * BIN;
   const int di = min(D, g.p1 - i0b), dj = min(D, g.p2 - j0b), dk = min(D, g.p3 - k0b);
   const BoxShape shape{i0b, j0b, k0b, di, dj, dk, SP, SR};
-  if (INTERP) box_load(tbox, re_pad, g, shape);
+  // the bin's box is a regular tile of the padded grid: one TMA copy of
+  // D x D x SR floats (the row stride's extra cells and cells past the grid
+  // end come along or read as zero; no footprint reaches them), else a
+  // cooperative load
+  if (INTERP) {
+    if (use_tma) {
+      if (threadIdx.x == 0) {
+        mbar_init(&tbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_arrive_expect_tx(&tbar, (uint32_t)(D * SP * sizeof(float)));
+        tma_load_3d(tbox, &tmap, &tbar, k0b, j0b, i0b);
+      }
+    } else {
+      box_load(tbox, re_pad, g, shape);
+    }
+  }
   box_rows(shape, [&](int, int, int, int s) { abox[s] = 0.0f; });
   __syncthreads();
+  if (INTERP && use_tma) {
+    constexpr uint64_t TMA_TIMEOUT_NS = 1000000000ull;
+    const bool late = !mbar_wait_for(&tbar, 0, TMA_TIMEOUT_NS);
+    if (__syncthreads_or(late)) {
+      // the copy gave no sign within the bound: report it, let it land, and
+      // leave the item out
+      if (threadIdx.x == 0 && err) atomicExch(err, (unsigned int)(-SPF_ERR_TIMEOUT));
+      mbar_wait_for(&tbar, 0, TMA_TIMEOUT_NS);
+      return;
+    }
+  }
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int grp = lane >> 3;  // row set of the lane; kernel axis for the weights
@@ -1644,18 +1673,33 @@ static int sorted_pass(spf_nufft_plan P, const float *d_weights, bool interp, co
   float s3 = (float)(P->s_scale * P->n[2] / (2.0 * M_PI));
   SPF_REQUIRE(P->n_items < (1LL << 31), "%s: too many items", what);
   const PointSrc src{P->s_quats, P->s_ppr, P->s_n_pix, P->s_x, P->s_y, P->s_z};
+  // TMA map of the padded grid for the bins' boxes (rows are 16-byte aligned)
+  CUtensorMap tmap;
+  memset(&tmap, 0, sizeof(tmap));
+  int use_tma = 0;
+  auto encode = tensor_map_encoder();
+  if (interp && (g.p3 & 3) == 0 && encode) {
+    const int D = BIN + P->w - 1;
+    cuuint64_t dims[3] = {(cuuint64_t)g.p3, (cuuint64_t)g.p2, (cuuint64_t)g.p1};
+    cuuint64_t strides[2] = {(cuuint64_t)g.p3 * sizeof(float),
+                             (cuuint64_t)g.p3 * g.p2 * sizeof(float)};
+    cuuint32_t box[3] = {(cuuint32_t)SORTED_ROW_STRIDE, (cuuint32_t)D, (cuuint32_t)D};
+    cuuint32_t estr[3] = {1, 1, 1};
+    use_tma = encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, P->re_pad, dims, strides, box,
+                     estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  }
   if (interp) {
     SPF_W_DISPATCH(P->w, (k_interp_spread_sorted<W, true>
                           <<<(unsigned)P->n_items, SORTED_THREADS, 0, s>>>(
                               P->re_pad, P->acc_pad, g, bd, P->items, P->sorted, src, s1, s2,
-                              s3, d_weights,
-                              device_error_word())));
+                              s3, d_weights, tmap, use_tma, device_error_word())));
   } else {
     SPF_W_DISPATCH(P->w, (k_interp_spread_sorted<W, false>
                           <<<(unsigned)P->n_items, SORTED_THREADS, 0, s>>>(
                               P->re_pad, P->acc_pad, g, bd, P->items, P->sorted, src, s1, s2,
-                              s3, d_weights,
-                              device_error_word())));
+                              s3, d_weights, tmap, 0, device_error_word())));
   }
   return check_launch(what);
 }
